@@ -1,0 +1,368 @@
+"""GB300 (sm_103a) backend for the FHEW/AP gate-bootstrapping path of
+zhehongw/3rd_Gen_FHE_ACC.
+
+Python host side over the C ABI of libfheacc.so (include/fheacc.h). It keeps
+the names and the argument meaning of the reference runtime's host API:
+key generation (LWE::LWE_secretkey, RLWE::RLWE_secretkey, RLWE::bootstrap_key,
+LWE::keyswitch_key, application::substitute_key), LWE_encrypt / LWE_decrypt,
+RLWE::eval_bootstrap, and the FPGA backend's fixed-width gate calls
+fpga_eval_bootstrap_x1/x4/x8/x12/x16 (FHE_ACC_runtime/include/myfpga.h:287-331),
+here served by the GPU. Ciphertexts and keys are numpy uint64 arrays in the
+reference's layouts (see include/fheacc.h).
+
+The package imports as importlib.import_module("3rd_gen_fhe_acc_gb300").
+The shared library must be built first (build.py, or __graft_entry__.build());
+nothing here falls back to a CPU implementation.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfheacc.so")
+
+OR, AND, NOR, NAND, XOR, XNOR = range(6)
+GATES = {"OR": OR, "AND": AND, "NOR": NOR, "NAND": NAND, "XOR": XOR, "XNOR": XNOR}
+FLAG_FPGA_COMPAT = 1
+
+OK = 0
+EINVAL, ENOMEM, ENODEV, EIO, ETIMEDOUT, ENOKEY, EBUSY = -22, -12, -19, -5, -110, -126, -16
+
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_i32p = ctypes.POINTER(ctypes.c_int32)
+
+
+class Params(ctypes.Structure):
+    """fheacc_params (include/fheacc.h); the reference's globals, params.h:11-134."""
+    _fields_ = [
+        ("n", ctypes.c_int32), ("q", ctypes.c_uint32), ("N", ctypes.c_int32), ("nbit", ctypes.c_uint32),
+        ("Q", ctypes.c_uint64),
+        ("BG_bits", ctypes.c_uint32), ("digitG", ctypes.c_uint32), ("Br", ctypes.c_uint32),
+        ("digitR", ctypes.c_uint32), ("Bks", ctypes.c_uint32), ("digitKS", ctypes.c_uint32),
+        ("Bks_R_bits", ctypes.c_uint32), ("digitKS_R", ctypes.c_uint32),
+        ("gate_constant", ctypes.c_uint64 * 6),
+        ("iN", ctypes.c_uint64), ("ROU", ctypes.c_uint64), ("E", ctypes.c_uint32), ("E_rlwe", ctypes.c_uint32),
+    ]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["gate_constant"] = list(self.gate_constant)
+        return d
+
+
+class FheaccError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("fheacc error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """The loaded libfheacc.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FheaccError(ENODEV, "libfheacc.so is not built (run __graft_entry__.build())")
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.POINTER(Params)
+        vp = ctypes.c_void_p
+        sz = ctypes.c_size_t
+        sig = {
+            "fheacc_params_preset": (ctypes.c_int, [ctypes.c_int, P]),
+            "fheacc_params_derive": (ctypes.c_int, [P]),
+            "fheacc_bootstrap_key_words": (sz, [P]),
+            "fheacc_lwe_ks_key_words": (sz, [P]),
+            "fheacc_subs_key_words": (sz, [P]),
+            "fheacc_twiddle_tables": (ctypes.c_int, [P, _u64p, _u64p]),
+            "fheacc_keygen_lwe_sk": (ctypes.c_int, [P, ctypes.c_uint64, _u64p]),
+            "fheacc_keygen_rlwe_sk": (ctypes.c_int, [P, ctypes.c_uint64, _u64p]),
+            "fheacc_keygen_bootstrap_key": (ctypes.c_int, [P, ctypes.c_uint64, _u64p, _u64p, _u64p, ctypes.c_int]),
+            "fheacc_keygen_lwe_ks_key": (ctypes.c_int, [P, ctypes.c_uint64, _u64p, _u64p, _u64p, ctypes.c_int]),
+            "fheacc_keygen_subs_key": (ctypes.c_int, [P, ctypes.c_uint64, _u64p, _u64p, ctypes.c_int]),
+            "fheacc_lwe_encrypt": (ctypes.c_int, [P, ctypes.c_uint64, _u64p, _u8p, sz, _u64p]),
+            "fheacc_lwe_decrypt": (ctypes.c_int, [P, _u64p, _u64p, sz, _u8p]),
+            "fheacc_rlwe_encrypt": (ctypes.c_int, [P, ctypes.c_uint64, _u64p, _u64p, _u64p]),
+            "fheacc_rlwe_phase": (ctypes.c_int, [P, _u64p, _u64p, _u64p]),
+            "fheacc_create": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(vp)]),
+            "fheacc_destroy": (ctypes.c_int, [vp]),
+            "fheacc_last_error": (ctypes.c_char_p, [vp]),
+            "fheacc_get_params": (ctypes.c_int, [vp, P]),
+            "fheacc_device_bytes": (sz, [vp]),
+            "fheacc_upload_bootstrap_key": (ctypes.c_int, [vp, _u64p, sz]),
+            "fheacc_upload_lwe_ks_key": (ctypes.c_int, [vp, _u64p, sz]),
+            "fheacc_upload_subs_key": (ctypes.c_int, [vp, _u64p, sz]),
+            "fheacc_bootstrap": (ctypes.c_int, [vp, _u64p, _u64p, _i32p, sz, _u64p, ctypes.c_uint32]),
+            "fheacc_bootstrap_async": (ctypes.c_int, [vp, vp, vp, vp, sz, vp, ctypes.c_uint32, vp]),
+            "fheacc_bootstrap_plain_async": (ctypes.c_int, [vp, vp, vp, vp, sz, vp, ctypes.c_uint32, vp]),
+            "fheacc_ntt_forward": (ctypes.c_int, [vp, vp, sz, vp]),
+            "fheacc_ntt_inverse": (ctypes.c_int, [vp, vp, sz, vp]),
+            "fheacc_rlwe_mult_rgsw": (ctypes.c_int, [vp, vp, vp, vp, sz, vp]),
+            "fheacc_blind_rotate_async": (ctypes.c_int, [vp, vp, vp, vp, sz, vp, ctypes.c_uint32, vp]),
+            "fheacc_lwe_keyswitch_async": (ctypes.c_int, [vp, vp, sz, vp, vp]),
+            "fheacc_lwe_modswitch_async": (ctypes.c_int, [vp, vp, sz, vp, vp]),
+            "fheacc_sync": (ctypes.c_int, [vp, ctypes.c_uint32]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p64(a):
+    assert a.dtype == np.uint64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_u64p)
+
+
+def _check(rc, ctx=None):
+    if rc != OK:
+        msg = lib().fheacc_last_error(ctx)
+        raise FheaccError(rc, msg.decode() if msg else "")
+
+
+def params_preset(preset=0):
+    """Parameter preset 0 (N=1024, Q<2^27, n=500), 1 (N=2048, Q<2^54, n=630) or
+    2 (the reference CPU app's set, fhe_wo_fpga.cpp:35-146)."""
+    p = Params()
+    _check(lib().fheacc_params_preset(preset, ctypes.byref(p)))
+    return p
+
+
+def derive(p):
+    _check(lib().fheacc_params_derive(ctypes.byref(p)))
+    return p
+
+
+def bootstrap_key_words(p):
+    return lib().fheacc_bootstrap_key_words(ctypes.byref(p))
+
+
+def lwe_ks_key_words(p):
+    return lib().fheacc_lwe_ks_key_words(ctypes.byref(p))
+
+
+def subs_key_words(p):
+    return lib().fheacc_subs_key_words(ctypes.byref(p))
+
+
+def twiddle_tables(p):
+    rou = np.zeros(p.N, dtype=np.uint64)
+    irou = np.zeros(p.N, dtype=np.uint64)
+    _check(lib().fheacc_twiddle_tables(ctypes.byref(p), _p64(rou), _p64(irou)))
+    return rou, irou
+
+
+# ------------------------------------------------------------ key generation
+def LWE_secretkey(p, seed):
+    """LWE::LWE_secretkey (LWE.cpp:22-53): n ternary words mod q."""
+    sk = np.zeros(p.n, dtype=np.uint64)
+    _check(lib().fheacc_keygen_lwe_sk(ctypes.byref(p), seed, _p64(sk)))
+    return sk
+
+
+def RLWE_secretkey(p, seed):
+    """RLWE::RLWE_secretkey (RLWE.cpp:243-279): the NTT-domain poly a."""
+    sk = np.zeros(p.N, dtype=np.uint64)
+    _check(lib().fheacc_keygen_rlwe_sk(ctypes.byref(p), seed, _p64(sk)))
+    return sk
+
+
+def bootstrap_key(p, seed, lwe_sk, rlwe_sk, threads=0):
+    """RLWE::bootstrap_key (RLWE.cpp:579-606), layout [Br][digitR][n][digitG][2][2][N]."""
+    bt = np.zeros(bootstrap_key_words(p), dtype=np.uint64)
+    _check(lib().fheacc_keygen_bootstrap_key(ctypes.byref(p), seed, _p64(lwe_sk), _p64(rlwe_sk), _p64(bt), threads))
+    return bt
+
+
+def keyswitch_key(p, seed, rlwe_sk, lwe_sk, threads=0):
+    """LWE::keyswitch_key (LWE.cpp:55-106), layout [Bks][digitKS][N][n+1]."""
+    ks = np.zeros(lwe_ks_key_words(p), dtype=np.uint64)
+    _check(lib().fheacc_keygen_lwe_ks_key(ctypes.byref(p), seed, _p64(rlwe_sk), _p64(lwe_sk), _p64(ks), threads))
+    return ks
+
+
+def substitute_key(p, seed, rlwe_sk, threads=0):
+    """application::substitute_key (app.cpp:4-24), layout [log2 N][digitKS_R][2][N]."""
+    sk = np.zeros(subs_key_words(p), dtype=np.uint64)
+    _check(lib().fheacc_keygen_subs_key(ctypes.byref(p), seed, _p64(rlwe_sk), _p64(sk), threads))
+    return sk
+
+
+def LWE_encrypt(p, seed, lwe_sk, bits):
+    """LWE::LWE_encrypt (LWE.cpp:108-146) of bits with t = 4; [count][n+1]."""
+    bits = np.ascontiguousarray(np.asarray(bits, dtype=np.uint8).reshape(-1))
+    out = np.zeros((bits.size, p.n + 1), dtype=np.uint64)
+    _check(lib().fheacc_lwe_encrypt(ctypes.byref(p), seed, _p64(lwe_sk), bits.ctypes.data_as(_u8p), bits.size,
+                                    _p64(out)))
+    return out
+
+
+def LWE_decrypt(p, lwe_sk, ct):
+    """LWE::LWE_decrypt (LWE.cpp:148-190), t = 4: values in [0, 4)."""
+    ct = np.ascontiguousarray(ct, dtype=np.uint64).reshape(-1, p.n + 1)
+    out = np.zeros(ct.shape[0], dtype=np.uint8)
+    _check(lib().fheacc_lwe_decrypt(ctypes.byref(p), _p64(lwe_sk), _p64(ct), ct.shape[0], out.ctypes.data_as(_u8p)))
+    return out
+
+
+def RLWE_encrypt(p, seed, rlwe_sk, msg_ntt):
+    out = np.zeros(2 * p.N, dtype=np.uint64)
+    msg_ntt = np.ascontiguousarray(msg_ntt, dtype=np.uint64)
+    _check(lib().fheacc_rlwe_encrypt(ctypes.byref(p), seed, _p64(rlwe_sk), _p64(msg_ntt), _p64(out)))
+    return out
+
+
+def RLWE_phase(p, rlwe_sk, ct):
+    out = np.zeros(p.N, dtype=np.uint64)
+    ct = np.ascontiguousarray(ct, dtype=np.uint64)
+    _check(lib().fheacc_rlwe_phase(ctypes.byref(p), _p64(rlwe_sk), _p64(ct), _p64(out)))
+    return out
+
+
+def gate_truth(gate, x, y):
+    """Plaintext truth table of the reference's gates (test.cpp:496-625)."""
+    x = np.asarray(x, dtype=np.uint8)
+    y = np.asarray(y, dtype=np.uint8)
+    return {OR: x | y, AND: x & y, NOR: (x | y) ^ 1, NAND: (x & y) ^ 1, XOR: x ^ y, XNOR: (x ^ y) ^ 1}[gate]
+
+
+# ------------------------------------------------------------------ device
+class Context:
+    """A device context (fheacc_ctx): parameters, twiddles and resident keys.
+
+    Replaces the FPGA slot set-up (OCL_config_wr_rd, BAR1_ROU_table_*_wr,
+    dma_write_*; myfpga.cpp:82-712).
+    """
+
+    def __init__(self, params, device=0):
+        L = lib()
+        h = ctypes.c_void_p()
+        _check(L.fheacc_create(ctypes.byref(params), device, ctypes.byref(h)))
+        self._h = h
+        self.params = Params()
+        _check(L.fheacc_get_params(h, ctypes.byref(self.params)), h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fheacc_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def last_error(self):
+        return lib().fheacc_last_error(self._h).decode()
+
+    def device_bytes(self):
+        return lib().fheacc_device_bytes(self._h)
+
+    def check(self, rc):
+        _check(rc, self._h)
+
+    def upload_bootstrap_key(self, btkey):
+        """dma_write_bootstrap_key (myfpga.cpp:596-656)."""
+        btkey = np.ascontiguousarray(btkey, dtype=np.uint64)
+        self.check(lib().fheacc_upload_bootstrap_key(self._h, _p64(btkey), btkey.size))
+
+    def upload_keyswitch_key(self, kskey):
+        kskey = np.ascontiguousarray(kskey, dtype=np.uint64)
+        self.check(lib().fheacc_upload_lwe_ks_key(self._h, _p64(kskey), kskey.size))
+
+    def upload_subs_key(self, subs):
+        """dma_write_subs_key (myfpga.cpp:658-712)."""
+        subs = np.ascontiguousarray(subs, dtype=np.uint64)
+        self.check(lib().fheacc_upload_subs_key(self._h, _p64(subs), subs.size))
+
+    def eval_bootstrap_batch(self, c1, c2, gates, flags=0):
+        """eval_bootstrap (RLWE.cpp:726-786) of every (c1[i], c2[i], gates[i]),
+        host arrays in, host array out."""
+        w = self.params.n + 1
+        c1 = np.ascontiguousarray(c1, dtype=np.uint64).reshape(-1, w)
+        c2 = np.ascontiguousarray(c2, dtype=np.uint64).reshape(-1, w)
+        g = np.ascontiguousarray(np.asarray(gates, dtype=np.int32).reshape(-1))
+        if g.size == 1 and c1.shape[0] > 1:
+            g = np.full(c1.shape[0], g[0], dtype=np.int32)
+        out = np.zeros_like(c1)
+        self.check(lib().fheacc_bootstrap(self._h, _p64(c1), _p64(c2), g.ctypes.data_as(_i32p), c1.shape[0],
+                                          _p64(out), flags))
+        return out
+
+    def eval_bootstrap(self, c1, c2, gate, flags=0):
+        """RLWE::eval_bootstrap (RLWE.cpp:726) of one gate."""
+        return self.eval_bootstrap_batch(c1, c2, [gate], flags)[0]
+
+    def _fixed(self, width, c1, c2, gates):
+        # fpga_eval_bootstrap_x* check the batch size (myfpga.cpp:1140-1144)
+        if len(c1) != width or len(c2) != width or len(gates) != width:
+            return None, -1
+        try:
+            return list(self.eval_bootstrap_batch(np.array(c1), np.array(c2), gates)), 0
+        except FheaccError as e:
+            return None, e.code
+
+    def gpu_eval_bootstrap_x1(self, c1, c2, gate):
+        """Counterpart of fpga_eval_bootstrap_x1 (myfpga.h:287): (result, rc)."""
+        try:
+            return self.eval_bootstrap(c1, c2, gate), 0
+        except FheaccError as e:
+            return None, e.code
+
+    def gpu_eval_bootstrap_x4(self, c1, c2, gates):
+        return self._fixed(4, c1, c2, gates)
+
+    def gpu_eval_bootstrap_x8(self, c1, c2, gates):
+        return self._fixed(8, c1, c2, gates)
+
+    def gpu_eval_bootstrap_x12(self, c1, c2, gates):
+        return self._fixed(12, c1, c2, gates)
+
+    def gpu_eval_bootstrap_x16(self, c1, c2, gates):
+        return self._fixed(16, c1, c2, gates)
+
+    # device-pointer entry points (ints are raw device addresses, e.g.
+    # torch.Tensor.data_ptr(); stream is a raw cudaStream_t or 0)
+    def bootstrap_async(self, d_c1, d_c2, d_gates, count, d_out, flags=0, stream=0):
+        self.check(lib().fheacc_bootstrap_async(self._h, d_c1, d_c2, d_gates, count, d_out, flags, stream or None))
+
+    def bootstrap_plain_async(self, d_c1, d_c2, d_gates, count, d_out, flags=0, stream=0):
+        self.check(lib().fheacc_bootstrap_plain_async(self._h, d_c1, d_c2, d_gates, count, d_out, flags,
+                                                      stream or None))
+
+    def ntt_forward(self, d_polys, count, stream=0):
+        self.check(lib().fheacc_ntt_forward(self._h, d_polys, count, stream or None))
+
+    def ntt_inverse(self, d_polys, count, stream=0):
+        self.check(lib().fheacc_ntt_inverse(self._h, d_polys, count, stream or None))
+
+    def rlwe_mult_rgsw(self, d_acc, d_rgsw, d_out, count, stream=0):
+        self.check(lib().fheacc_rlwe_mult_rgsw(self._h, d_acc, d_rgsw, d_out, count, stream or None))
+
+    def blind_rotate_async(self, d_c1, d_c2, d_gates, count, d_acc, flags=0, stream=0):
+        self.check(lib().fheacc_blind_rotate_async(self._h, d_c1, d_c2, d_gates, count, d_acc, flags, stream or None))
+
+    def lwe_keyswitch_async(self, d_rlwe, count, d_out, stream=0):
+        self.check(lib().fheacc_lwe_keyswitch_async(self._h, d_rlwe, count, d_out, stream or None))
+
+    def lwe_modswitch_async(self, d_in, count, d_out, stream=0):
+        self.check(lib().fheacc_lwe_modswitch_async(self._h, d_in, count, d_out, stream or None))
+
+    def sync(self, timeout_ms=0):
+        self.check(lib().fheacc_sync(self._h, timeout_ms))

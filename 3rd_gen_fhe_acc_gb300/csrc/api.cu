@@ -1,0 +1,428 @@
+// api.cu -- the C ABI of libfheacc.so (declared in include/fheacc.h): device
+// context, key upload with the one-time device re-layout, and the bootstrap
+// entry points. Replaces the FPGA backend's configuration, DMA and issue loop
+// (FHE_ACC_runtime/src/myfpga.cpp:82-1660).
+#include "ctx.hpp"
+#include "host/host_math.hpp"
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <new>
+#include <thread>
+#include <vector>
+
+using namespace fheacc;
+
+static thread_local std::string g_create_error;
+
+namespace fheacc {
+
+int ensure_scratch(Context &c, Scratch &s, size_t bytes)
+{
+    if (s.bytes >= bytes) return FHEACC_OK;
+    if (s.ptr) {
+        cudaStreamSynchronize(c.stream);
+        cudaFree(s.ptr);   // implicit device synchronisation
+        s.ptr = nullptr;
+        s.bytes = 0;
+    }
+    size_t want = std::max(bytes, (size_t)1 << 20);
+    cudaError_t e = cudaMalloc(&s.ptr, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return c.fail(FHEACC_ENOMEM, std::string("scratch allocation failed: ") + cudaGetErrorString(e));
+    }
+    s.bytes = want;
+    return FHEACC_OK;
+}
+
+}  // namespace fheacc
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+cudaStream_t pick_stream(Context *c, void *stream) { return stream ? (cudaStream_t)stream : c->stream; }
+
+uint32_t shoup32_companion(uint64_t w, uint64_t Q) { return (uint32_t)((w << 32) / Q); }
+
+int build_tables(Context &c)
+{
+    host::Tables T;
+    T.build(c.p);
+    const int N = c.p.N;
+    const uint64_t Q = c.p.Q;
+    std::vector<uint2> fw(N), iw(N);
+    for (int i = 0; i < N; i++) {
+        fw[i] = make_uint2((uint32_t)T.rou[i], shoup32_companion(T.rou[i], Q));
+        iw[i] = make_uint2((uint32_t)T.irou[i], shoup32_companion(T.irou[i], Q));
+    }
+    cudaError_t e = cudaMalloc(&c.d_fwd_tw, N * sizeof(uint2));
+    if (e == cudaSuccess) e = cudaMalloc(&c.d_inv_tw, N * sizeof(uint2));
+    if (e == cudaSuccess) e = cudaMemcpy(c.d_fwd_tw, fw.data(), N * sizeof(uint2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c.d_inv_tw, iw.data(), N * sizeof(uint2), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return c.cuda_fail(e, "twiddle upload");
+    dev::Ntt32Consts &k = c.nc;
+    std::memset(&k, 0, sizeof k);
+    k.Q = (uint32_t)Q;
+    k.twoQ = (uint32_t)(2 * Q);
+    for (int i = 1; i < 32; i++) {
+        k.fw[i] = (uint32_t)T.rou[i];
+        k.fws[i] = shoup32_companion(T.rou[i], Q);
+        k.iw[i] = (uint32_t)T.irou[i];
+        k.iws[i] = shoup32_companion(T.irou[i], Q);
+    }
+    k.iN = (uint32_t)c.p.iN;
+    k.iNs = shoup32_companion(c.p.iN, Q);
+    uint64_t w1 = host::mulmod(T.irou[1], c.p.iN, Q);
+    k.iw1N = (uint32_t)w1;
+    k.iw1Ns = shoup32_companion(w1, Q);
+    return FHEACC_OK;
+}
+
+// Copies `words` 32-bit words from a host vector into device memory in chunks.
+int upload_u32(Context &c, uint32_t *dst, const uint32_t *src, size_t words)
+{
+    cudaError_t e = cudaMemcpy(dst, src, words * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "key upload");
+}
+
+}  // namespace
+
+extern "C" {
+
+int fheacc_create(const fheacc_params *p, int device, fheacc_ctx **out)
+{
+    if (!p || !out) {
+        g_create_error = "null argument";
+        return FHEACC_EINVAL;
+    }
+    *out = nullptr;
+    fheacc_params pp = *p;
+    if (fheacc_params_derive(&pp) != FHEACC_OK) {
+        const char *why = host::check_params(pp);
+        g_create_error = std::string("invalid parameter set: ") + (why ? why : "derivation failed");
+        return FHEACC_EINVAL;
+    }
+    if (pp.N != 1024 || pp.Q >= (1ULL << 27) || pp.digitG < 2 || pp.digitG > 4) {
+        g_create_error = "unsupported parameter set: this build runs N = 1024, Q < 2^27, digitG 2..4";
+        return FHEACC_EINVAL;
+    }
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev <= 0 || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        g_create_error = std::string("no usable CUDA device: ") + (e != cudaSuccess ? cudaGetErrorString(e) : "bad index");
+        return FHEACC_ENODEV;
+    }
+    Context *c = new (std::nothrow) Context();
+    if (!c) {
+        g_create_error = "out of host memory";
+        return FHEACC_ENOMEM;
+    }
+    c->p = pp;
+    c->device = device;
+    DeviceGuard g(device);
+    DevParams &d = c->dp;
+    d.n = pp.n; d.N = pp.N; d.logN = 10; d.q = pp.q; d.embed = 2u * (uint32_t)pp.N / pp.q; d.Q = pp.Q;
+    d.BG_bits = pp.BG_bits; d.digitG = pp.digitG; d.Br = pp.Br; d.digitR = pp.digitR;
+    d.Bks = pp.Bks; d.digitKS = pp.digitKS; d.Bks_R_bits = pp.Bks_R_bits; d.digitKS_R = pp.digitKS_R;
+    for (int i = 0; i < 6; i++) d.gate_constant[i] = pp.gate_constant[i];
+    d.gate_constant[6] = d.gate_constant[7] = 0;
+    d.mu64 = (uint64_t)(((unsigned __int128)1 << 64) / pp.Q);
+    d.ks_row = (uint32_t)(((pp.n + 1) + 31) / 32 * 32);
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("stream creation failed: ") + cudaGetErrorString(e);
+        delete c;
+        return FHEACC_EIO;
+    }
+    int rc = build_tables(*c);
+    if (rc != FHEACC_OK) {
+        g_create_error = c->err;
+        fheacc_destroy(reinterpret_cast<fheacc_ctx *>(c));
+        return rc;
+    }
+    *out = reinterpret_cast<fheacc_ctx *>(c);
+    return FHEACC_OK;
+}
+
+int fheacc_destroy(fheacc_ctx *ctx)
+{
+    if (!ctx) return FHEACC_OK;
+    Context *c = reinterpret_cast<Context *>(ctx);
+    DeviceGuard g(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->d_fwd_tw);
+    cudaFree(c->d_inv_tw);
+    cudaFree(c->d_btkey);
+    cudaFree(c->d_kskey);
+    cudaFree(c->d_subs);
+    cudaFree(c->extract.ptr);
+    cudaFree(c->io.ptr);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return FHEACC_OK;
+}
+
+const char *fheacc_last_error(const fheacc_ctx *ctx)
+{
+    if (!ctx) return g_create_error.c_str();
+    return reinterpret_cast<const Context *>(ctx)->err.c_str();
+}
+
+int fheacc_get_params(const fheacc_ctx *ctx, fheacc_params *out)
+{
+    if (!ctx || !out) return FHEACC_EINVAL;
+    *out = reinterpret_cast<const Context *>(ctx)->p;
+    return FHEACC_OK;
+}
+
+size_t fheacc_device_bytes(const fheacc_ctx *ctx)
+{
+    return ctx ? reinterpret_cast<const Context *>(ctx)->device_bytes() : 0;
+}
+
+int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t words)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    if (!btkey || words != fheacc_bootstrap_key_words(&c.p)) return c.fail(FHEACC_EINVAL, "bootstrap key size mismatch");
+    DeviceGuard g(c.device);
+    const size_t n = c.p.n, dR = c.p.digitR, Br = c.p.Br;
+    const size_t rw = (size_t)c.p.digitG * 4 * c.p.N;
+    const uint64_t Q = c.p.Q;
+    if (!c.d_btkey) {
+        cudaError_t e = cudaMalloc(&c.d_btkey, words * sizeof(uint32_t));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            c.d_btkey = nullptr;
+            return c.fail(FHEACC_ENOMEM, "device memory for the bootstrap key");
+        }
+        c.btkey_bytes = words * sizeof(uint32_t);
+    }
+    // host [r][j][i] -> device [(i * digitR + j) * Br + r], one step (all r) per chunk
+    std::vector<uint32_t> stage(Br * rw);
+    for (size_t i = 0; i < n; i++) {
+        for (size_t j = 0; j < dR; j++) {
+            for (size_t r = 0; r < Br; r++) {
+                const uint64_t *src = btkey + ((r * dR + j) * n + i) * rw;
+                uint32_t *dst = stage.data() + r * rw;
+                for (size_t x = 0; x < rw; x++) dst[x] = (uint32_t)(src[x] % Q);
+            }
+            int rc = upload_u32(c, c.d_btkey + (i * dR + j) * Br * rw, stage.data(), Br * rw);
+            if (rc) return rc;
+        }
+    }
+    return FHEACC_OK;
+}
+
+int fheacc_upload_lwe_ks_key(fheacc_ctx *ctx, const uint64_t *kskey, size_t words)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    if (!kskey || words != fheacc_lwe_ks_key_words(&c.p)) return c.fail(FHEACC_EINVAL, "LWE key-switch key size mismatch");
+    DeviceGuard g(c.device);
+    const size_t rows = (size_t)c.p.Bks * c.p.digitKS * c.p.N, w = (size_t)c.p.n + 1, rs = c.dp.ks_row;
+    if (!c.d_kskey) {
+        cudaError_t e = cudaMalloc(&c.d_kskey, rows * rs * sizeof(uint32_t));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            c.d_kskey = nullptr;
+            return c.fail(FHEACC_ENOMEM, "device memory for the LWE key-switch key");
+        }
+        c.kskey_bytes = rows * rs * sizeof(uint32_t);
+    }
+    const size_t chunk = 8192;
+    std::vector<uint32_t> stage(chunk * rs, 0);
+    for (size_t r0 = 0; r0 < rows; r0 += chunk) {
+        const size_t m = std::min(chunk, rows - r0);
+        for (size_t r = 0; r < m; r++)
+            for (size_t k = 0; k < w; k++) stage[r * rs + k] = (uint32_t)(kskey[(r0 + r) * w + k] % c.p.Q);
+        int rc = upload_u32(c, c.d_kskey + r0 * rs, stage.data(), m * rs);
+        if (rc) return rc;
+    }
+    return FHEACC_OK;
+}
+
+int fheacc_upload_subs_key(fheacc_ctx *ctx, const uint64_t *subs_key, size_t words)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    if (!subs_key || words != fheacc_subs_key_words(&c.p)) return c.fail(FHEACC_EINVAL, "substitute key size mismatch");
+    DeviceGuard g(c.device);
+    if (!c.d_subs) {
+        cudaError_t e = cudaMalloc(&c.d_subs, words * sizeof(uint32_t));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            c.d_subs = nullptr;
+            return c.fail(FHEACC_ENOMEM, "device memory for the substitute key");
+        }
+        c.subs_bytes = words * sizeof(uint32_t);
+    }
+    std::vector<uint32_t> stage(words);
+    for (size_t x = 0; x < words; x++) stage[x] = (uint32_t)(subs_key[x] % c.p.Q);
+    return upload_u32(c, c.d_subs, stage.data(), words);
+}
+
+static int bootstrap_device(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
+                            size_t count, uint64_t *d_out, uint32_t flags, cudaStream_t st, int max_ctas)
+{
+    if (!c.d_btkey) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
+    if (!c.d_kskey) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
+    int rc = ensure_scratch(c, c.extract, count * kExtractStride * sizeof(uint32_t));
+    if (rc) return rc;
+    uint32_t *ext = (uint32_t *)c.extract.ptr;
+    rc = launch_blind_rotate32(c, d_c1, d_c2, d_gates, count, flags, nullptr, ext, max_ctas, st);
+    if (rc) return rc;
+    return launch_lwe_keyswitch32(c, ext, count, true, d_out, st);
+}
+
+int fheacc_bootstrap_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
+                           size_t count, uint64_t *d_out, uint32_t flags, void *stream)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    if (count && (!d_c1 || !d_c2 || !d_gates || !d_out)) return c.fail(FHEACC_EINVAL, "null buffer");
+    DeviceGuard g(c.device);
+    return bootstrap_device(c, d_c1, d_c2, d_gates, count, d_out, flags, pick_stream(&c, stream), 0);
+}
+
+int fheacc_bootstrap_plain_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2,
+                                 const int32_t *d_gates, size_t count, uint64_t *d_out, uint32_t flags,
+                                 void *stream)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    if (count && (!d_c1 || !d_c2 || !d_gates || !d_out)) return c.fail(FHEACC_EINVAL, "null buffer");
+    DeviceGuard g(c.device);
+    cudaStream_t st = pick_stream(&c, stream);
+    const size_t w = (size_t)c.p.n + 1;
+    for (size_t i = 0; i < count; i++) {
+        int rc = bootstrap_device(c, d_c1 + i * w, d_c2 + i * w, d_gates + i, 1, d_out + i * w, flags, st, 1);
+        if (rc) return rc;
+    }
+    return FHEACC_OK;
+}
+
+int fheacc_bootstrap(fheacc_ctx *ctx, const uint64_t *c1, const uint64_t *c2, const int32_t *gates, size_t count,
+                     uint64_t *out, uint32_t flags)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    if (count == 0) return FHEACC_OK;
+    if (!c1 || !c2 || !gates || !out) return c.fail(FHEACC_EINVAL, "null buffer");
+    const size_t w = (size_t)c.p.n + 1;
+    for (size_t i = 0; i < count; i++) {
+        if (gates[i] < 0 || gates[i] > 5) return c.fail(FHEACC_EINVAL, "gate code out of range");
+        if (std::memcmp(c1 + i * w, c2 + i * w, w * sizeof(uint64_t)) == 0)
+            return c.fail(FHEACC_EINVAL, "c1 == c2: only independent ciphertexts can be bootstrapped");
+    }
+    DeviceGuard g(c.device);
+    const size_t lwe_bytes = count * w * sizeof(uint64_t);
+    const size_t gate_off = (3 * lwe_bytes + 255) / 256 * 256;
+    int rc = ensure_scratch(c, c.io, gate_off + count * sizeof(int32_t));
+    if (rc) return rc;
+    char *base = (char *)c.io.ptr;
+    uint64_t *d_c1 = (uint64_t *)base, *d_c2 = (uint64_t *)(base + lwe_bytes), *d_out = (uint64_t *)(base + 2 * lwe_bytes);
+    int32_t *d_g = (int32_t *)(base + gate_off);
+    cudaStream_t st = c.stream;
+    cudaError_t e = cudaMemcpyAsync(d_c1, c1, lwe_bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_c2, c2, lwe_bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_g, gates, count * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return c.cuda_fail(e, "input copy");
+    rc = bootstrap_device(c, d_c1, d_c2, d_g, count, d_out, flags, st, 0);
+    if (rc) return rc;
+    e = cudaMemcpyAsync(out, d_out, lwe_bytes, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "bootstrap");
+}
+
+int fheacc_ntt_forward(fheacc_ctx *ctx, uint64_t *d_polys, size_t count, void *stream)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    DeviceGuard g(c.device);
+    return launch_ntt32(c, d_polys, count, false, pick_stream(&c, stream));
+}
+
+int fheacc_ntt_inverse(fheacc_ctx *ctx, uint64_t *d_polys, size_t count, void *stream)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    DeviceGuard g(c.device);
+    return launch_ntt32(c, d_polys, count, true, pick_stream(&c, stream));
+}
+
+int fheacc_rlwe_mult_rgsw(fheacc_ctx *ctx, const uint64_t *d_acc, const uint64_t *d_rgsw, uint64_t *d_out,
+                          size_t count, void *stream)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    DeviceGuard g(c.device);
+    return launch_rlwe_mult_rgsw32(c, d_acc, d_rgsw, d_out, count, pick_stream(&c, stream));
+}
+
+int fheacc_blind_rotate_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
+                              size_t count, uint64_t *d_acc, uint32_t flags, void *stream)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    DeviceGuard g(c.device);
+    return launch_blind_rotate32(c, d_c1, d_c2, d_gates, count, flags, d_acc, nullptr, 0, pick_stream(&c, stream));
+}
+
+int fheacc_lwe_keyswitch_async(fheacc_ctx *ctx, const uint64_t *d_rlwe, size_t count, uint64_t *d_out,
+                               void *stream)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    DeviceGuard g(c.device);
+    int rc = ensure_scratch(c, c.extract, count * kExtractStride * sizeof(uint32_t));
+    if (rc) return rc;
+    cudaStream_t st = pick_stream(&c, stream);
+    rc = launch_extract_from_ntt32(c, d_rlwe, count, (uint32_t *)c.extract.ptr, st);
+    if (rc) return rc;
+    return launch_lwe_keyswitch32(c, (uint32_t *)c.extract.ptr, count, false, d_out, st);
+}
+
+int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t count, uint64_t *d_out, void *stream)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    DeviceGuard g(c.device);
+    return launch_modswitch(c, d_in, count, d_out, pick_stream(&c, stream));
+}
+
+int fheacc_sync(fheacc_ctx *ctx, uint32_t timeout_ms)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    DeviceGuard g(c.device);
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t e = cudaStreamQuery(c.stream);
+        if (e == cudaSuccess) return FHEACC_OK;
+        if (e != cudaErrorNotReady) return c.cuda_fail(e, "sync");
+        if (timeout_ms) {
+            auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+            if (ms >= (long long)timeout_ms) return c.fail(FHEACC_ETIMEDOUT, "sync timed out");
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,92 @@
+// ctx.hpp -- the device context behind fheacc_ctx and the launchers shared by
+// the kernel translation units. Internal to libfheacc.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+#include "fheacc.h"
+#include "ntt32.cuh"
+
+namespace fheacc {
+
+// Device copy of the parameters the kernels read.
+struct DevParams {
+    int n, N, logN;
+    uint32_t q, embed;          // embed = 2N / q
+    uint64_t Q;
+    uint32_t BG_bits, digitG, Br, digitR, Bks, digitKS, Bks_R_bits, digitKS_R;
+    uint64_t gate_constant[8];  // entries 6, 7 are 0 (guard for bad gate codes)
+    uint64_t mu64;              // floor(2^64 / Q), Barrett constant
+    uint32_t ks_row;            // padded words per LWE key-switch row (>= n+1, multiple of 32)
+};
+
+struct Scratch {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct Context {
+    fheacc_params p{};
+    DevParams dp{};
+    int device = 0;
+    bool wide = false;            // 64-bit words (Q >= 2^27) -- not yet supported on device
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    // twiddles: (w, w') pairs indexed like the reference tables
+    uint2 *d_fwd_tw = nullptr, *d_inv_tw = nullptr;
+    dev::Ntt32Consts nc{};
+
+    // keys, device layouts
+    uint32_t *d_btkey = nullptr;   // [(i*digitR + j)*Br + r][digitG][2][2][N]
+    size_t btkey_bytes = 0;
+    uint32_t *d_kskey = nullptr;   // [(d*digitKS + j)*N + i][ks_row]
+    size_t kskey_bytes = 0;
+    uint32_t *d_subs = nullptr;    // [logN][digitKS_R][2][N]
+    size_t subs_bytes = 0;
+
+    // scratch owned by the context, grown on demand
+    Scratch extract;               // extracted RLWEs between blind rotation and key switch
+    Scratch io;                    // device staging for the host-buffer entry points
+
+    size_t device_bytes() const
+    {
+        return btkey_bytes + kskey_bytes + subs_bytes + extract.bytes + io.bytes +
+               2 * (size_t)p.N * sizeof(uint2);
+    }
+    int fail(int code, const std::string &msg)
+    {
+        err = msg;
+        return code;
+    }
+    int cuda_fail(cudaError_t e, const char *where)
+    {
+        err = std::string(where) + ": " + cudaGetErrorString(e);
+        return FHEACC_EIO;
+    }
+};
+
+// Grows `s` to at least `bytes` (device memory).
+int ensure_scratch(Context &c, Scratch &s, size_t bytes);
+
+// launchers (bootstrap32.cu)
+int launch_ntt32(Context &c, uint64_t *d_polys, size_t count, bool inverse, cudaStream_t st);
+int launch_rlwe_mult_rgsw32(Context &c, const uint64_t *d_acc, const uint64_t *d_rgsw, uint64_t *d_out,
+                            size_t count, cudaStream_t st);
+// Blind rotation; writes either NTT accumulators (d_acc_out, [count][2N] u64)
+// or the extracted time-domain RLWE for the key switch (d_extract, u32
+// [count][N + 32]: a[N] after NTT_a_transpose, then b[0]).
+int launch_blind_rotate32(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
+                          size_t count, uint32_t flags, uint64_t *d_acc_out, uint32_t *d_extract,
+                          int max_ctas, cudaStream_t st);
+// LWE key switch (+ optional modulus switch) from extracted RLWEs
+// (lwe_ks.cu).
+int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
+                           cudaStream_t st);
+int launch_extract_from_ntt32(Context &c, const uint64_t *d_rlwe, size_t count, uint32_t *d_extract,
+                              cudaStream_t st);
+int launch_modswitch(Context &c, const uint64_t *d_in, size_t count, uint64_t *d_out, cudaStream_t st);
+
+constexpr size_t kExtractStride = 1024 + 32;   // u32 words per extracted RLWE (N = 1024)
+
+}  // namespace fheacc

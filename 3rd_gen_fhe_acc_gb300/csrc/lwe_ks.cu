@@ -1,0 +1,126 @@
+// lwe_ks.cu -- RLWE -> LWE key switch and modulus switch, 32-bit words.
+//
+// Reference behaviour: LWE::LWE_keyswitch (FHE_ACC_runtime/src/LWE.cpp:233-253)
+// and LWE::LWE_modswitch / scale_round (LWE.cpp:255-269). The reference's FPGA
+// path runs these on the host (myfpga.cpp:1519-1523); here they run on the GPU
+// right after the blind rotation.
+//
+// Input is the extracted RLWE (time-domain a[N] after NTT_a_transpose, and
+// b[0]). For every coefficient i < N and digit j < digitKS the LWE row
+// kskey[d][j][i], d = base-Bks digit j of a[i], is subtracted. One CTA per
+// ciphertext: the digits are computed once into shared memory, then the CTA
+// walks the N * digitKS rows; a row is n+1 consecutive words, read by
+// consecutive threads (coalesced). Sums are kept in 64-bit registers without
+// reduction (N * digitKS * Q < 2^64) and reduced once at the end; the modulus
+// switch is fused into the same epilogue.
+#include "ctx.hpp"
+#include <algorithm>
+
+namespace fheacc {
+namespace dev {
+
+struct KsArgs {
+    const uint32_t *ext;
+    size_t count;
+    const uint32_t *kskey;
+    uint64_t *out;
+    int n, N, digitKS;
+    uint32_t Bks, ks_row, q, modswitch;
+    uint64_t Q;
+};
+
+constexpr int kKsThreads = 256;
+constexpr int kKsPerThread = 4;   // up to n + 1 <= 1024 coefficients
+
+__device__ __forceinline__ uint64_t scale_round_dev(uint64_t x, uint64_t new_mod, uint64_t old_mod)
+{
+    // LWE.cpp:255-260: (old + 2 x new) / (2 old), exact integer
+    unsigned __int128 num = (unsigned __int128)old_mod + 2 * (unsigned __int128)x * new_mod;
+    return (uint64_t)(num / (2 * (unsigned __int128)old_mod));
+}
+
+__global__ void __launch_bounds__(kKsThreads) lwe_ks32_kernel(const __grid_constant__ KsArgs A)
+{
+    extern __shared__ uint8_t digits[];   // [N][digitKS]
+    const int n = A.n, N = A.N, D = A.digitKS;
+    const uint32_t Q = (uint32_t)A.Q;
+    for (size_t ci = blockIdx.x; ci < A.count; ci += gridDim.x) {
+        const uint32_t *ext = A.ext + ci * kExtractStride;
+        for (int i = threadIdx.x; i < N; i += blockDim.x) {
+            uint32_t a = ext[i];
+            for (int j = 0; j < D; j++) {
+                digits[i * D + j] = (uint8_t)(a % A.Bks);
+                a /= A.Bks;
+            }
+        }
+        __syncthreads();
+        uint64_t acc[kKsPerThread] = {0, 0, 0, 0};
+        const uint32_t *key = A.kskey;
+        for (int i = 0; i < N; i++) {
+            for (int j = 0; j < D; j++) {
+                const uint32_t d = digits[i * D + j];
+                const uint32_t *row = key + ((size_t)(d * D + j) * N + i) * A.ks_row;
+#pragma unroll
+                for (int c = 0; c < kKsPerThread; c++) {
+                    const int k = threadIdx.x + c * kKsThreads;
+                    if (k <= n) acc[c] += __ldg(row + k);
+                }
+            }
+        }
+        const uint32_t b0 = ext[N];
+        const uint32_t Q8 = Q / 8 + 1;
+        uint64_t *out = A.out + ci * (size_t)(n + 1);
+#pragma unroll
+        for (int c = 0; c < kKsPerThread; c++) {
+            const int k = threadIdx.x + c * kKsThreads;
+            if (k <= n) {
+                const uint64_t s = acc[c] % Q;
+                uint64_t v;
+                if (k < n) v = s ? Q - s : 0;
+                else v = ((uint64_t)(b0 + Q8) % Q + Q - s) % Q;
+                out[k] = A.modswitch ? scale_round_dev(v, A.q, A.Q) : v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void modswitch_kernel(const uint64_t *__restrict__ in, uint64_t *__restrict__ out, size_t words,
+                                 uint64_t q, uint64_t Q)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = scale_round_dev(in[i], q, Q);
+}
+
+}  // namespace dev
+
+int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
+                           cudaStream_t st)
+{
+    if (!count) return FHEACC_OK;
+    if (!c.d_kskey) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
+    if (c.p.n + 1 > dev::kKsThreads * dev::kKsPerThread) return c.fail(FHEACC_EINVAL, "n too large for key switch");
+    dev::KsArgs A{};
+    A.ext = d_extract; A.count = count; A.kskey = c.d_kskey; A.out = d_out;
+    A.n = c.p.n; A.N = c.p.N; A.digitKS = (int)c.p.digitKS; A.Bks = c.p.Bks; A.ks_row = c.dp.ks_row;
+    A.q = c.p.q; A.modswitch = modswitch ? 1u : 0u; A.Q = c.p.Q;
+    const size_t smem = (size_t)c.p.N * c.p.digitKS;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
+    size_t blocks = std::min<size_t>(count, (size_t)std::max(sms, 1) * 8);
+    dev::lwe_ks32_kernel<<<(unsigned)blocks, dev::kKsThreads, smem, st>>>(A);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "lwe_ks32 launch");
+}
+
+int launch_modswitch(Context &c, const uint64_t *d_in, size_t count, uint64_t *d_out, cudaStream_t st)
+{
+    if (!count) return FHEACC_OK;
+    size_t words = count * ((size_t)c.p.n + 1);
+    unsigned blocks = (unsigned)std::min<size_t>((words + 255) / 256, 4096);
+    dev::modswitch_kernel<<<blocks, 256, 0, st>>>(d_in, d_out, words, c.p.q, c.p.Q);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "modswitch launch");
+}
+
+}  // namespace fheacc

@@ -1,0 +1,205 @@
+// ntt32.cuh -- one-warp negacyclic NTT / inverse NTT of a 1024-point
+// polynomial with 32-bit words, for Q < 2^27.
+//
+// Computes exactly the transforms of the reference's NTT / iNTT
+// (FHE_ACC_runtime/src/nbt.cpp:423-454 and 456-491: Cooley-Tukey with the
+// bit-reversed psi table, Gentleman-Sande with the bit-reversed psi^-1 table
+// and a final *N^-1), so canonical outputs are bit-identical.
+//
+// Data layout: each lane holds 32 coefficients in registers.
+//   layout A: lane l, register r holds element  l + 32 r   (strided)
+//   layout B: lane l, register r holds element 32 l + r    (contiguous)
+// The forward transform runs its first five stages (t = 512..32) in layout A,
+// where every lane uses the same twiddle (taken from the kernel's parameter
+// bank), one padded shared-memory transpose, and the last five stages
+// (t = 16..1) in layout B with per-lane twiddles read through L1. The inverse
+// runs the same way backwards. Shared-memory addresses are padded by one word
+// per 32 (element e at e + e/32), so both transpose directions are free of bank
+// conflicts.
+//
+// Modular arithmetic: Shoup multiplication by precomputed (w, w' =
+// floor(w 2^32 / Q)) gives x*w mod Q in [0, 2Q) for any 32-bit x. The forward
+// butterflies never reduce the upper input: each stage adds at most 2Q to the
+// bound, so inputs below Q leave the transform below 21Q < 2^32 (Q < 2^27).
+// The inverse keeps Harvey's [0, 2Q) invariant and ends canonical.
+#pragma once
+#include <cstdint>
+
+namespace fheacc {
+namespace dev {
+
+constexpr int kN32 = 1024;
+constexpr int kPadN = 1024 + 32;   // padded words per polynomial in shared memory
+
+// Warp-uniform twiddles (stages with m < 32), passed in the kernel's parameter
+// bank so that fully unrolled stages read them as constant operands.
+struct Ntt32Consts {
+    uint32_t Q, twoQ;
+    uint32_t fw[32], fws[32];    // rou[m+i],  m+i < 32, and Shoup companions
+    uint32_t iw[32], iws[32];    // irou[m+i], m+i < 32
+    uint32_t iN, iNs;            // N^-1
+    uint32_t iw1N, iw1Ns;        // irou[1] * N^-1
+};
+
+__device__ __forceinline__ int pad32(int e) { return e + (e >> 5); }
+
+__device__ __forceinline__ uint32_t shoup32(uint32_t x, uint32_t w, uint32_t ws, uint32_t Q)
+{
+    uint32_t t = __umulhi(x, ws);
+    return x * w - t * Q;   // in [0, 2Q)
+}
+
+// Cooley-Tukey butterfly, upper input left unreduced.
+__device__ __forceinline__ void ct_bfly(uint32_t &x, uint32_t &y, uint32_t w, uint32_t ws, uint32_t Q,
+                                        uint32_t twoQ)
+{
+    uint32_t t = shoup32(y, w, ws, Q);
+    y = x + twoQ - t;
+    x = x + t;
+}
+
+// Gentleman-Sande butterfly, inputs and outputs in [0, 2Q).
+__device__ __forceinline__ void gs_bfly(uint32_t &x, uint32_t &y, uint32_t w, uint32_t ws, uint32_t Q,
+                                        uint32_t twoQ)
+{
+    uint32_t u = x + y;
+    u = min(u, u - twoQ);
+    uint32_t v = shoup32(x - y + twoQ, w, ws, Q);
+    x = u;
+    y = v;
+}
+
+// Forward stage s (0..4) in layout A.
+template <int S>
+__device__ __forceinline__ void fwd_stage_A(uint32_t (&x)[32], const Ntt32Consts &c)
+{
+    constexpr int h = 16 >> S, m = 1 << S;
+#pragma unroll
+    for (int r = 0; r < 32; r++) {
+        if (!(r & h)) {
+            const int i = r / (2 * h);
+            ct_bfly(x[r], x[r + h], c.fw[m + i], c.fws[m + i], c.Q, c.twoQ);
+        }
+    }
+}
+
+// Forward stage s (5..9) in layout B. tw: (w, w') pairs indexed by m + i.
+template <int S>
+__device__ __forceinline__ void fwd_stage_B(uint32_t (&x)[32], const uint2 *__restrict__ tw, int lane,
+                                            uint32_t Q, uint32_t twoQ)
+{
+    constexpr int t = 512 >> S, m = 1 << S, G = 16 / t;   // G twiddles per lane
+    uint2 w[G];
+    const uint2 *base = tw + m + lane * G;
+#pragma unroll
+    for (int g = 0; g < G; g++) w[g] = __ldg(base + g);
+#pragma unroll
+    for (int r = 0; r < 32; r++) {
+        if (!(r & t)) {
+            const int g = r / (2 * t);
+            ct_bfly(x[r], x[r + t], w[g].x, w[g].y, Q, twoQ);
+        }
+    }
+}
+
+// Inverse stage with butterfly distance t (1..16) in layout B.
+template <int T>
+__device__ __forceinline__ void inv_stage_B(uint32_t (&x)[32], const uint2 *__restrict__ tw, int lane,
+                                            uint32_t Q, uint32_t twoQ)
+{
+    constexpr int m = 512 / T, G = 16 / T;
+    uint2 w[G];
+    const uint2 *base = tw + m + lane * G;
+#pragma unroll
+    for (int g = 0; g < G; g++) w[g] = __ldg(base + g);
+#pragma unroll
+    for (int r = 0; r < 32; r++) {
+        if (!(r & T)) {
+            const int g = r / (2 * T);
+            gs_bfly(x[r], x[r + T], w[g].x, w[g].y, Q, twoQ);
+        }
+    }
+}
+
+// Inverse stage with butterfly distance t = 32*H (H = 1..8) in layout A.
+template <int H>
+__device__ __forceinline__ void inv_stage_A(uint32_t (&x)[32], const Ntt32Consts &c)
+{
+    constexpr int m = 16 / H;
+#pragma unroll
+    for (int r = 0; r < 32; r++) {
+        if (!(r & H)) {
+            const int i = r / (2 * H);
+            gs_bfly(x[r], x[r + H], c.iw[m + i], c.iws[m + i], c.Q, c.twoQ);
+        }
+    }
+}
+
+// Layout A -> B through a padded per-warp buffer (kPadN words).
+__device__ __forceinline__ void transpose_A_to_B(uint32_t (&x)[32], uint32_t *buf, int lane)
+{
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < 32; r++) buf[33 * r + lane] = x[r];
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < 32; r++) x[r] = buf[33 * lane + r];
+    __syncwarp();
+}
+
+__device__ __forceinline__ void transpose_B_to_A(uint32_t (&x)[32], uint32_t *buf, int lane)
+{
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < 32; r++) buf[33 * lane + r] = x[r];
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < 32; r++) x[r] = buf[33 * r + lane];
+    __syncwarp();
+}
+
+// Forward NTT: x in layout A (values < Q) -> layout B, values < 21Q, in the
+// reference's bit-reversed output order. buf: kPadN words of scratch.
+__device__ __forceinline__ void ntt_fwd_1024(uint32_t (&x)[32], const Ntt32Consts &c,
+                                             const uint2 *__restrict__ fwd_tw, uint32_t *buf, int lane)
+{
+    fwd_stage_A<0>(x, c);
+    fwd_stage_A<1>(x, c);
+    fwd_stage_A<2>(x, c);
+    fwd_stage_A<3>(x, c);
+    fwd_stage_A<4>(x, c);
+    transpose_A_to_B(x, buf, lane);
+    fwd_stage_B<5>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<6>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<7>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<8>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<9>(x, fwd_tw, lane, c.Q, c.twoQ);
+}
+
+// Inverse NTT: x in layout B (values < 2Q, bit-reversed order) -> layout A,
+// canonical time-domain coefficients (times N^-1).
+__device__ __forceinline__ void ntt_inv_1024(uint32_t (&x)[32], const Ntt32Consts &c,
+                                             const uint2 *__restrict__ inv_tw, uint32_t *buf, int lane)
+{
+    inv_stage_B<1>(x, inv_tw, lane, c.Q, c.twoQ);
+    inv_stage_B<2>(x, inv_tw, lane, c.Q, c.twoQ);
+    inv_stage_B<4>(x, inv_tw, lane, c.Q, c.twoQ);
+    inv_stage_B<8>(x, inv_tw, lane, c.Q, c.twoQ);
+    inv_stage_B<16>(x, inv_tw, lane, c.Q, c.twoQ);
+    transpose_B_to_A(x, buf, lane);
+    inv_stage_A<1>(x, c);
+    inv_stage_A<2>(x, c);
+    inv_stage_A<4>(x, c);
+    inv_stage_A<8>(x, c);
+    // last stage (t = 512, m = 1) with N^-1 folded into both outputs
+#pragma unroll
+    for (int r = 0; r < 16; r++) {
+        uint32_t u = shoup32(x[r] + x[r + 16], c.iN, c.iNs, c.Q);
+        uint32_t v = shoup32(x[r] - x[r + 16] + c.twoQ, c.iw1N, c.iw1Ns, c.Q);
+        x[r] = min(u, u - c.Q);
+        x[r + 16] = min(v, v - c.Q);
+    }
+}
+
+}  // namespace dev
+}  // namespace fheacc

@@ -1,0 +1,186 @@
+/*
+ * fheacc.h -- C ABI of libfheacc.so, the GB300 (sm_103a) device backend for the
+ * FHEW/AP gate-bootstrapping path of zhehongw/3rd_Gen_FHE_ACC.
+ *
+ * The library replaces the runtime's AWS-F1 device backend (namespace FPGA,
+ * FHE_ACC_runtime/include/myfpga.h:128-404). Each entry point below names the
+ * reference interface it stands in for. Plain pointers and sizes only; every
+ * function returns an int status (FHEACC_OK or a negative FHEACC_E* code) and
+ * never exits or aborts. fheacc_last_error() describes the last failure.
+ *
+ * Word formats follow the reference's ciphertext_t (uint64_t):
+ *   LWE   : a[n] then b                  (LWE.h:36-64)            n+1 words
+ *   RLWE  : a[N] then b[N], NTT domain in the reference's bit-reversed
+ *           order (RLWE.h:127-159, nbt.cpp:423-454)               2N words
+ *   RGSW  : [digitG][2 rows][2 polys a,b][N]  = c_text[h][g].a/.b  (RLWE.h:313-329)
+ *   bootstrap key : [Br][digitR][n] RGSW  = btkey[r][j][i]        (RLWE.h:331-345)
+ *   LWE key-switch key : [Bks][digitKS][N] LWE mod Q = kskey[d][j][i] (LWE.h:86-101)
+ *   substitute key : [log2 N][digitKS_R] RLWE = subs_key[l].RLWE_kskey[k] (app.h:22-28)
+ *   gates : int32, the reference's enum GATES {OR, AND, NOR, NAND, XOR, XNOR}
+ *           (params.h:107)
+ */
+#ifndef FHEACC_H
+#define FHEACC_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FHEACC_OK          0
+#define FHEACC_EINVAL    (-22)   /* bad argument / parameter set             */
+#define FHEACC_ENOMEM    (-12)   /* host or device allocation failed         */
+#define FHEACC_ENODEV    (-19)   /* no usable CUDA device                    */
+#define FHEACC_EIO        (-5)   /* CUDA error                               */
+#define FHEACC_ETIMEDOUT (-110)  /* fheacc_sync / bounded device wait expired */
+#define FHEACC_ENOKEY    (-126)  /* required key not uploaded               */
+#define FHEACC_EBUSY     (-16)   /* serving queue full                       */
+
+/* flags for the bootstrap calls */
+#define FHEACC_FLAG_FPGA_COMPAT 1u  /* also apply residue-0 keys, as
+                                       fpga_eval_bootstrap_x4..x16 do
+                                       (myfpga.cpp:1200-1210) */
+
+enum fheacc_gate { FHEACC_OR = 0, FHEACC_AND, FHEACC_NOR, FHEACC_NAND, FHEACC_XOR, FHEACC_XNOR };
+
+/* Parameter set. Replaces the reference's mutable globals (params.h:11-134)
+ * and the OCL register file pushed by FPGA::OCL_config_wr_rd
+ * (myfpga.cpp:82-326). Fields marked (derived) are filled by
+ * fheacc_params_derive when zero. */
+typedef struct fheacc_params {
+    int32_t  n;              /* LWE dimension                          */
+    uint32_t q;              /* LWE modulus, power of two              */
+    int32_t  N;              /* ring dimension, 1024 or 2048           */
+    uint32_t nbit;           /* Q = largest prime < 2^nbit, Q = 1 mod 2N (if Q == 0) */
+    uint64_t Q;              /* RLWE modulus                           */
+    uint32_t BG_bits;        /* gadget base 2^BG_bits                  */
+    uint32_t digitG;         /* (derived) ceil(log_BG Q)               */
+    uint32_t Br;             /* refresh base                           */
+    uint32_t digitR;         /* (derived) ceil(log_Br q)               */
+    uint32_t Bks;            /* RLWE->LWE key-switch base              */
+    uint32_t digitKS;        /* (derived) ceil(log_Bks Q)              */
+    uint32_t Bks_R_bits;     /* RLWE->RLWE key-switch base 2^Bks_R_bits */
+    uint32_t digitKS_R;      /* (derived) ceil(log_Bks_R Q)            */
+    uint64_t gate_constant[6]; /* (derived) OR..XNOR bound1, fhe_wo_fpga.cpp:141-146 */
+    uint64_t iN;             /* (derived) N^-1 mod Q                   */
+    uint64_t ROU;            /* (derived) smallest primitive 2N-th root of unity */
+    uint32_t E;              /* (derived) LWE noise bound q/16         */
+    uint32_t E_rlwe;         /* RLWE noise bound (reference: 18)       */
+} fheacc_params;
+
+/* Presets of the workloads this backend is measured on.
+ *  0 : n=500, N=1024, Q=134215681 (largest prime < 2^27, = 1 mod 2N),
+ *      BG=2^7 x4 digits, Br=23, Bks=25, Bks_R=2^9, q=512
+ *  1 : n=630, N=2048, Q=18014398509404161 (< 2^54), BG=2^9 x6, Br=23,
+ *      Bks=25, Bks_R=2^9, q=512
+ *  2 : the reference CPU app's set (fhe_wo_fpga.cpp:35-146): n=512, N=1024,
+ *      Q=134215681, BG=2^9 x3, Br=23, Bks=25, Bks_R=2^9, q=512 */
+int fheacc_params_preset(int preset, fheacc_params *out);
+/* Fill the (derived) fields; fhe_wo_fpga.cpp:89-161. */
+int fheacc_params_derive(fheacc_params *p);
+
+/* Sizes, in 64-bit words, of the key formats above. */
+size_t fheacc_bootstrap_key_words(const fheacc_params *p);
+size_t fheacc_lwe_ks_key_words(const fheacc_params *p);
+size_t fheacc_subs_key_words(const fheacc_params *p);
+
+/* Twiddle tables (psi^bitrev(i), psi^-bitrev(i)), root_of_unity_table,
+ * params.cpp:149-175. rou/irou: N words each. */
+int fheacc_twiddle_tables(const fheacc_params *p, uint64_t *rou, uint64_t *irou);
+
+/* ---------------------------------------------------------------- host side
+ * Key generation and encryption (host, no GPU). Deterministic from `seed`:
+ * the same seed gives the same words on every machine. These keep the
+ * reference's key-generation API (LWE.cpp:22-146, RLWE.cpp:243-606,
+ * app.cpp:4-24) behind plain arrays. threads <= 0 uses all online cores. */
+int fheacc_keygen_lwe_sk(const fheacc_params *p, uint64_t seed, uint64_t *sk /* n */);
+int fheacc_keygen_rlwe_sk(const fheacc_params *p, uint64_t seed, uint64_t *sk_ntt /* N */);
+int fheacc_keygen_bootstrap_key(const fheacc_params *p, uint64_t seed, const uint64_t *lwe_sk,
+                                const uint64_t *rlwe_sk_ntt, uint64_t *btkey, int threads);
+int fheacc_keygen_lwe_ks_key(const fheacc_params *p, uint64_t seed, const uint64_t *rlwe_sk_ntt,
+                             const uint64_t *lwe_sk, uint64_t *kskey, int threads);
+int fheacc_keygen_subs_key(const fheacc_params *p, uint64_t seed, const uint64_t *rlwe_sk_ntt,
+                           uint64_t *subs_key, int threads);
+/* LWE_encrypt of bits (m * q/4), LWE.cpp:108-146. out: [count][n+1]. */
+int fheacc_lwe_encrypt(const fheacc_params *p, uint64_t seed, const uint64_t *lwe_sk,
+                       const uint8_t *bits, size_t count, uint64_t *out);
+/* LWE_decrypt with t = 4, LWE.cpp:148-190. out: count values in [0, 4). */
+int fheacc_lwe_decrypt(const fheacc_params *p, const uint64_t *lwe_sk, const uint64_t *ct,
+                       size_t count, uint8_t *out);
+/* RLWE_encrypt of an NTT-domain plaintext poly, RLWE.cpp:324-344. */
+int fheacc_rlwe_encrypt(const fheacc_params *p, uint64_t seed, const uint64_t *rlwe_sk_ntt,
+                        const uint64_t *msg_ntt, uint64_t *out /* 2N */);
+/* b - a*s in NTT domain, then inverse NTT: the noisy time-domain phase
+ * (RLWE_decrypt before denoise, RLWE.cpp:346-357). */
+int fheacc_rlwe_phase(const fheacc_params *p, const uint64_t *rlwe_sk_ntt, const uint64_t *ct,
+                      uint64_t *phase_time /* N */);
+
+/* -------------------------------------------------------------- device side */
+typedef struct fheacc_ctx fheacc_ctx;
+
+/* Create a context on CUDA device `device`: derives the parameter set and
+ * builds the twiddle tables on the device. Replaces OCL_config_wr_rd
+ * (myfpga.cpp:82-326) and BAR1_ROU_table_{1k,2k}_wr (myfpga.cpp:399-594). */
+int fheacc_create(const fheacc_params *p, int device, fheacc_ctx **out);
+int fheacc_destroy(fheacc_ctx *ctx);
+/* Last error message of ctx (or of the last failed create when ctx is NULL). */
+const char *fheacc_last_error(const fheacc_ctx *ctx);
+int fheacc_get_params(const fheacc_ctx *ctx, fheacc_params *out);
+/* Device memory held by the context (keys, tables, scratch), in bytes. */
+size_t fheacc_device_bytes(const fheacc_ctx *ctx);
+
+/* Key upload, host words in the formats above; re-laid-out for the device
+ * once, at upload. Replace dma_write_bootstrap_key (myfpga.cpp:596-656),
+ * dma_write_subs_key (myfpga.cpp:658-712). The LWE key-switch key has no FPGA
+ * counterpart (the FPGA runtime key-switches on the host, myfpga.cpp:1519). */
+int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t words);
+int fheacc_upload_lwe_ks_key(fheacc_ctx *ctx, const uint64_t *kskey, size_t words);
+int fheacc_upload_subs_key(fheacc_ctx *ctx, const uint64_t *subs_key, size_t words);
+
+/* Gate bootstrapping of `count` independent gates, HOST buffers, blocking:
+ * out[i] = eval_bootstrap(c1[i], c2[i], gates[i]) (RLWE.cpp:726-786).
+ * Replaces fpga_eval_bootstrap_x1/_x4/_x8/_x12/_x16 (myfpga.cpp:1003-1660)
+ * with any count. c1/c2/out: [count][n+1]. A gate with c1 == c2 returns
+ * FHEACC_EINVAL (the CPU path exits, the FPGA path returns rc = -1). */
+int fheacc_bootstrap(fheacc_ctx *ctx, const uint64_t *c1, const uint64_t *c2,
+                     const int32_t *gates, size_t count, uint64_t *out, uint32_t flags);
+/* Same, DEVICE buffers, asynchronous on `stream` (cudaStream_t, NULL = the
+ * context's stream). Inputs are not checked for c1 == c2. */
+int fheacc_bootstrap_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2,
+                           const int32_t *d_gates, size_t count, uint64_t *d_out,
+                           uint32_t flags, void *stream);
+/* The plain form: one launch sequence per gate (the per-gate issue of
+ * fpga_eval_bootstrap_x1, myfpga.cpp:1003-1127), DEVICE buffers. */
+int fheacc_bootstrap_plain_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2,
+                                 const int32_t *d_gates, size_t count, uint64_t *d_out,
+                                 uint32_t flags, void *stream);
+
+/* Sub-steps of the path, DEVICE buffers, asynchronous (parity checks).
+ * Forward / inverse negacyclic NTT of `count` polys in place
+ * (nbt.cpp:423-454 / 456-491). Inputs canonical (< Q); outputs canonical. */
+int fheacc_ntt_forward(fheacc_ctx *ctx, uint64_t *d_polys, size_t count, void *stream);
+int fheacc_ntt_inverse(fheacc_ctx *ctx, uint64_t *d_polys, size_t count, void *stream);
+/* RLWE_mult_RGSW (RLWE.cpp:642-704) of count accumulators, each with its own
+ * RGSW (reference layout). */
+int fheacc_rlwe_mult_rgsw(fheacc_ctx *ctx, const uint64_t *d_acc, const uint64_t *d_rgsw,
+                          uint64_t *d_out, size_t count, void *stream);
+/* Blind rotation of eval_bootstrap (RLWE.cpp:733-767): NTT accumulators out,
+ * [count][2N]. */
+int fheacc_blind_rotate_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2,
+                              const int32_t *d_gates, size_t count, uint64_t *d_acc,
+                              uint32_t flags, void *stream);
+/* LWE_keyswitch (LWE.cpp:233-253): NTT RLWEs -> LWE mod Q, [count][n+1]. */
+int fheacc_lwe_keyswitch_async(fheacc_ctx *ctx, const uint64_t *d_rlwe, size_t count,
+                               uint64_t *d_out, void *stream);
+/* LWE_modswitch (LWE.cpp:262-269): LWE mod Q -> LWE mod q. */
+int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t count,
+                               uint64_t *d_out, void *stream);
+
+/* Wait for all work of the context, at most timeout_ms (0 = no limit). */
+int fheacc_sync(fheacc_ctx *ctx, uint32_t timeout_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,101 @@
+"""Gate bootstrapping on the GPU, end to end, against the oracle (bit-exact)
+and by decryption (the truth tables of test::bootstrapping, test.cpp:496-625).
+"""
+import numpy as np
+import pytest
+
+from conftest import random_gate_batch
+
+pytestmark = pytest.mark.gpu
+
+
+def test_truth_tables_all_gates(F, ctx0, keys0):
+    """Every gate on every input pair, as test::bootstrapping does."""
+    xs, ys, gs = [], [], []
+    for g in range(6):
+        for a in (0, 1):
+            for b in (0, 1):
+                xs.append(a); ys.append(b); gs.append(g)
+    x = np.array(xs, dtype=np.uint8); y = np.array(ys, dtype=np.uint8); g = np.array(gs, dtype=np.int32)
+    c = keys0.encrypt(np.concatenate([x, y]), seed=77)
+    c1, c2 = c[:24], c[24:]
+    out = ctx0.eval_bootstrap_batch(c1, c2, g)
+    want, failed = keys0.oracle.eval_bootstrap_batch(c1, c2, g, keys0.btkey, keys0.kskey)
+    assert failed == 0
+    assert np.array_equal(out, want)
+    dec = keys0.decrypt(out)
+    truth = np.array([F.gate_truth(int(gg), a, b) for gg, a, b in zip(g, x, y)], dtype=np.uint8)
+    assert np.array_equal(dec, truth)
+
+
+@pytest.mark.parametrize("count", [1, 33])
+def test_batch_bitexact(F, ctx0, keys0, count):
+    x, y, g, c1, c2 = random_gate_batch(keys0, count, seed=100 + count)
+    out = ctx0.eval_bootstrap_batch(c1, c2, g)
+    want, failed = keys0.oracle.eval_bootstrap_batch(c1, c2, g, keys0.btkey, keys0.kskey)
+    assert failed == 0
+    assert np.array_equal(out, want)
+    truth = np.array([F.gate_truth(int(a), b, c) for a, b, c in zip(g, x, y)], dtype=np.uint8)
+    assert np.array_equal(keys0.decrypt(out), truth)
+
+
+def test_plain_equals_batched(F, ctx0, keys0, cuda_ok):
+    torch = cuda_ok
+    x, y, g, c1, c2 = random_gate_batch(keys0, 5, seed=7)
+    d1 = torch.from_numpy(c1.view(np.int64)).cuda()
+    d2 = torch.from_numpy(c2.view(np.int64)).cuda()
+    dg = torch.from_numpy(g).cuda()
+    ob = torch.zeros_like(d1)
+    op = torch.zeros_like(d1)
+    ctx0.bootstrap_async(d1.data_ptr(), d2.data_ptr(), dg.data_ptr(), 5, ob.data_ptr())
+    ctx0.bootstrap_plain_async(d1.data_ptr(), d2.data_ptr(), dg.data_ptr(), 5, op.data_ptr())
+    ctx0.sync()
+    assert torch.equal(ob, op)
+    assert np.array_equal(ob.cpu().numpy().view(np.uint64), ctx0.eval_bootstrap_batch(c1, c2, g))
+
+
+def test_fpga_compat_mode(F, ctx0, keys0):
+    """The no-skip issue order of fpga_eval_bootstrap_x4..x16
+    (myfpga.cpp:1200-1210) against the oracle run the same way."""
+    x, y, g, c1, c2 = random_gate_batch(keys0, 3, seed=3)
+    out = ctx0.eval_bootstrap_batch(c1, c2, g, flags=F.FLAG_FPGA_COMPAT)
+    want, failed = keys0.oracle.eval_bootstrap_batch(c1, c2, g, keys0.btkey, keys0.kskey, fpga_compat=True)
+    assert np.array_equal(out, want)
+    truth = np.array([F.gate_truth(int(a), b, c) for a, b, c in zip(g, x, y)], dtype=np.uint8)
+    assert np.array_equal(keys0.decrypt(out), truth)
+
+
+def test_errors(F, ctx0, keys0):
+    x, y, g, c1, c2 = random_gate_batch(keys0, 2, seed=5)
+    with pytest.raises(F.FheaccError) as e:
+        ctx0.eval_bootstrap_batch(c1, c1, g)          # c1 == c2 (RLWE.cpp:727-730)
+    assert e.value.code == F.EINVAL
+    with pytest.raises(F.FheaccError):
+        ctx0.eval_bootstrap_batch(c1, c2, [7, 0])     # bad gate code
+    assert ctx0.eval_bootstrap_batch(c1[:0], c2[:0], np.zeros(0, dtype=np.int32)).shape == (0, keys0.P.n + 1)
+    res, rc = ctx0.gpu_eval_bootstrap_x4(list(c1), list(c2), list(g))   # wrong width
+    assert res is None and rc == -1
+
+
+def test_fixed_width_wrappers(F, ctx0, keys0):
+    x, y, g, c1, c2 = random_gate_batch(keys0, 4, seed=44)
+    res, rc = ctx0.gpu_eval_bootstrap_x4(list(c1), list(c2), list(g))
+    assert rc == 0
+    assert np.array_equal(np.array(res), ctx0.eval_bootstrap_batch(c1, c2, g))
+    one, rc = ctx0.gpu_eval_bootstrap_x1(c1[0], c2[0], int(g[0]))
+    assert rc == 0 and np.array_equal(one, res[0])
+
+
+def test_reference_fixture(F, ctx0, keys0):
+    """GPU outputs equal the words the reference's own eval_bootstrap produced
+    for the same seeded keys and inputs (tests/golden/make_ref_fixtures.py)."""
+    import os
+    import sys
+    gold = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, gold)
+    from make_ref_fixtures import digest, truth_table_inputs
+    fx = np.load(os.path.join(gold, "ref_bootstrap_p0.npz"))
+    x, y, g, c1, c2 = truth_table_inputs(keys0)
+    assert digest(c1, c2) == fx["inputs_sha256"].item().decode()
+    out = ctx0.eval_bootstrap_batch(c1, c2, g)
+    assert np.array_equal(out, fx["out"].astype(np.uint64))
