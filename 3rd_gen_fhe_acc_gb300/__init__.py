@@ -25,6 +25,9 @@ LIB_PATH = os.path.join(HERE, "libfheacc.so")
 OR, AND, NOR, NAND, XOR, XNOR = range(6)
 GATES = {"OR": OR, "AND": AND, "NOR": NOR, "NAND": NAND, "XOR": XOR, "XNOR": XNOR}
 FLAG_FPGA_COMPAT = 1
+FLAG_PROFILE = 2
+OPT_BR_REGS_FOR_3 = 1
+OPT_BR_CTAS_PER_SM = 2
 
 OK = 0
 EINVAL, ENOMEM, ENODEV, EIO, ETIMEDOUT, ENOKEY, EBUSY = -22, -12, -19, -5, -110, -126, -16
@@ -105,6 +108,9 @@ def lib():
             "fheacc_lwe_keyswitch_async": (ctypes.c_int, [vp, vp, sz, vp, vp]),
             "fheacc_lwe_modswitch_async": (ctypes.c_int, [vp, vp, sz, vp, vp]),
             "fheacc_sync": (ctypes.c_int, [vp, ctypes.c_uint32]),
+            "fheacc_kernel_times": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_float)]),
+            "fheacc_set_option": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
+            "fheacc_measure_imad_rate": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -366,3 +372,18 @@ class Context:
 
     def sync(self, timeout_ms=0):
         self.check(lib().fheacc_sync(self._h, timeout_ms))
+
+    def set_option(self, option, value):
+        self.check(lib().fheacc_set_option(self._h, option, value))
+
+    def kernel_times(self):
+        """(blind rotation ms, key switch ms) of the last FLAG_PROFILE call."""
+        ms = (ctypes.c_float * 2)()
+        self.check(lib().fheacc_kernel_times(self._h, ms))
+        return float(ms[0]), float(ms[1])
+
+    def measure_imad_rate(self):
+        """IMAD lane operations per second of this device."""
+        v = ctypes.c_double()
+        self.check(lib().fheacc_measure_imad_rate(self._h, ctypes.byref(v)))
+        return v.value

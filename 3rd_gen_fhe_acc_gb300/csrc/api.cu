@@ -55,7 +55,16 @@ struct DeviceGuard {
     }
 };
 
-cudaStream_t pick_stream(Context *c, void *stream) { return stream ? (cudaStream_t)stream : c->stream; }
+// NULL selects the legacy default stream, as in the CUDA runtime API.
+cudaStream_t pick_stream(Context *, void *stream) { return (cudaStream_t)stream; }
+
+// Marks the end of an asynchronous call so that fheacc_sync can wait for it.
+int mark_done(Context &c, cudaStream_t st, int rc)
+{
+    if (rc != FHEACC_OK) return rc;
+    cudaError_t e = cudaEventRecord(c.done, st);
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "event record");
+}
 
 uint32_t shoup32_companion(uint64_t w, uint64_t Q) { return (uint32_t)((w << 32) / Q); }
 
@@ -150,6 +159,19 @@ int fheacc_create(const fheacc_params *p, int device, fheacc_ctx **out)
         delete c;
         return FHEACC_EIO;
     }
+    e = cudaEventCreateWithFlags(&c->done, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("event creation failed: ") + cudaGetErrorString(e);
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return FHEACC_EIO;
+    }
+    for (int i = 0; i < 3 && e == cudaSuccess; i++) e = cudaEventCreate(&c->prof[i]);
+    if (e != cudaSuccess) {
+        g_create_error = std::string("event creation failed: ") + cudaGetErrorString(e);
+        fheacc_destroy(reinterpret_cast<fheacc_ctx *>(c));
+        return FHEACC_EIO;
+    }
     int rc = build_tables(*c);
     if (rc != FHEACC_OK) {
         g_create_error = c->err;
@@ -171,8 +193,12 @@ int fheacc_destroy(fheacc_ctx *ctx)
     cudaFree(c->d_btkey);
     cudaFree(c->d_kskey);
     cudaFree(c->d_subs);
+    cudaFree(c->accs.ptr);
     cudaFree(c->extract.ptr);
     cudaFree(c->io.ptr);
+    if (c->done) cudaEventDestroy(c->done);
+    for (auto &ev : c->prof)
+        if (ev) cudaEventDestroy(ev);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return FHEACC_OK;
@@ -221,7 +247,7 @@ int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t w
             for (size_t r = 0; r < Br; r++) {
                 const uint64_t *src = btkey + ((r * dR + j) * n + i) * rw;
                 uint32_t *dst = stage.data() + r * rw;
-                for (size_t x = 0; x < rw; x++) dst[x] = (uint32_t)(src[x] % Q);
+                for (size_t x = 0; x < rw; x++) dst[(x & ~(size_t)1023) + btile_index(x & 1023)] = (uint32_t)(src[x] % Q);
             }
             int rc = upload_u32(c, c.d_btkey + (i * dR + j) * Br * rw, stage.data(), Br * rw);
             if (rc) return rc;
@@ -286,9 +312,14 @@ static int bootstrap_device(Context &c, const uint64_t *d_c1, const uint64_t *d_
     int rc = ensure_scratch(c, c.extract, count * kExtractStride * sizeof(uint32_t));
     if (rc) return rc;
     uint32_t *ext = (uint32_t *)c.extract.ptr;
+    const bool prof = (flags & FHEACC_FLAG_PROFILE) != 0;
+    if (prof) cudaEventRecord(c.prof[0], st);
     rc = launch_blind_rotate32(c, d_c1, d_c2, d_gates, count, flags, nullptr, ext, max_ctas, st);
     if (rc) return rc;
-    return launch_lwe_keyswitch32(c, ext, count, true, d_out, st);
+    if (prof) cudaEventRecord(c.prof[1], st);
+    rc = launch_lwe_keyswitch32(c, ext, count, true, d_out, st);
+    if (prof && rc == FHEACC_OK) cudaEventRecord(c.prof[2], st);
+    return rc;
 }
 
 int fheacc_bootstrap_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
@@ -298,7 +329,8 @@ int fheacc_bootstrap_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t
     Context &c = *reinterpret_cast<Context *>(ctx);
     if (count && (!d_c1 || !d_c2 || !d_gates || !d_out)) return c.fail(FHEACC_EINVAL, "null buffer");
     DeviceGuard g(c.device);
-    return bootstrap_device(c, d_c1, d_c2, d_gates, count, d_out, flags, pick_stream(&c, stream), 0);
+    cudaStream_t st = pick_stream(&c, stream);
+    return mark_done(c, st, bootstrap_device(c, d_c1, d_c2, d_gates, count, d_out, flags, st, 0));
 }
 
 int fheacc_bootstrap_plain_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2,
@@ -315,7 +347,7 @@ int fheacc_bootstrap_plain_async(fheacc_ctx *ctx, const uint64_t *d_c1, const ui
         int rc = bootstrap_device(c, d_c1 + i * w, d_c2 + i * w, d_gates + i, 1, d_out + i * w, flags, st, 1);
         if (rc) return rc;
     }
-    return FHEACC_OK;
+    return mark_done(c, st, FHEACC_OK);
 }
 
 int fheacc_bootstrap(fheacc_ctx *ctx, const uint64_t *c1, const uint64_t *c2, const int32_t *gates, size_t count,
@@ -356,7 +388,8 @@ int fheacc_ntt_forward(fheacc_ctx *ctx, uint64_t *d_polys, size_t count, void *s
     if (!ctx) return FHEACC_EINVAL;
     Context &c = *reinterpret_cast<Context *>(ctx);
     DeviceGuard g(c.device);
-    return launch_ntt32(c, d_polys, count, false, pick_stream(&c, stream));
+    cudaStream_t st = pick_stream(&c, stream);
+    return mark_done(c, st, launch_ntt32(c, d_polys, count, false, st));
 }
 
 int fheacc_ntt_inverse(fheacc_ctx *ctx, uint64_t *d_polys, size_t count, void *stream)
@@ -364,7 +397,8 @@ int fheacc_ntt_inverse(fheacc_ctx *ctx, uint64_t *d_polys, size_t count, void *s
     if (!ctx) return FHEACC_EINVAL;
     Context &c = *reinterpret_cast<Context *>(ctx);
     DeviceGuard g(c.device);
-    return launch_ntt32(c, d_polys, count, true, pick_stream(&c, stream));
+    cudaStream_t st = pick_stream(&c, stream);
+    return mark_done(c, st, launch_ntt32(c, d_polys, count, true, st));
 }
 
 int fheacc_rlwe_mult_rgsw(fheacc_ctx *ctx, const uint64_t *d_acc, const uint64_t *d_rgsw, uint64_t *d_out,
@@ -373,7 +407,8 @@ int fheacc_rlwe_mult_rgsw(fheacc_ctx *ctx, const uint64_t *d_acc, const uint64_t
     if (!ctx) return FHEACC_EINVAL;
     Context &c = *reinterpret_cast<Context *>(ctx);
     DeviceGuard g(c.device);
-    return launch_rlwe_mult_rgsw32(c, d_acc, d_rgsw, d_out, count, pick_stream(&c, stream));
+    cudaStream_t st = pick_stream(&c, stream);
+    return mark_done(c, st, launch_rlwe_mult_rgsw32(c, d_acc, d_rgsw, d_out, count, st));
 }
 
 int fheacc_blind_rotate_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
@@ -382,7 +417,8 @@ int fheacc_blind_rotate_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint6
     if (!ctx) return FHEACC_EINVAL;
     Context &c = *reinterpret_cast<Context *>(ctx);
     DeviceGuard g(c.device);
-    return launch_blind_rotate32(c, d_c1, d_c2, d_gates, count, flags, d_acc, nullptr, 0, pick_stream(&c, stream));
+    cudaStream_t st = pick_stream(&c, stream);
+    return mark_done(c, st, launch_blind_rotate32(c, d_c1, d_c2, d_gates, count, flags, d_acc, nullptr, 0, st));
 }
 
 int fheacc_lwe_keyswitch_async(fheacc_ctx *ctx, const uint64_t *d_rlwe, size_t count, uint64_t *d_out,
@@ -396,7 +432,7 @@ int fheacc_lwe_keyswitch_async(fheacc_ctx *ctx, const uint64_t *d_rlwe, size_t c
     cudaStream_t st = pick_stream(&c, stream);
     rc = launch_extract_from_ntt32(c, d_rlwe, count, (uint32_t *)c.extract.ptr, st);
     if (rc) return rc;
-    return launch_lwe_keyswitch32(c, (uint32_t *)c.extract.ptr, count, false, d_out, st);
+    return mark_done(c, st, launch_lwe_keyswitch32(c, (uint32_t *)c.extract.ptr, count, false, d_out, st));
 }
 
 int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t count, uint64_t *d_out, void *stream)
@@ -404,7 +440,48 @@ int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t cou
     if (!ctx) return FHEACC_EINVAL;
     Context &c = *reinterpret_cast<Context *>(ctx);
     DeviceGuard g(c.device);
-    return launch_modswitch(c, d_in, count, d_out, pick_stream(&c, stream));
+    cudaStream_t st = pick_stream(&c, stream);
+    return mark_done(c, st, launch_modswitch(c, d_in, count, d_out, st));
+}
+
+int fheacc_set_option(fheacc_ctx *ctx, int option, int value)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    switch (option) {
+    case FHEACC_OPT_BR_REGS_FOR_3:
+        c.tune.br_regs_for_3 = value ? 1 : 0;
+        return FHEACC_OK;
+    case FHEACC_OPT_BR_CTAS_PER_SM:
+        if (value < 0 || value > 32) return c.fail(FHEACC_EINVAL, "CTAs per SM out of range");
+        c.tune.br_ctas_per_sm = value;
+        return FHEACC_OK;
+    default:
+        return c.fail(FHEACC_EINVAL, "unknown option");
+    }
+}
+
+int fheacc_kernel_times(fheacc_ctx *ctx, float ms[2])
+{
+    if (!ctx || !ms) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    DeviceGuard g(c.device);
+    cudaError_t e = cudaEventSynchronize(c.prof[2]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[0], c.prof[0], c.prof[1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[1], c.prof[1], c.prof[2]);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return c.cuda_fail(e, "kernel times (no profiled call yet?)");
+    }
+    return FHEACC_OK;
+}
+
+int fheacc_measure_imad_rate(fheacc_ctx *ctx, double *imad_per_s)
+{
+    if (!ctx || !imad_per_s) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    DeviceGuard g(c.device);
+    return measure_imad_rate(c, imad_per_s);
 }
 
 int fheacc_sync(fheacc_ctx *ctx, uint32_t timeout_ms)
@@ -415,6 +492,7 @@ int fheacc_sync(fheacc_ctx *ctx, uint32_t timeout_ms)
     auto t0 = std::chrono::steady_clock::now();
     for (;;) {
         cudaError_t e = cudaStreamQuery(c.stream);
+        if (e == cudaSuccess) e = cudaEventQuery(c.done);
         if (e == cudaSuccess) return FHEACC_OK;
         if (e != cudaErrorNotReady) return c.cuda_fail(e, "sync");
         if (timeout_ms) {

@@ -1,0 +1,338 @@
+// blind_rotate32.cu -- batched blind rotation of FHEW/AP gate bootstrapping,
+// N = 1024, Q < 2^27 (32-bit words).
+//
+// Reference behaviour: the accumulate loop of RLWE::eval_bootstrap
+// (FHE_ACC_runtime/src/RLWE.cpp:733-767) -- LWE_evaluate (LWE.cpp:203-222),
+// acc_initialization (RLWE.cpp:706-724), then for every LWE coefficient i and
+// refresh digit j with a non-zero residue r an RLWE_mult_RGSW (RLWE.cpp:642-704)
+// with btkey[r][j][i] -- followed by the NTT_a_transpose and inverse NTT that
+// open LWE_keyswitch (LWE.cpp:235-238). On the FPGA this loop is the host's
+// instruction issue (myfpga.cpp:1446-1492) feeding iNTT_module.sv,
+// NTT_leading_stage.sv, poly_mult_RLWE.sv and accumulator.sv.
+//
+// Schedule. The grid is persistent; CTA b owns the group of ciphertexts
+// b, b + grid, b + 2 grid, ... (at most kMaxGroup per chunk). Steps are the
+// OUTER loop: a CTA applies step s to every ciphertext of its group before
+// step s + 1, so all CTAs walk through the bootstrapping key together and the
+// 23 RGSW keys of a step (1.5 MB) are fetched from HBM about once and then
+// served from L2 to every CTA. Accumulators live in global memory (8 KB per
+// ciphertext, L2-resident for batches of thousands).
+//
+// Inside a CTA the (step, ciphertext) items flow through a two-stage warp-
+// specialised pipeline, one item per period, periods separated by
+// __syncthreads:
+//   inverse-NTT warps (2): load acc of item k+1, inverse NTT of a and b,
+//                          canonical time-domain coefficients -> tslot[k+1 & 1]
+//   digit warps (2*digitG): item k: digit h of poly p from tslot[k & 1],
+//                          forward NTT -> dbuf; named barrier; multiply-
+//                          accumulate with the item's RGSW key (64-bit sums,
+//                          one Barrett reduction per output) -> acc (global)
+// An item whose ciphertext is still in the digit stage waits one period.
+//
+// Global layouts. Accumulators and bootstrap-key polys are stored "B-tiled":
+// element 32 l + r of a poly sits at word ((r / 4) * 32 + l) * 4 + r % 4, so a
+// warp loading a poly into the NTT's contiguous register layout, and the MAC
+// threads reading keys and writing accumulators, move 512 contiguous bytes
+// per instruction.
+#include "ctx.hpp"
+#include "step32.cuh"
+#include <algorithm>
+
+namespace fheacc {
+namespace dev {
+
+constexpr int kMaxGroup = 12;   // ciphertexts per CTA and chunk (residue table in shared memory)
+
+struct PipeArgs {
+    const uint64_t *c1, *c2;
+    const int32_t *gates;
+    size_t count;
+    const uint32_t *btkey;   // B-tiled polys, [(i*digitR + j)*Br + r][digitG][2][2][1024]
+    uint32_t *accs;          // scratch [count][2][1024], B-tiled, values < 2Q
+    uint64_t *acc_out;       // optional: canonical NTT accumulators [count][2048]
+    uint32_t *extract;       // optional: [count][kExtractStride]
+    int n;
+    uint32_t q, embed, Br, digitR, bg_bits, flags;
+    uint64_t mu64;
+    uint64_t gate_constant[8];
+};
+
+// Shared memory of one CTA. tslot holds lane-major copies of the inverse-NTT
+// warps' registers (layout A), dbuf the digit NTT outputs as swizzled rows
+// (layout B); both double as the per-warp transpose scratch.
+template <int DG>
+struct PipeSmem {
+    uint32_t tslot[2][2][kN32];   // time-domain accumulators, one slot per pipeline stage
+    uint32_t dbuf[2 * DG][kN32];  // digit NTT outputs / transposes of the digit warps
+};
+
+__device__ __forceinline__ void load_btile(uint32_t (&x)[32], const uint32_t *src, int lane)
+{
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+#pragma unroll
+    for (int qq = 0; qq < 8; qq++) {
+        const uint4 v = __ldcg(s4 + qq * 32 + lane);
+        x[4 * qq] = v.x; x[4 * qq + 1] = v.y; x[4 * qq + 2] = v.z; x[4 * qq + 3] = v.w;
+    }
+}
+
+// Layout-B registers of the poly reversed in index (NTT_a_transpose).
+__device__ __forceinline__ void load_btile_reversed(uint32_t (&x)[32], const uint32_t *src, int lane)
+{
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+#pragma unroll
+    for (int qq = 0; qq < 8; qq++) {
+        const uint4 v = __ldcg(s4 + (7 - qq) * 32 + (31 - lane));
+        x[4 * qq] = v.w; x[4 * qq + 1] = v.z; x[4 * qq + 2] = v.y; x[4 * qq + 3] = v.x;
+    }
+}
+
+__device__ __forceinline__ void store_btile(uint32_t *dst, const uint32_t (&x)[32], int lane)
+{
+    uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+#pragma unroll
+    for (int qq = 0; qq < 8; qq++) __stcg(d4 + qq * 32 + lane, make_uint4(x[4 * qq], x[4 * qq + 1], x[4 * qq + 2],
+                                                                       x[4 * qq + 3]));
+}
+
+__device__ __forceinline__ void named_barrier(int id, int threads)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
+template <int DG, int MINB>
+__global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
+    br32_pipe_kernel(const __grid_constant__ PipeArgs A, const __grid_constant__ Ntt32Consts c,
+                     const uint2 *__restrict__ fwd_tw, const uint2 *__restrict__ inv_tw, uint32_t mu32)
+{
+    constexpr int GW = 2 * DG;   // digit warps
+    constexpr int NW = GW + 2;   // plus the two inverse-NTT warps
+    constexpr int GT = 32 * GW;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PipeSmem<DG> &s = *reinterpret_cast<PipeSmem<DG> *>(smem_raw);
+    uint8_t *res = smem_raw + sizeof(PipeSmem<DG>);   // [kMaxGroup][n * digitR] residues
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = A.n, S = n * (int)A.digitR;
+    const uint32_t q = A.q, qmask = q - 1;
+    const size_t rgsw_words = (size_t)DG * 4 * 1024;
+    const bool compat = (A.flags & FHEACC_FLAG_FPGA_COMPAT) != 0;
+    const size_t G = gridDim.x;
+
+    for (size_t base = 0; base < A.count; base += G * kMaxGroup) {
+        const size_t first = base + blockIdx.x;
+        int m = 0;
+        while (m < kMaxGroup && first + (size_t)m * G < A.count) m++;
+
+        // ---- prologue: LWE_evaluate, residues, acc_initialization (one warp per ciphertext)
+        for (int k = warp; k < m; k += NW) {
+            const size_t gid = first + (size_t)k * G;
+            const int g = A.gates[gid];
+            const bool x2 = (g == 4 || g == 5);
+            const uint64_t *c1 = A.c1 + gid * (size_t)(n + 1), *c2 = A.c2 + gid * (size_t)(n + 1);
+            for (int i = lane; i < n; i += 32) {
+                const uint64_t v = x2 ? 2 * (c1[i] - c2[i]) : c1[i] + c2[i];
+                uint32_t nega = (q - (uint32_t)(v & qmask)) & qmask;
+                for (uint32_t j = 0; j < A.digitR; j++) {
+                    res[k * S + i * (int)A.digitR + (int)j] = (uint8_t)(nega % A.Br);
+                    nega /= A.Br;
+                }
+            }
+            const uint64_t vb = x2 ? 2 * (c1[n] - c2[n]) : c1[n] + c2[n];
+            const uint32_t bval = (uint32_t)(vb & qmask);
+            const uint64_t gc = A.gate_constant[(unsigned)g < 6u ? g : 6];
+            const uint32_t b1 = (uint32_t)(gc & qmask), b2 = (b1 + q / 2) & qmask;
+            const uint32_t Q8 = c.Q / 8 + 1, negQ8 = c.Q - Q8;
+            uint32_t x[32];
+#pragma unroll
+            for (int r = 0; r < 32; r++) {
+                const uint32_t idx = lane + 32 * r;
+                uint32_t v = 0;
+                if (idx % A.embed == 0 && idx / A.embed < q / 2) {
+                    const uint32_t tmp = (bval - idx / A.embed) & qmask;
+                    if (b1 < b2) v = (tmp >= b1 && tmp < b2) ? negQ8 : Q8;
+                    else v = (tmp >= b2 && tmp < b1) ? Q8 : negQ8;
+                }
+                x[r] = v;
+            }
+            uint32_t *buf = warp < GW ? s.dbuf[warp] : s.tslot[0][warp - GW];
+            ntt_fwd_1024(x, c, fwd_tw, buf, lane);
+#pragma unroll
+            for (int r = 0; r < 32; r++) x[r] = reduce32(x[r], mu32, c.Q);
+            uint32_t *acc = A.accs + gid * 2048;
+            store_btile(acc + 1024, x, lane);
+            uint4 *a4 = reinterpret_cast<uint4 *>(acc);
+#pragma unroll
+            for (int qq = 0; qq < 8; qq++) __stcg(a4 + qq * 32 + lane, make_uint4(0, 0, 0, 0));
+            __syncwarp();
+        }
+        __syncthreads();
+
+        // ---- pipeline over the (step, ciphertext) items of the group
+        int hs = 0, hk = -1;   // cursor: last item taken by the inverse-NTT warps
+        int gs = -1, gk = -1;  // item of the digit warps (gk < 0: none)
+        int sh = 0;            // slot written by the inverse-NTT warps this period
+        bool hdone = (m == 0);
+        for (;;) {
+            int ns = hs, nk = hk;
+            bool found = false;
+            if (!hdone) {
+                for (;;) {
+                    if (++nk == m) {
+                        nk = 0;
+                        ++ns;
+                    }
+                    if (ns >= S) break;
+                    if (compat || res[nk * S + ns]) {
+                        found = true;
+                        break;
+                    }
+                }
+                if (!found) hdone = true;
+            }
+            const bool hv = found && !(gk >= 0 && gk == nk);
+            if (hv) {
+                hs = ns;
+                hk = nk;
+            }
+            if (!hv && gk < 0 && hdone) break;
+
+            if (warp >= GW) {
+                if (hv) {
+                    const int hp = warp - GW;
+                    uint32_t x[32];
+                    load_btile(x, A.accs + (first + (size_t)hk * G) * 2048 + hp * 1024, lane);
+                    uint32_t *ts = s.tslot[sh][hp];
+                    ntt_inv_1024(x, c, inv_tw, ts, lane);
+                    store_row(ts, lane, x);
+                }
+            } else if (gk >= 0) {
+                const int p = warp / DG, h = warp % DG;
+                const uint32_t shift = A.bg_bits * h, mask = (1u << A.bg_bits) - 1;
+                uint32_t x[32];
+                load_row(x, s.tslot[sh ^ 1][p], lane);
+#pragma unroll
+                for (int r = 0; r < 32; r++) x[r] = (x[r] >> shift) & mask;
+                ntt_fwd_1024(x, c, fwd_tw, s.dbuf[warp], lane);
+                store_row(s.dbuf[warp], lane, x);
+                named_barrier(1, GT);
+                const uint32_t rr = res[gk * S + gs];
+                const uint4 *key = reinterpret_cast<const uint4 *>(A.btkey + ((size_t)gs * A.Br + rr) * rgsw_words);
+                uint4 *acc = reinterpret_cast<uint4 *>(A.accs + (first + (size_t)gk * G) * 2048);
+                for (int u = threadIdx.x; u < 256; u += GT) {
+                    const int pa = sw_chunk(u & 31, u >> 5);   // elements 32 (u % 32) + 4 (u / 32) + 0..3
+                    uint64_t sa[4] = {0, 0, 0, 0}, sb[4] = {0, 0, 0, 0};
+#pragma unroll 1
+                    for (int pp = 0; pp < 2; pp++) {
+#pragma unroll
+                        for (int hh = 0; hh < DG; hh++) {
+                            const uint4 dv = *reinterpret_cast<const uint4 *>(s.dbuf[pp * DG + hh] + pa);
+                            const uint4 ka = __ldg(key + ((hh * 2 + pp) * 2 + 0) * 256 + u);
+                            const uint4 kb = __ldg(key + ((hh * 2 + pp) * 2 + 1) * 256 + u);
+                            sa[0] += (uint64_t)dv.x * ka.x; sb[0] += (uint64_t)dv.x * kb.x;
+                            sa[1] += (uint64_t)dv.y * ka.y; sb[1] += (uint64_t)dv.y * kb.y;
+                            sa[2] += (uint64_t)dv.z * ka.z; sb[2] += (uint64_t)dv.z * kb.z;
+                            sa[3] += (uint64_t)dv.w * ka.w; sb[3] += (uint64_t)dv.w * kb.w;
+                        }
+                    }
+                    __stcg(acc + u, make_uint4(barrett64_lazy(sa[0], A.mu64, c.Q), barrett64_lazy(sa[1], A.mu64, c.Q),
+                                               barrett64_lazy(sa[2], A.mu64, c.Q), barrett64_lazy(sa[3], A.mu64, c.Q)));
+                    __stcg(acc + 256 + u,
+                           make_uint4(barrett64_lazy(sb[0], A.mu64, c.Q), barrett64_lazy(sb[1], A.mu64, c.Q),
+                                      barrett64_lazy(sb[2], A.mu64, c.Q), barrett64_lazy(sb[3], A.mu64, c.Q)));
+                }
+            }
+            __syncthreads();
+            if (hv) {
+                gs = hs;
+                gk = hk;
+            } else {
+                gs = -1;
+                gk = -1;
+            }
+            sh ^= 1;
+        }
+
+        // ---- epilogue: NTT accumulators out, or extraction for the key switch
+        for (int t = warp; t < 2 * m; t += NW) {
+            const int k = t >> 1, P = t & 1;
+            const size_t gid = first + (size_t)k * G;
+            const uint32_t *acc = A.accs + gid * 2048 + P * 1024;
+            uint32_t x[32];
+            if (A.extract) {
+                if (P == 0) load_btile_reversed(x, acc, lane);
+                else load_btile(x, acc, lane);
+                uint32_t *buf = warp < GW ? s.dbuf[warp] : s.tslot[0][warp - GW];
+                ntt_inv_1024(x, c, inv_tw, buf, lane);
+                uint32_t *ext = A.extract + gid * kExtractStride;
+                if (P == 0) {
+#pragma unroll
+                    for (int r = 0; r < 32; r++) ext[lane + 32 * r] = x[r];
+                } else if (lane == 0) {
+                    ext[1024] = x[0];
+                }
+            } else {
+                load_btile(x, acc, lane);
+                uint64_t *out = A.acc_out + gid * 2048 + P * 1024 + 32 * lane;
+#pragma unroll
+                for (int r = 0; r < 32; r++) out[r] = min(x[r], x[r] - c.Q);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace dev
+
+static int sm_count(Context &c)
+{
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, c.device);
+    return v > 0 ? v : 1;
+}
+
+template <int DG, int MINB>
+static int launch_pipe_dg(Context &c, const dev::PipeArgs &A, int max_ctas, cudaStream_t st)
+{
+    constexpr int threads = 32 * (2 * DG + 2);
+    const size_t smem = sizeof(dev::PipeSmem<DG>) + (size_t)dev::kMaxGroup * c.p.n * c.p.digitR;
+    cudaError_t e = cudaFuncSetAttribute(dev::br32_pipe_kernel<DG, MINB>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return c.cuda_fail(e, "blind rotation smem attribute");
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::br32_pipe_kernel<DG, MINB>, threads, smem);
+    if (per_sm < 1) per_sm = 1;
+    // at least two ciphertexts per CTA keep both pipeline stages busy
+    if (c.tune.br_ctas_per_sm > 0) per_sm = std::min(per_sm, c.tune.br_ctas_per_sm);
+    size_t blocks = std::min<size_t>((size_t)sm_count(c) * per_sm, (A.count + 1) / 2);
+    if (max_ctas > 0) blocks = std::min<size_t>(blocks, (size_t)max_ctas);
+    blocks = std::max<size_t>(blocks, 1);
+    dev::br32_pipe_kernel<DG, MINB><<<(unsigned)blocks, threads, smem, st>>>(A, c.nc, c.d_fwd_tw, c.d_inv_tw,
+                                                                            (uint32_t)((1ULL << 32) / c.p.Q));
+    e = cudaGetLastError();
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "blind rotation launch");
+}
+
+int launch_blind_rotate32(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
+                          size_t count, uint32_t flags, uint64_t *d_acc_out, uint32_t *d_extract, int max_ctas,
+                          cudaStream_t st)
+{
+    if (!count) return FHEACC_OK;
+    if (!c.d_btkey) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
+    int rc = ensure_scratch(c, c.accs, count * 2048 * sizeof(uint32_t));
+    if (rc) return rc;
+    dev::PipeArgs A{};
+    A.c1 = d_c1; A.c2 = d_c2; A.gates = d_gates; A.count = count;
+    A.btkey = c.d_btkey; A.accs = (uint32_t *)c.accs.ptr; A.acc_out = d_acc_out; A.extract = d_extract;
+    A.n = c.p.n; A.q = c.p.q; A.embed = c.dp.embed; A.Br = c.p.Br; A.digitR = c.p.digitR;
+    A.bg_bits = c.p.BG_bits; A.flags = flags; A.mu64 = c.dp.mu64;
+    for (int i = 0; i < 8; i++) A.gate_constant[i] = c.dp.gate_constant[i];
+    const bool three = c.tune.br_regs_for_3 != 0;
+    switch (c.p.digitG) {
+    case 2: return three ? launch_pipe_dg<2, 3>(c, A, max_ctas, st) : launch_pipe_dg<2, 2>(c, A, max_ctas, st);
+    case 3: return three ? launch_pipe_dg<3, 3>(c, A, max_ctas, st) : launch_pipe_dg<3, 2>(c, A, max_ctas, st);
+    case 4: return three ? launch_pipe_dg<4, 3>(c, A, max_ctas, st) : launch_pipe_dg<4, 2>(c, A, max_ctas, st);
+    default: return c.fail(FHEACC_EINVAL, "digitG must be 2..4 for the 32-bit path");
+    }
+}
+
+}  // namespace fheacc

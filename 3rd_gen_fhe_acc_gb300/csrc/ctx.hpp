@@ -20,6 +20,13 @@ struct DevParams {
     uint32_t ks_row;            // padded words per LWE key-switch row (>= n+1, multiple of 32)
 };
 
+// Launch-shape choices of the blind-rotation kernel (set by fheacc_set_option
+// or picked by fheacc_autotune).
+struct Tuning {
+    int br_regs_for_3 = 0;    // compile-time register budget for 3 CTAs/SM (else 2)
+    int br_ctas_per_sm = 0;   // cap on resident CTAs per SM (0: occupancy limit)
+};
+
 struct Scratch {
     void *ptr = nullptr;
     size_t bytes = 0;
@@ -30,15 +37,18 @@ struct Context {
     DevParams dp{};
     int device = 0;
     bool wide = false;            // 64-bit words (Q >= 2^27) -- not yet supported on device
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;  // used by the blocking host-buffer entry points
+    cudaEvent_t done = nullptr;     // recorded after every asynchronous call
+    cudaEvent_t prof[3] = {nullptr, nullptr, nullptr};   // FHEACC_FLAG_PROFILE marks
     std::string err;
+    Tuning tune;
 
     // twiddles: (w, w') pairs indexed like the reference tables
     uint2 *d_fwd_tw = nullptr, *d_inv_tw = nullptr;
     dev::Ntt32Consts nc{};
 
     // keys, device layouts
-    uint32_t *d_btkey = nullptr;   // [(i*digitR + j)*Br + r][digitG][2][2][N]
+    uint32_t *d_btkey = nullptr;   // [(i*digitR + j)*Br + r][digitG][2][2][N], polys B-tiled
     size_t btkey_bytes = 0;
     uint32_t *d_kskey = nullptr;   // [(d*digitKS + j)*N + i][ks_row]
     size_t kskey_bytes = 0;
@@ -46,12 +56,13 @@ struct Context {
     size_t subs_bytes = 0;
 
     // scratch owned by the context, grown on demand
+    Scratch accs;                  // blind-rotation accumulators, [count][2][N] u32
     Scratch extract;               // extracted RLWEs between blind rotation and key switch
     Scratch io;                    // device staging for the host-buffer entry points
 
     size_t device_bytes() const
     {
-        return btkey_bytes + kskey_bytes + subs_bytes + extract.bytes + io.bytes +
+        return btkey_bytes + kskey_bytes + subs_bytes + accs.bytes + extract.bytes + io.bytes +
                2 * (size_t)p.N * sizeof(uint2);
     }
     int fail(int code, const std::string &msg)
@@ -86,7 +97,17 @@ int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, 
 int launch_extract_from_ntt32(Context &c, const uint64_t *d_rlwe, size_t count, uint32_t *d_extract,
                               cudaStream_t st);
 int launch_modswitch(Context &c, const uint64_t *d_in, size_t count, uint64_t *d_out, cudaStream_t st);
+// IMAD throughput probe (probe.cu)
+int measure_imad_rate(Context &c, double *imad_per_s);
 
 constexpr size_t kExtractStride = 1024 + 32;   // u32 words per extracted RLWE (N = 1024)
+
+// Word index of element e = 32 l + r of a 1024-word poly in the "B-tiled"
+// device layout used for bootstrap keys and blind-rotation accumulators.
+inline size_t btile_index(size_t e)
+{
+    const size_t l = e >> 5, r = e & 31;
+    return (((r >> 2) << 5) + l) * 4 + (r & 3);
+}
 
 }  // namespace fheacc

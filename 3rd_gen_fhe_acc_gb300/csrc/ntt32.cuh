@@ -13,9 +13,8 @@
 // where every lane uses the same twiddle (taken from the kernel's parameter
 // bank), one padded shared-memory transpose, and the last five stages
 // (t = 16..1) in layout B with per-lane twiddles read through L1. The inverse
-// runs the same way backwards. Shared-memory addresses are padded by one word
-// per 32 (element e at e + e/32), so both transpose directions are free of bank
-// conflicts.
+// runs the same way backwards. The transpose goes through a swizzled shared-
+// memory tile: rows move as 128-bit chunks, columns as conflict-free words.
 //
 // Modular arithmetic: Shoup multiplication by precomputed (w, w' =
 // floor(w 2^32 / Q)) gives x*w mod Q in [0, 2Q) for any 32-bit x. The forward
@@ -135,31 +134,54 @@ __device__ __forceinline__ void inv_stage_A(uint32_t (&x)[32], const Ntt32Consts
     }
 }
 
-// Layout A -> B through a padded per-warp buffer (kPadN words).
+// Swizzled 32 x 32 tile of a 1024-word poly (no padding): element e in row
+// e / 32, column e % 32 sits at  row * 32 + ((col / 4) ^ (row % 8)) * 4 + col % 4.
+// A lane reading or writing a whole row (layout B, or any lane-major copy)
+// moves 8 conflict-free 128-bit chunks; a warp touching one element of every
+// column of a row (layout A) hits 32 distinct banks.
+__device__ __forceinline__ int sw_addr(int row, int col) { return (row << 5) + ((((col >> 2) ^ (row & 7))) << 2) + (col & 3); }
+__device__ __forceinline__ int sw_chunk(int row, int k) { return (row << 5) + ((k ^ (row & 7)) << 2); }
+
+__device__ __forceinline__ void store_row(uint32_t *buf, int row, const uint32_t (&x)[32])
+{
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        *reinterpret_cast<uint4 *>(buf + sw_chunk(row, k)) = make_uint4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]);
+}
+
+__device__ __forceinline__ void load_row(uint32_t (&x)[32], const uint32_t *buf, int row)
+{
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const uint4 v = *reinterpret_cast<const uint4 *>(buf + sw_chunk(row, k));
+        x[4 * k] = v.x; x[4 * k + 1] = v.y; x[4 * k + 2] = v.z; x[4 * k + 3] = v.w;
+    }
+}
+
+// Layout A -> B through a per-warp buffer of 1024 words (16-byte aligned).
 __device__ __forceinline__ void transpose_A_to_B(uint32_t (&x)[32], uint32_t *buf, int lane)
 {
     __syncwarp();
 #pragma unroll
-    for (int r = 0; r < 32; r++) buf[33 * r + lane] = x[r];
+    for (int r = 0; r < 32; r++) buf[sw_addr(r, lane)] = x[r];
     __syncwarp();
-#pragma unroll
-    for (int r = 0; r < 32; r++) x[r] = buf[33 * lane + r];
+    load_row(x, buf, lane);
     __syncwarp();
 }
 
 __device__ __forceinline__ void transpose_B_to_A(uint32_t (&x)[32], uint32_t *buf, int lane)
 {
     __syncwarp();
-#pragma unroll
-    for (int r = 0; r < 32; r++) buf[33 * lane + r] = x[r];
+    store_row(buf, lane, x);
     __syncwarp();
 #pragma unroll
-    for (int r = 0; r < 32; r++) x[r] = buf[33 * r + lane];
+    for (int r = 0; r < 32; r++) x[r] = buf[sw_addr(r, lane)];
     __syncwarp();
 }
 
 // Forward NTT: x in layout A (values < Q) -> layout B, values < 21Q, in the
-// reference's bit-reversed output order. buf: kPadN words of scratch.
+// reference's bit-reversed output order. buf: 1024 words of 16-byte aligned
+// scratch.
 __device__ __forceinline__ void ntt_fwd_1024(uint32_t (&x)[32], const Ntt32Consts &c,
                                              const uint2 *__restrict__ fwd_tw, uint32_t *buf, int lane)
 {

@@ -1,0 +1,422 @@
+"""Gate-bootstrapping throughput on GB300.
+
+One step = one batched gate-bootstrapping pass over a fixed synthetic batch:
+4096 independent NAND gates with the n=500, N=1024, Q=134215681 (uint32),
+BG=2^7 x4 parameter set, keys and inputs generated from fixed seeds.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line. `value` is bootstraps/s with inputs resident in HBM,
+timed with CUDA events on the launching stream (L2 flushed between steps);
+`e2e` is the same metric through the host-buffer C-ABI call fheacc_bootstrap
+(host->device copies, the kernels and device->host copies inside the timed
+region). `--impl reference` times the CPU restatement of the reference's
+eval_bootstrap (oracle/) on all host cores on the same workload.
+Under torchrun every rank bootstraps its own batch on its own GPU (the gates
+are independent: no collective on the data path) and rank 0 reports the
+aggregate over the max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+METRIC = "gate bootstraps/sec on 1 GB300 (batched persistent vs plain per-gate launch, bit-exact); p99 ms"
+SEEDS = dict(lwe_sk=1, rlwe_sk=2, btkey=3, kskey=4, enc=5)
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic.json")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self, use_cuda):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("nccl" if use_cuda else "gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, x):
+        if self.ws == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def steps_of(c1, c2, gates, P):
+    """Exact number of RLWE x RGSW steps of each gate (RLWE.cpp:754-767)."""
+    q = P.q
+    a1 = c1[:, :P.n].astype(np.int64)
+    a2 = c2[:, :P.n].astype(np.int64)
+    x2 = ((gates == 4) | (gates == 5))[:, None]
+    a = np.where(x2, 2 * (a1 - a2), a1 + a2) % q
+    nega = (q - a) % q
+    steps = np.zeros(c1.shape[0], dtype=np.int64)
+    for _ in range(P.digitR):
+        steps += (nega % P.Br != 0).sum(axis=1)
+        nega //= P.Br
+    return steps
+
+
+def make_inputs(F, P, batch, rank):
+    lsk = F.LWE_secretkey(P, SEEDS["lwe_sk"])
+    rsk = F.RLWE_secretkey(P, SEEDS["rlwe_sk"])
+    rng = np.random.default_rng(1000 + rank)
+    x = rng.integers(0, 2, batch).astype(np.uint8)
+    y = rng.integers(0, 2, batch).astype(np.uint8)
+    c = F.LWE_encrypt(P, SEEDS["enc"] + 7919 * rank, lsk, np.concatenate([x, y]))
+    gates = np.full(batch, F.NAND, dtype=np.int32)
+    return lsk, rsk, x, y, c[:batch].copy(), c[batch:].copy(), gates
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference(args):
+    """CPU restatement of eval_bootstrap (oracle/), all host cores."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import __graft_entry__
+    __graft_entry__.build_product()
+    __graft_entry__._build_oracle()
+    import importlib
+    F = importlib.import_module("3rd_gen_fhe_acc_gb300")
+    from oracle_lib import Oracle
+    P = F.params_preset(args.preset)
+    lsk, rsk, x, y, c1, c2, gates = make_inputs(F, P, args.batch, 0)
+    bt = F.bootstrap_key(P, SEEDS["btkey"], lsk, rsk)
+    ks = F.keyswitch_key(P, SEEDS["kskey"], rsk, lsk)
+    ora = Oracle.from_params(P)
+    cores = cpu_cores()
+    per_step = args.cpu_sample or 2 * cores
+    times = []
+    for s in range(args.warmup + args.steps):
+        lo = (s * per_step) % max(args.batch - per_step, 1)
+        t0 = time.perf_counter()
+        out, failed = ora.eval_bootstrap_batch(c1[lo:lo + per_step], c2[lo:lo + per_step], gates[lo:lo + per_step],
+                                               bt, ks, threads=cores)
+        dt = time.perf_counter() - t0
+        assert failed == 0
+        if s >= args.warmup:
+            times.append(dt)
+    value = per_step / statistics.mean(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "bootstraps/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": config_of(P, args),
+        "cpu_baseline": {"value": value, "unit": "bootstraps/s", "cores": cores, "kind": "port",
+                         "sample": "%d gates per step of the %d-gate batch, oracle eval_bootstrap "
+                                   "(C restatement of RLWE.cpp:726-786) on %d threads" % (per_step, args.batch,
+                                                                                        cores)},
+        "e2e": {"value": value, "unit": "bootstraps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def config_of(P, args):
+    return {"workload": "%d independent NAND-gate bootstraps: n=%d, N=%d, Q=%d (uint32 words), BG=2^%d x%d, "
+                        "Br=%d x%d, Bks=%d x%d, q=%d; keys and input bits from fixed seeds" % (
+                            args.batch, P.n, P.N, P.Q, P.BG_bits, P.digitG, P.Br, P.digitR, P.Bks, P.digitKS, P.q),
+            "batch": args.batch, "gate": "NAND", "n": P.n, "N": P.N, "Q": P.Q,
+            "l2": "flushed between timed steps (write of a 512 MiB buffer); keys (1.8 GB) exceed L2",
+            "parallelism": "one batch per GPU (independent gates, no collective)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--preset", type=int, default=0)
+    ap.add_argument("--plain-sample", type=int, default=48)
+    ap.add_argument("--cpu-sample", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import __graft_entry__
+    __graft_entry__.build_product()
+    import importlib
+    F = importlib.import_module("3rd_gen_fhe_acc_gb300")
+    D = Dist(use_cuda=True)
+    dev_id = D.local if D.ws > 1 else 0
+    torch.cuda.set_device(dev_id)
+    P = F.params_preset(args.preset)
+    B = args.batch
+    lsk, rsk, x, y, c1, c2, gates = make_inputs(F, P, B, D.rank)
+    bt = F.bootstrap_key(P, SEEDS["btkey"], lsk, rsk)
+    ks = F.keyswitch_key(P, SEEDS["kskey"], rsk, lsk)
+    ctx = F.Context(P, dev_id)
+    ctx.upload_bootstrap_key(bt)
+    ctx.upload_keyswitch_key(ks)
+    W = P.n + 1
+    stream = torch.cuda.current_stream()
+    st = stream.cuda_stream
+    d1 = torch.from_numpy(c1.view(np.int64)).cuda()
+    d2 = torch.from_numpy(c2.view(np.int64)).cuda()
+    dg = torch.from_numpy(gates).cuda()
+    dout = torch.zeros_like(d1)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    truth = np.array([F.gate_truth(int(g), a, b) for g, a, b in zip(gates, x, y)], dtype=np.uint8)
+
+    def step_device(profile):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.bootstrap_async(d1.data_ptr(), d2.data_ptr(), dg.data_ptr(), B, dout.data_ptr(),
+                            F.FLAG_PROFILE if profile else 0, st)
+        e1.record(stream)
+        return e0, e1
+
+    # warm-up, device-resident
+    for _ in range(args.warmup):
+        flush.fill_(1)
+        step_device(False)
+    torch.cuda.synchronize()
+    out0 = dout.cpu().numpy().view(np.uint64).copy()
+    dec_ok = int((F.LWE_decrypt(P, lsk, out0) == truth).sum())
+
+    # timed region: K steps, device-resident inputs
+    imad = ctx.measure_imad_rate()
+    clocks = ClockSampler(dev_id)
+    clocks.start()
+    step_ms, br_ms, ks_ms = [], [], []
+    D.barrier()
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0, e1 = step_device(True)
+        torch.cuda.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        b, k = ctx.kernel_times()
+        br_ms.append(b)
+        ks_ms.append(k)
+    torch.cuda.synchronize()
+    D.barrier()
+    clk = clocks.stop()
+    total_s = D.max(sum(step_ms) / 1e3)
+    value = D.ws * B * args.steps / total_s
+    same = np.array_equal(dout.cpu().numpy().view(np.uint64), out0)
+
+    # e2e: host buffers through the C ABI (pinned host memory)
+    h1 = torch.from_numpy(c1.view(np.int64)).pin_memory()
+    h2 = torch.from_numpy(c2.view(np.int64)).pin_memory()
+    hg = torch.from_numpy(gates).pin_memory()
+    ho = torch.zeros_like(h1).pin_memory()
+    n1, n2, ng, no = (t.numpy() for t in (h1, h2, hg, ho))
+    e2e_s = []
+    for s in range(args.warmup + args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = F.lib().fheacc_bootstrap(ctx.handle, n1.ctypes.data_as(F._u64p), n2.ctypes.data_as(F._u64p),
+                                     ng.ctypes.data_as(F._i32p), B, no.ctypes.data_as(F._u64p), 0)
+        dt = time.perf_counter() - t0
+        ctx.check(r)
+        if s >= args.warmup:
+            e2e_s.append(dt)
+    D.barrier()
+    e2e_total = D.max(sum(e2e_s))
+    e2e_value = D.ws * B * args.steps / e2e_total
+    e2e_same = np.array_equal(no.view(np.uint64), out0)
+
+    # plain form: one launch sequence per gate
+    Pn = min(args.plain_sample, B)
+    ctx.bootstrap_plain_async(d1.data_ptr(), d2.data_ptr(), dg.data_ptr(), 4, dout.data_ptr(), 0, st)
+    torch.cuda.synchronize()
+    lat = []
+    for i in range(Pn):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        off = i * W
+        ctx.bootstrap_plain_async(d1.data_ptr() + 8 * off, d2.data_ptr() + 8 * off, dg.data_ptr() + 4 * i, 1,
+                                  dout.data_ptr() + 8 * off, 0, st)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        lat.append(e0.elapsed_time(e1))
+    plain_value = Pn / (sum(lat) / 1e3)
+    plain_ok = np.array_equal(dout.cpu().numpy().view(np.uint64)[:Pn], out0[:Pn])
+
+    # roofline of the dominant kernel (blind rotation)
+    steps = steps_of(c1, c2, gates, P)
+    total_steps = int(steps.sum())
+    N, dG = P.N, P.digitG
+    logN = N.bit_length() - 1
+    # 2 inverse + 2*digitG forward NTTs, the MAC products, and the N^-1 scaling
+    # of the two inverse NTTs: 69,632 per step for this parameter set
+    modmul_per_step = (2 + 2 * dG) * (N // 2) * logN + 2 * (2 * dG) * N + 2 * N
+    br_s = statistics.mean(br_ms) / 1e3
+    achieved_modmul = total_steps * modmul_per_step / br_s
+    peak_modmul = imad / 4.0
+    rgsw_bytes = 2 * dG * 2 * N * 4
+    btkey_bytes = P.Br * P.digitR * P.n * rgsw_bytes
+    traffic = None
+    if os.path.exists(TRAFFIC_FILE):
+        with open(TRAFFIC_FILE) as f:
+            tj = json.load(f)
+        traffic = tj.get("blind_rotate32", {}).get("bytes_per_launch_4096")
+    hbm_peak = None
+    peaks_src = "fallback 6800 GB/s"
+    if os.path.exists(PEAKS_FILE):
+        with open(PEAKS_FILE) as f:
+            hbm_peak = json.load(f).get("hbm_gbs")
+            peaks_src = "measured (MEASURED_PEAKS.json hbm_gbs)"
+    hbm_peak = hbm_peak or 6800.0
+    key_stream_gbs = total_steps * rgsw_bytes / br_s / 1e9
+    roofline = {
+        "bound": "int", "achieved": achieved_modmul / 1e9, "peak": peak_modmul / 1e9, "unit": "G modmul/s",
+        "frac": achieved_modmul / peak_modmul, "traffic": traffic,
+        "kernel": "blind_rotate32_kernel", "kernel_ms": statistics.mean(br_ms),
+        "work": "%d RLWE x RGSW steps x %d modular multiplies (NTT butterflies, MAC products, N^-1 scaling)" % (
+            total_steps, modmul_per_step),
+        "peak_source": "IMAD rate measured in this run (%.1f T lane-op/s) / 4 IMAD issue slots per Shoup "
+                       "modular multiply (mul.hi counts 2)" % (imad / 1e12),
+    }
+    roofline_hbm = {
+        "bound": "hbm", "achieved": btkey_bytes / br_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
+        "frac": btkey_bytes / br_s / 1e9 / hbm_peak, "traffic": traffic,
+        "algorithmic_bytes": btkey_bytes, "peak_source": peaks_src,
+        "key_stream_gbs": key_stream_gbs, "key_stream_frac": key_stream_gbs / hbm_peak,
+        "note": "algorithmic bytes = bootstrap key read once per launch; key_stream = RGSW bytes consumed by "
+                "all steps of all gates (served mostly from L2)",
+    }
+
+    cpu = None
+    if D.rank == 0 and D.ws == 1 and not args.no_cpu:
+        import __graft_entry__ as ge
+        ge._build_oracle()
+        from oracle_lib import Oracle
+        ora = Oracle.from_params(P)
+        cores = cpu_cores()
+        nsample = args.cpu_sample or 8 * cores
+        t0 = time.perf_counter()
+        co, failed = ora.eval_bootstrap_batch(c1[:nsample], c2[:nsample], gates[:nsample], bt, ks, threads=cores)
+        dt = time.perf_counter() - t0
+        cpu = {"value": nsample / dt, "unit": "bootstraps/s", "cores": cores, "kind": "port",
+               "sample": "first %d gates of the batch, oracle eval_bootstrap (C restatement of "
+                         "RLWE.cpp:726-786) on %d threads, %.1f s" % (nsample, cores, dt),
+               "bitexact_vs_gpu": "%d/%d" % (int((co == out0[:nsample]).all(axis=1).sum()), nsample)}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "bootstraps/s", "n_gpus": D.ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": config_of(P, args),
+        "e2e": {"value": e2e_value, "unit": "bootstraps/s",
+                "h2d_bytes_per_step": int(2 * B * W * 8 + B * 4), "d2h_bytes_per_step": int(B * W * 8),
+                "ms_per_step": 1e3 * statistics.mean(e2e_s)},
+        "roofline": roofline, "roofline_hbm": roofline_hbm,
+        "cpu_baseline": cpu, "clocks": clk,
+        "gpu_launches": 2 * args.steps,
+        "plain": {"value": plain_value, "unit": "bootstraps/s", "gates": Pn,
+                  "latency_ms_p50": statistics.median(lat), "latency_ms_p99": float(np.percentile(lat, 99)),
+                  "batched_over_plain": value / plain_value / D.ws},
+        "batch_latency_ms_p50": statistics.median(step_ms), "batch_latency_ms_p99": float(np.percentile(step_ms, 99)),
+        "checks": {"decrypt_ok": "%d/%d" % (dec_ok, B), "steps_repeatable": bool(same), "e2e_equal": bool(e2e_same),
+                   "plain_equal": bool(plain_ok), "kernel_ms": {"blind_rotate": statistics.mean(br_ms),
+                                                                "keyswitch": statistics.mean(ks_ms)}},
+    }
+    if D.rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    D.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

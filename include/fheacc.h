@@ -41,6 +41,9 @@ extern "C" {
 #define FHEACC_FLAG_FPGA_COMPAT 1u  /* also apply residue-0 keys, as
                                        fpga_eval_bootstrap_x4..x16 do
                                        (myfpga.cpp:1200-1210) */
+#define FHEACC_FLAG_PROFILE     2u  /* record CUDA events around each kernel of
+                                       the call, on the launching stream;
+                                       read them with fheacc_kernel_times */
 
 enum fheacc_gate { FHEACC_OR = 0, FHEACC_AND, FHEACC_NOR, FHEACC_NAND, FHEACC_XOR, FHEACC_XNOR };
 
@@ -145,8 +148,10 @@ int fheacc_upload_subs_key(fheacc_ctx *ctx, const uint64_t *subs_key, size_t wor
  * FHEACC_EINVAL (the CPU path exits, the FPGA path returns rc = -1). */
 int fheacc_bootstrap(fheacc_ctx *ctx, const uint64_t *c1, const uint64_t *c2,
                      const int32_t *gates, size_t count, uint64_t *out, uint32_t flags);
-/* Same, DEVICE buffers, asynchronous on `stream` (cudaStream_t, NULL = the
- * context's stream). Inputs are not checked for c1 == c2. */
+/* Same, DEVICE buffers, asynchronous on `stream` (a cudaStream_t; NULL is the
+ * legacy default stream, as in the CUDA runtime). Inputs are not checked for
+ * c1 == c2. All *_async calls and the sub-steps below follow the same stream
+ * rule; fheacc_sync waits for the most recent of them. */
 int fheacc_bootstrap_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2,
                            const int32_t *d_gates, size_t count, uint64_t *d_out,
                            uint32_t flags, void *stream);
@@ -177,7 +182,25 @@ int fheacc_lwe_keyswitch_async(fheacc_ctx *ctx, const uint64_t *d_rlwe, size_t c
 int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t count,
                                uint64_t *d_out, void *stream);
 
-/* Wait for all work of the context, at most timeout_ms (0 = no limit). */
+/* Launch-shape options of the blind-rotation kernel.
+ *  FHEACC_OPT_BR_REGS_FOR_3 : 1 = build for 3 resident CTAs per SM (64
+ *                             registers per thread), 0 = 2 CTAs per SM
+ *  FHEACC_OPT_BR_CTAS_PER_SM: cap on resident CTAs per SM, 0 = occupancy limit */
+#define FHEACC_OPT_BR_REGS_FOR_3  1
+#define FHEACC_OPT_BR_CTAS_PER_SM 2
+int fheacc_set_option(fheacc_ctx *ctx, int option, int value);
+
+/* Per-kernel device times (ms) of the most recent call made with
+ * FHEACC_FLAG_PROFILE: ms[0] blind rotation, ms[1] key switch + modulus
+ * switch. Waits for that call to finish. */
+int fheacc_kernel_times(fheacc_ctx *ctx, float ms[2]);
+/* Measures this device's 32-bit integer multiply-add throughput (IMAD lane
+ * operations per second) with a short dependent-chain kernel of this library;
+ * the denominator of the integer roofline. */
+int fheacc_measure_imad_rate(fheacc_ctx *ctx, double *imad_per_s);
+
+/* Wait until the most recent asynchronous call of the context (and every
+ * blocking call) has finished, at most timeout_ms (0 = no limit). */
 int fheacc_sync(fheacc_ctx *ctx, uint32_t timeout_ms);
 
 #ifdef __cplusplus

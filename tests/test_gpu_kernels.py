@@ -75,7 +75,8 @@ def test_rlwe_mult_rgsw_random(F, ctx0, keys0, cuda_ok):
     rgsw = rng.integers(0, Q, (count, 4 * 4 * 1024), dtype=np.uint64)
     rgsw[1] = Q - 1
     out = torch.zeros((count, 2048), dtype=torch.int64, device="cuda")
-    ctx0.rlwe_mult_rgsw(dev(torch, acc).data_ptr(), dev(torch, rgsw).data_ptr(), out.data_ptr(), count)
+    da, dr = dev(torch, acc), dev(torch, rgsw)   # keep the inputs alive until the kernel has run
+    ctx0.rlwe_mult_rgsw(da.data_ptr(), dr.data_ptr(), out.data_ptr(), count)
     torch.cuda.synchronize()
     want = np.stack([o.rlwe_mult_rgsw(acc[i], rgsw[i]) for i in range(count)])
     assert np.array_equal(host(out), want)
@@ -86,7 +87,8 @@ def test_blind_rotate_vs_oracle(F, ctx0, keys0, cuda_ok):
     x, y, g, c1, c2 = random_gate_batch(keys0, 6, seed=21, gates=[0, 1, 2, 3, 4, 5])
     acc = torch.zeros((6, 2048), dtype=torch.int64, device="cuda")
     dg = torch.from_numpy(g).cuda()
-    ctx0.blind_rotate_async(dev(torch, c1).data_ptr(), dev(torch, c2).data_ptr(), dg.data_ptr(), 6, acc.data_ptr())
+    d1, d2 = dev(torch, c1), dev(torch, c2)
+    ctx0.blind_rotate_async(d1.data_ptr(), d2.data_ptr(), dg.data_ptr(), 6, acc.data_ptr())
     ctx0.sync()
     got = host(acc)
     for i in range(6):
@@ -103,7 +105,8 @@ def test_lwe_keyswitch_and_modswitch(F, ctx0, keys0, cuda_ok):
     count = 5
     rlwe = rng.integers(0, Q, (count, 2048), dtype=np.uint64)
     out = torch.zeros((count, keys0.P.n + 1), dtype=torch.int64, device="cuda")
-    ctx0.lwe_keyswitch_async(dev(torch, rlwe).data_ptr(), count, out.data_ptr())
+    dr = dev(torch, rlwe)
+    ctx0.lwe_keyswitch_async(dr.data_ptr(), count, out.data_ptr())
     ctx0.sync()
     ks = host(out)
     want = np.stack([o.lwe_keyswitch(rlwe[i], keys0.kskey) for i in range(count)])

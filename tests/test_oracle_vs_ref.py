@@ -71,21 +71,18 @@ def test_eval_bootstrap(pair, keys0):
     r.free_keys()
 
 
-def test_substitute_keyswitch_expand_small(F):
-    """RLWE_substitute, RLWE_keyswitch and expand_RLWE at N=256 (the
-    reference code takes any power-of-two N)."""
-    P = F.params_preset(0)
-    P.N, P.Q, P.ROU, P.iN, P.n = 256, 0, 0, 0, 16
-    P.digitG = P.digitKS = P.digitKS_R = 0
-    F.derive(P)
-    o = Oracle.from_params(P)
+def test_substitute_keyswitch_expand(F, keys0):
+    """RLWE_substitute, RLWE_keyswitch and expand_RLWE at N=1024. (The
+    reference builds its rotation polys for N >= 1024 only: rotate_vector_gen,
+    params.cpp:177-210, indexes N - 2^j for j < 11.)"""
+    P = keys0.P
+    o = keys0.oracle
     r = Ref(o)
-    rsk = F.RLWE_secretkey(P, 1)
-    subs = F.substitute_key(P, 2, rsk)
+    subs = keys0.subs
     rng = np.random.default_rng(4)
     c = rng.integers(0, P.Q, 2 * P.N, dtype=np.uint64)
     kw = int(P.digitKS_R) * 2 * P.N
-    for f in range(3):
+    for f in (0, 3, 9):
         s1 = o.rlwe_substitute(c, f)
         assert np.array_equal(s1, r.rlwe_substitute(c, f))
         assert np.array_equal(o.rlwe_keyswitch(s1, subs[f * kw:(f + 1) * kw]),
