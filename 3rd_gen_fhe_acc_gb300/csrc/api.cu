@@ -74,11 +74,20 @@ int build_tables(Context &c)
     T.build(c.p);
     const int N = c.p.N;
     const uint64_t Q = c.p.Q;
-    std::vector<uint2> fw(N), iw(N);
-    for (int i = 0; i < N; i++) {
-        fw[i] = make_uint2((uint32_t)T.rou[i], shoup32_companion(T.rou[i], Q));
-        iw[i] = make_uint2((uint32_t)T.irou[i], shoup32_companion(T.irou[i], Q));
-    }
+    // Lane-interleaved per-lane twiddles of the layout-B NTT stages (see
+    // load_stage_twiddles in ntt32.cuh): entry m + G*lane + g at
+    // off + (g/2)*64 + 2*lane + g%2.
+    std::vector<uint2> fw(N, make_uint2(0, 0)), iw(N, make_uint2(0, 0));
+    auto put = [&](std::vector<uint2> &dst, const std::vector<uint64_t> &tab, int off, int m, int G) {
+        for (int lane = 0; lane < 32; lane++)
+            for (int g = 0; g < G; g++) {
+                const uint64_t w = tab[m + G * lane + g];
+                const int at = G == 1 ? off + lane : off + (g / 2) * 64 + 2 * lane + (g % 2);
+                dst[at] = make_uint2((uint32_t)w, shoup32_companion(w, Q));
+            }
+    };
+    for (int s = 5; s <= 9; s++) put(fw, T.rou, 32 * ((1 << (s - 5)) - 1), 1 << s, 16 >> (9 - s));
+    for (int t = 1; t <= 16; t *= 2) put(iw, T.irou, 32 * (32 - 32 / t), 512 / t, 16 / t);
     cudaError_t e = cudaMalloc(&c.d_fwd_tw, N * sizeof(uint2));
     if (e == cudaSuccess) e = cudaMalloc(&c.d_inv_tw, N * sizeof(uint2));
     if (e == cudaSuccess) e = cudaMemcpy(c.d_fwd_tw, fw.data(), N * sizeof(uint2), cudaMemcpyHostToDevice);

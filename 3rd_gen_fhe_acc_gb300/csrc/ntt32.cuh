@@ -12,7 +12,8 @@
 // The forward transform runs its first five stages (t = 512..32) in layout A,
 // where every lane uses the same twiddle (taken from the kernel's parameter
 // bank), one padded shared-memory transpose, and the last five stages
-// (t = 16..1) in layout B with per-lane twiddles read through L1. The inverse
+// (t = 16..1) in layout B with per-lane twiddles read through L1 from
+// lane-interleaved tables (coalesced warp loads). The inverse
 // runs the same way backwards. The transpose goes through a swizzled shared-
 // memory tile: rows move as 128-bit chunks, columns as conflict-free words.
 //
@@ -82,16 +83,36 @@ __device__ __forceinline__ void fwd_stage_A(uint32_t (&x)[32], const Ntt32Consts
     }
 }
 
-// Forward stage s (5..9) in layout B. tw: (w, w') pairs indexed by m + i.
+// Per-lane twiddles of the layout-B stages come from "lane-interleaved"
+// tables (built by the host, see fheacc::build_tables): a stage in which every
+// lane needs G consecutive table entries m + G*lane + g stores entry (g, lane)
+// at (g / 2) * 64 + 2 * lane + g % 2, so each warp load reads 256 or 512
+// contiguous bytes. Forward stages s = 5..9 (G = 1..16) start at
+// 32 * (2^(s-5) - 1); inverse stages t = 1..16 (G = 16/t) at 32 * (32 - 32/t).
+template <int G, int OFF>
+__device__ __forceinline__ void load_stage_twiddles(uint2 (&w)[G], const uint2 *__restrict__ tw, int lane)
+{
+    if (G == 1) {
+        w[0] = __ldg(tw + OFF + lane);
+    } else {
+        const uint4 *t4 = reinterpret_cast<const uint4 *>(tw + OFF);
+#pragma unroll
+        for (int gg = 0; gg < G / 2; gg++) {
+            const uint4 v = __ldg(t4 + gg * 32 + lane);
+            w[2 * gg] = make_uint2(v.x, v.y);
+            w[2 * gg + 1] = make_uint2(v.z, v.w);
+        }
+    }
+}
+
+// Forward stage s (5..9) in layout B.
 template <int S>
 __device__ __forceinline__ void fwd_stage_B(uint32_t (&x)[32], const uint2 *__restrict__ tw, int lane,
                                             uint32_t Q, uint32_t twoQ)
 {
-    constexpr int t = 512 >> S, m = 1 << S, G = 16 / t;   // G twiddles per lane
+    constexpr int t = 512 >> S, G = 16 / t;   // G twiddles per lane
     uint2 w[G];
-    const uint2 *base = tw + m + lane * G;
-#pragma unroll
-    for (int g = 0; g < G; g++) w[g] = __ldg(base + g);
+    load_stage_twiddles<G, 32 * ((1 << (S - 5)) - 1)>(w, tw, lane);
 #pragma unroll
     for (int r = 0; r < 32; r++) {
         if (!(r & t)) {
@@ -106,11 +127,9 @@ template <int T>
 __device__ __forceinline__ void inv_stage_B(uint32_t (&x)[32], const uint2 *__restrict__ tw, int lane,
                                             uint32_t Q, uint32_t twoQ)
 {
-    constexpr int m = 512 / T, G = 16 / T;
+    constexpr int G = 16 / T;
     uint2 w[G];
-    const uint2 *base = tw + m + lane * G;
-#pragma unroll
-    for (int g = 0; g < G; g++) w[g] = __ldg(base + g);
+    load_stage_twiddles<G, 32 * (32 - 32 / T)>(w, tw, lane);
 #pragma unroll
     for (int r = 0; r < 32; r++) {
         if (!(r & T)) {
