@@ -26,6 +26,7 @@ OR, AND, NOR, NAND, XOR, XNOR = range(6)
 GATES = {"OR": OR, "AND": AND, "NOR": NOR, "NAND": NAND, "XOR": XOR, "XNOR": XNOR}
 FLAG_FPGA_COMPAT = 1
 FLAG_PROFILE = 2
+NOALLOC_MAX_GATES = 64
 OPT_BR_REGS_FOR_3 = 1
 OPT_BR_CTAS_PER_SM = 2
 
@@ -101,6 +102,7 @@ def lib():
             "fheacc_bootstrap": (ctypes.c_int, [vp, _u64p, _u64p, _i32p, sz, _u64p, ctypes.c_uint32]),
             "fheacc_bootstrap_async": (ctypes.c_int, [vp, vp, vp, vp, sz, vp, ctypes.c_uint32, vp]),
             "fheacc_bootstrap_plain_async": (ctypes.c_int, [vp, vp, vp, vp, sz, vp, ctypes.c_uint32, vp]),
+            "fheacc_bootstrap_noalloc": (ctypes.c_int, [vp, vp, vp, vp, sz, vp, ctypes.c_uint32, vp]),
             "fheacc_ntt_forward": (ctypes.c_int, [vp, vp, sz, vp]),
             "fheacc_ntt_inverse": (ctypes.c_int, [vp, vp, sz, vp]),
             "fheacc_rlwe_mult_rgsw": (ctypes.c_int, [vp, vp, vp, vp, sz, vp]),
@@ -347,6 +349,13 @@ class Context:
     # torch.Tensor.data_ptr(); stream is a raw cudaStream_t or 0)
     def bootstrap_async(self, d_c1, d_c2, d_gates, count, d_out, flags=0, stream=0):
         self.check(lib().fheacc_bootstrap_async(self._h, d_c1, d_c2, d_gates, count, d_out, flags, stream or None))
+
+    def bootstrap_noalloc(self, d_c1, d_c2, d_gates, count, d_out, flags=0, stream=0):
+        """fheacc_bootstrap_noalloc: the same gate bootstraps with no device
+        allocation (for callers that may not allocate), at most NOALLOC_MAX_GATES
+        gates per call; the library's one scratch array is shared by all calls."""
+        self.check(lib().fheacc_bootstrap_noalloc(self._h, d_c1, d_c2, d_gates, count, d_out, flags,
+                                                  stream or None))
 
     def bootstrap_plain_async(self, d_c1, d_c2, d_gates, count, d_out, flags=0, stream=0):
         self.check(lib().fheacc_bootstrap_plain_async(self._h, d_c1, d_c2, d_gates, count, d_out, flags,

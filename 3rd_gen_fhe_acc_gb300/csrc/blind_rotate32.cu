@@ -336,3 +336,30 @@ int launch_blind_rotate32(Context &c, const uint64_t *d_c1, const uint64_t *d_c2
 }
 
 }  // namespace fheacc
+
+namespace fheacc {
+
+// Same launch as launch_blind_rotate32, with the accumulator scratch supplied
+// by the caller (`accs`: count * 2048 u32 words, 16-byte aligned); allocates
+// nothing.
+int launch_blind_rotate32_with(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
+                               size_t count, uint32_t flags, uint32_t *accs, uint32_t *d_extract, cudaStream_t st)
+{
+    if (!count) return FHEACC_OK;
+    if (!c.d_btkey) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
+    dev::PipeArgs A{};
+    A.c1 = d_c1; A.c2 = d_c2; A.gates = d_gates; A.count = count;
+    A.btkey = c.d_btkey; A.accs = accs; A.acc_out = nullptr; A.extract = d_extract;
+    A.n = c.p.n; A.q = c.p.q; A.embed = c.dp.embed; A.Br = c.p.Br; A.digitR = c.p.digitR;
+    A.bg_bits = c.p.BG_bits; A.flags = flags; A.mu64 = c.dp.mu64;
+    for (int i = 0; i < 8; i++) A.gate_constant[i] = c.dp.gate_constant[i];
+    const bool three = c.tune.br_regs_for_3 != 0;
+    switch (c.p.digitG) {
+    case 2: return three ? launch_pipe_dg<2, 3>(c, A, 0, st) : launch_pipe_dg<2, 2>(c, A, 0, st);
+    case 3: return three ? launch_pipe_dg<3, 3>(c, A, 0, st) : launch_pipe_dg<3, 2>(c, A, 0, st);
+    case 4: return three ? launch_pipe_dg<4, 3>(c, A, 0, st) : launch_pipe_dg<4, 2>(c, A, 0, st);
+    default: return c.fail(FHEACC_EINVAL, "digitG must be 2..4 for the 32-bit path");
+    }
+}
+
+}  // namespace fheacc

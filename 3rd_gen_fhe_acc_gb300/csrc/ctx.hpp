@@ -90,6 +90,10 @@ int launch_rlwe_mult_rgsw32(Context &c, const uint64_t *d_acc, const uint64_t *d
 int launch_blind_rotate32(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
                           size_t count, uint32_t flags, uint64_t *d_acc_out, uint32_t *d_extract,
                           int max_ctas, cudaStream_t st);
+// The same blind rotation writing extracted RLWEs, with caller-supplied
+// accumulator scratch (count * 2048 u32 words); performs no allocation.
+int launch_blind_rotate32_with(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
+                               size_t count, uint32_t flags, uint32_t *accs, uint32_t *d_extract, cudaStream_t st);
 // LWE key switch (+ optional modulus switch) from extracted RLWEs
 // (lwe_ks.cu).
 int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,

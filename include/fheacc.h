@@ -155,6 +155,26 @@ int fheacc_bootstrap(fheacc_ctx *ctx, const uint64_t *c1, const uint64_t *c2,
 int fheacc_bootstrap_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2,
                            const int32_t *d_gates, size_t count, uint64_t *d_out,
                            uint32_t flags, void *stream);
+/* Gate bootstrapping that allocates nothing, DEVICE buffers, asynchronous on
+ * `stream`; same results as fheacc_bootstrap_async. No counterpart in the
+ * reference. It is meant for callers that may not allocate while they run:
+ * fheacc_bootstrap_async grows the context's scratch with cudaMalloc/cudaFree
+ * (cudaFree synchronises the whole device), which a serving loop sharing the
+ * GPU with other streams, a process under a fixed device-memory reservation,
+ * or a real-time loop cannot accept. Here the scratch is a fixed device array
+ * inside the library (776 KiB, present on every GPU that loads it until exit),
+ * so at most FHEACC_NOALLOC_MAX_GATES gates per call; larger counts return
+ * FHEACC_EINVAL. Parameter sets with N = 1024 only. The first call on a
+ * device looks up the array's device address (make that first call before any
+ * stream capture). All calls share the one array: calls whose work overlaps on
+ * the GPU (different streams, or different contexts on the same device) race
+ * and give wrong results; order them on one stream or synchronise. Keys must
+ * have been uploaded to ctx beforehand. */
+#define FHEACC_NOALLOC_MAX_GATES 64
+int fheacc_bootstrap_noalloc(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2,
+                             const int32_t *d_gates, size_t count, uint64_t *d_out, uint32_t flags,
+                             void *stream);
+
 /* The plain form: one launch sequence per gate (the per-gate issue of
  * fpga_eval_bootstrap_x1, myfpga.cpp:1003-1127), DEVICE buffers. */
 int fheacc_bootstrap_plain_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2,
