@@ -36,6 +36,7 @@ EINVAL, ENOMEM, ENODEV, EIO, ETIMEDOUT, ENOKEY, EBUSY = -22, -12, -19, -5, -110,
 _u64p = ctypes.POINTER(ctypes.c_uint64)
 _u8p = ctypes.POINTER(ctypes.c_uint8)
 _i32p = ctypes.POINTER(ctypes.c_int32)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
 
 
 class Params(ctypes.Structure):
@@ -54,6 +55,16 @@ class Params(ctypes.Structure):
         d = {k: getattr(self, k) for k, _ in self._fields_}
         d["gate_constant"] = list(self.gate_constant)
         return d
+
+
+class RequestDone(ctypes.Structure):
+    _fields_ = [("request_id", ctypes.c_uint64), ("status", ctypes.c_int32), ("queue_ms", ctypes.c_double),
+                ("latency_ms", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("rounds", ctypes.c_uint64), ("gates", ctypes.c_uint64), ("busy_s", ctypes.c_double),
+                ("waiting", ctypes.c_uint64), ("active", ctypes.c_uint64), ("free_slots", ctypes.c_uint64)]
 
 
 class FheaccError(RuntimeError):
@@ -103,6 +114,13 @@ def lib():
             "fheacc_bootstrap_async": (ctypes.c_int, [vp, vp, vp, vp, sz, vp, ctypes.c_uint32, vp]),
             "fheacc_bootstrap_plain_async": (ctypes.c_int, [vp, vp, vp, vp, sz, vp, ctypes.c_uint32, vp]),
             "fheacc_bootstrap_noalloc": (ctypes.c_int, [vp, vp, vp, vp, sz, vp, ctypes.c_uint32, vp]),
+            "fheacc_server_create": (ctypes.c_int, [vp, sz, sz, ctypes.POINTER(vp)]),
+            "fheacc_server_submit": (ctypes.c_int, [vp, _u64p, ctypes.c_uint32, _i32p, _u32p, _u32p, ctypes.c_uint32,
+                                                    ctypes.c_uint32, _u64p, ctypes.POINTER(ctypes.c_uint64)]),
+            "fheacc_server_poll": (ctypes.c_int, [vp, ctypes.POINTER(RequestDone), sz, ctypes.POINTER(sz),
+                                                  ctypes.c_uint32]),
+            "fheacc_server_stats": (ctypes.c_int, [vp, ctypes.POINTER(ServerStats)]),
+            "fheacc_server_destroy": (ctypes.c_int, [vp]),
             "fheacc_ntt_forward": (ctypes.c_int, [vp, vp, sz, vp]),
             "fheacc_ntt_inverse": (ctypes.c_int, [vp, vp, sz, vp]),
             "fheacc_rlwe_mult_rgsw": (ctypes.c_int, [vp, vp, vp, vp, sz, vp]),
@@ -396,3 +414,99 @@ class Context:
         v = ctypes.c_double()
         self.check(lib().fheacc_measure_imad_rate(self._h, ctypes.byref(v)))
         return v.value
+
+
+# ------------------------------------------------------------------ serving
+class Server:
+    """Continuous-batching request loop (fheacc_server_*): requests are gate
+    circuits over LWE ciphertexts; all ready gates of all admitted requests run
+    in one batched launch per round; admission by free pool slots."""
+
+    def __init__(self, ctx, max_batch=4096, pool_ciphertexts=1 << 18):
+        h = ctypes.c_void_p()
+        ctx.check(lib().fheacc_server_create(ctx.handle, max_batch, pool_ciphertexts, ctypes.byref(h)))
+        self._h = h
+        self.ctx = ctx
+        self.W = ctx.params.n + 1
+        self._pending = {}
+
+    def submit(self, inputs, gate_types, in1, in2, num_outputs):
+        """Returns (request id, output array filled when the request completes)."""
+        inputs = np.ascontiguousarray(inputs, dtype=np.uint64).reshape(-1, self.W)
+        gt = np.ascontiguousarray(gate_types, dtype=np.int32)
+        a = np.ascontiguousarray(in1, dtype=np.uint32)
+        b = np.ascontiguousarray(in2, dtype=np.uint32)
+        out = np.zeros((num_outputs, self.W), dtype=np.uint64)
+        rid = ctypes.c_uint64()
+        self.ctx.check(lib().fheacc_server_submit(self._h, _p64(inputs), inputs.shape[0], gt.ctypes.data_as(_i32p),
+                                                  a.ctypes.data_as(_u32p), b.ctypes.data_as(_u32p), gt.size,
+                                                  num_outputs, _p64(out), ctypes.byref(rid)))
+        self._pending[rid.value] = (out, inputs, gt, a, b)   # keep buffers alive until done
+        return rid.value, out
+
+    def poll(self, max_done=256, timeout_ms=0):
+        """[(request id, status, queue ms, latency ms, output array)]"""
+        arr = (RequestDone * max_done)()
+        n = ctypes.c_size_t()
+        self.ctx.check(lib().fheacc_server_poll(self._h, arr, max_done, ctypes.byref(n), timeout_ms))
+        res = []
+        for i in range(n.value):
+            d = arr[i]
+            out = self._pending.pop(d.request_id)[0]
+            res.append((d.request_id, d.status, d.queue_ms, d.latency_ms, out))
+        return res
+
+    def stats(self):
+        st = ServerStats()
+        self.ctx.check(lib().fheacc_server_stats(self._h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fheacc_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def psi_equality_circuit(num_items, bits=32, or_reduce=False):
+    """Gate circuit of a PSI-style equality query: the client item's `bits`
+    encrypted bits (nodes 0..bits-1) against `num_items` encrypted server items
+    (nodes bits + j*bits + b): per item `bits` XNOR gates and an AND tree; the
+    item results are the last nodes (or one OR over them with or_reduce).
+    Returns (gate_types, in1, in2, num_outputs)."""
+    types, in1, in2 = [], [], []
+    n_in = bits * (1 + num_items)
+    roots_src = []
+
+    def add(t, a, b):
+        types.append(t)
+        in1.append(a)
+        in2.append(b)
+        return n_in + len(types) - 1
+
+    pending_roots = []
+    for j in range(num_items):
+        level = [add(XNOR, b, bits + j * bits + b) for b in range(bits)]
+        while len(level) > 2:
+            nxt = [add(AND, level[i], level[i + 1]) for i in range(0, len(level) - 1, 2)]
+            if len(level) % 2:
+                nxt.append(level[-1])
+            level = nxt
+        pending_roots.append(level)
+    if bits == 1:
+        raise ValueError("bits must be at least 2")
+    roots = [add(AND, lv[0], lv[1]) for lv in pending_roots]   # one root per item, last
+    if not or_reduce:
+        return types, in1, in2, num_items
+    level = roots
+    while len(level) > 1:
+        nxt = [add(OR, level[i], level[i + 1]) for i in range(0, len(level) - 1, 2)]
+        if len(level) % 2:
+            nxt.append(level[-1])
+        level = nxt
+    return types, in1, in2, 1

@@ -45,6 +45,7 @@ constexpr int kMaxGroup = 12;   // ciphertexts per CTA and chunk (residue table 
 
 struct PipeArgs {
     const uint64_t *c1, *c2;
+    const uint32_t *idx1, *idx2;   // optional: gate g reads c1 + idx1[g] * (n+1) (else g)
     const int32_t *gates;
     size_t count;
     const uint32_t *btkey;   // B-tiled polys, [(i*digitR + j)*Br + r][digitG][2][2][1024]
@@ -128,7 +129,8 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
             const size_t gid = first + (size_t)k * G;
             const int g = A.gates[gid];
             const bool x2 = (g == 4 || g == 5);
-            const uint64_t *c1 = A.c1 + gid * (size_t)(n + 1), *c2 = A.c2 + gid * (size_t)(n + 1);
+            const uint64_t *c1 = A.c1 + (A.idx1 ? (size_t)A.idx1[gid] : gid) * (size_t)(n + 1);
+            const uint64_t *c2 = A.c2 + (A.idx2 ? (size_t)A.idx2[gid] : gid) * (size_t)(n + 1);
             for (int i = lane; i < n; i += 32) {
                 const uint64_t v = x2 ? 2 * (c1[i] - c2[i]) : c1[i] + c2[i];
                 uint32_t nega = (q - (uint32_t)(v & qmask)) & qmask;
@@ -345,10 +347,17 @@ namespace fheacc {
 int launch_blind_rotate32_with(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
                                size_t count, uint32_t flags, uint32_t *accs, uint32_t *d_extract, cudaStream_t st)
 {
+    return launch_blind_rotate32_indexed(c, d_c1, d_c2, nullptr, nullptr, d_gates, count, flags, accs, d_extract, st);
+}
+
+int launch_blind_rotate32_indexed(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const uint32_t *d_idx1,
+                                  const uint32_t *d_idx2, const int32_t *d_gates, size_t count, uint32_t flags,
+                                  uint32_t *accs, uint32_t *d_extract, cudaStream_t st)
+{
     if (!count) return FHEACC_OK;
     if (!c.d_btkey) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
     dev::PipeArgs A{};
-    A.c1 = d_c1; A.c2 = d_c2; A.gates = d_gates; A.count = count;
+    A.c1 = d_c1; A.c2 = d_c2; A.idx1 = d_idx1; A.idx2 = d_idx2; A.gates = d_gates; A.count = count;
     A.btkey = c.d_btkey; A.accs = accs; A.acc_out = nullptr; A.extract = d_extract;
     A.n = c.p.n; A.q = c.p.q; A.embed = c.dp.embed; A.Br = c.p.Br; A.digitR = c.p.digitR;
     A.bg_bits = c.p.BG_bits; A.flags = flags; A.mu64 = c.dp.mu64;

@@ -94,6 +94,14 @@ int launch_blind_rotate32(Context &c, const uint64_t *d_c1, const uint64_t *d_c2
 // accumulator scratch (count * 2048 u32 words); performs no allocation.
 int launch_blind_rotate32_with(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
                                size_t count, uint32_t flags, uint32_t *accs, uint32_t *d_extract, cudaStream_t st);
+// Blind rotation whose gate g reads c1 + idx1[g] * (n+1) and c2 + idx2[g] *
+// (n+1) (index arrays optional), caller-supplied accumulator scratch.
+int launch_blind_rotate32_indexed(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const uint32_t *d_idx1,
+                                  const uint32_t *d_idx2, const int32_t *d_gates, size_t count, uint32_t flags,
+                                  uint32_t *accs, uint32_t *d_extract, cudaStream_t st);
+// Key switch writing ciphertext ci to d_out + out_idx[ci] * (n+1) (optional).
+int launch_lwe_keyswitch32_indexed(Context &c, const uint32_t *d_extract, size_t count, bool modswitch,
+                                   uint64_t *d_out, const uint32_t *d_out_idx, cudaStream_t st);
 // LWE key switch (+ optional modulus switch) from extracted RLWEs
 // (lwe_ks.cu).
 int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,

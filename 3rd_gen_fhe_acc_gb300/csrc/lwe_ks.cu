@@ -24,6 +24,7 @@ struct KsArgs {
     size_t count;
     const uint32_t *kskey;
     uint64_t *out;
+    const uint32_t *out_idx;   // optional: ciphertext ci is written to out + out_idx[ci] * (n+1)
     int n, N, digitKS;
     uint32_t Bks, ks_row, q, modswitch;
     uint64_t Q;
@@ -69,7 +70,7 @@ __global__ void __launch_bounds__(kKsThreads) lwe_ks32_kernel(const __grid_const
         }
         const uint32_t b0 = ext[N];
         const uint32_t Q8 = Q / 8 + 1;
-        uint64_t *out = A.out + ci * (size_t)(n + 1);
+        uint64_t *out = A.out + (A.out_idx ? (size_t)A.out_idx[ci] : ci) * (size_t)(n + 1);
 #pragma unroll
         for (int c = 0; c < kKsPerThread; c++) {
             const int k = threadIdx.x + c * kKsThreads;
@@ -97,11 +98,17 @@ __global__ void modswitch_kernel(const uint64_t *__restrict__ in, uint64_t *__re
 int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
                            cudaStream_t st)
 {
+    return launch_lwe_keyswitch32_indexed(c, d_extract, count, modswitch, d_out, nullptr, st);
+}
+
+int launch_lwe_keyswitch32_indexed(Context &c, const uint32_t *d_extract, size_t count, bool modswitch,
+                                   uint64_t *d_out, const uint32_t *d_out_idx, cudaStream_t st)
+{
     if (!count) return FHEACC_OK;
     if (!c.d_kskey) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
     if (c.p.n + 1 > dev::kKsThreads * dev::kKsPerThread) return c.fail(FHEACC_EINVAL, "n too large for key switch");
     dev::KsArgs A{};
-    A.ext = d_extract; A.count = count; A.kskey = c.d_kskey; A.out = d_out;
+    A.ext = d_extract; A.count = count; A.kskey = c.d_kskey; A.out = d_out; A.out_idx = d_out_idx;
     A.n = c.p.n; A.N = c.p.N; A.digitKS = (int)c.p.digitKS; A.Bks = c.p.Bks; A.ks_row = c.dp.ks_row;
     A.q = c.p.q; A.modswitch = modswitch ? 1u : 0u; A.Q = c.p.Q;
     const size_t smem = (size_t)c.p.N * c.p.digitKS;

@@ -239,6 +239,62 @@ def profile_case():
     return 0 if ok == B else 1
 
 
+def run_serving(F, ctx, P, lsk, rate, duration, kmax=256, seed=7, max_batch=4096, pool=1 << 20):
+    """Poisson stream of PSI equality queries (a 32-bit client item against
+    k ~ U[1, kmax] encrypted server items: 32 XNOR + a 31-gate AND tree per
+    item) at `rate` bootstraps/s for `duration` seconds through the
+    continuous-batching server; returns latency percentiles and throughput."""
+    rng = np.random.default_rng(seed)
+    mean_gates = 63 * (kmax + 1) / 2
+    req_rate = rate / mean_gates
+    # pre-generate the requests (encryption is not part of the served path)
+    arrivals, reqs = [], []
+    t = 0.0
+    while True:
+        t += rng.exponential(1.0 / req_rate)
+        if t > duration:
+            break
+        k = int(rng.integers(1, kmax + 1))
+        bits = rng.integers(0, 2, 32 * (k + 1)).astype(np.uint8)
+        arrivals.append(t)
+        reqs.append((F.LWE_encrypt(P, 50_000 + len(reqs), lsk, bits), F.psi_equality_circuit(k)))
+    if not reqs:
+        return None
+    srv = F.Server(ctx, max_batch=max_batch, pool_ciphertexts=pool)
+    lat, queue = [], []
+    done_gates = 0
+    gates_of = {}
+    t0 = time.perf_counter()
+
+    def feeder():
+        for ta, (ct, circ) in zip(arrivals, reqs):
+            d = ta - (time.perf_counter() - t0)
+            if d > 0:
+                time.sleep(d)
+            rid, _ = srv.submit(ct, *circ)
+            gates_of[rid] = len(circ[0])
+
+    th = threading.Thread(target=feeder)
+    th.start()
+    while len(lat) < len(reqs):
+        for rid, status, q_ms, l_ms, out in srv.poll(timeout_ms=100):
+            assert status == 0
+            lat.append(l_ms)
+            queue.append(q_ms)
+            done_gates += gates_of.get(rid, 0)
+        if time.perf_counter() - t0 > duration + 600:
+            break
+    elapsed = time.perf_counter() - t0
+    th.join()
+    st = srv.stats()
+    srv.close()
+    return {"offered_bootstraps_per_s": rate, "requests": len(lat), "items_per_request": "U[1,%d]" % kmax,
+            "gates": int(st["gates"]), "rounds": int(st["rounds"]),
+            "throughput_bootstraps_per_s": st["gates"] / elapsed, "duration_s": elapsed,
+            "latency_ms_p50": float(np.percentile(lat, 50)), "latency_ms_p99": float(np.percentile(lat, 99)),
+            "queue_ms_p99": float(np.percentile(queue, 99)), "gpu_busy_frac": st["busy_s"] / elapsed}
+
+
 def config_of(P, args):
     return {"workload": "%d independent NAND-gate bootstraps: n=%d, N=%d, Q=%d (uint32 words), BG=2^%d x%d, "
                         "Br=%d x%d, Bks=%d x%d, q=%d; keys and input bits from fixed seeds" % (
@@ -259,6 +315,10 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=48)
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve", action="store_true",
+                    help="sweep serving rates (PSI queries through the continuous-batching server) and exit")
+    ap.add_argument("--serve-rate", type=float, default=20000.0, help="offered bootstraps/s of the serving sample")
+    ap.add_argument("--serve-seconds", type=float, default=8.0)
     ap.add_argument("--profile-case", action="store_true",
                     help="only run the small profiling case (n=64, 608 gates, 2 launches) and exit")
     args = ap.parse_args()
@@ -434,6 +494,13 @@ def main():
                          "RLWE.cpp:726-786) on %d threads, %.1f s" % (nsample, cores, dt),
                "bitexact_vs_gpu": "%d/%d" % (int((co == out0[:nsample]).all(axis=1).sum()), nsample)}
 
+    serving = None
+    if D.ws == 1 and args.serve_seconds > 0:
+        serving = run_serving(F, ctx, P, lsk, args.serve_rate, args.serve_seconds)
+    if args.serve:
+        sweep = [run_serving(F, ctx, P, lsk, r, 10.0) for r in (1e3, 5e3, 1e4, 2e4, 3e4, 4e4, 6e4, 1e5)]
+        print(json.dumps({"serving_sweep": sweep}))
+
     line = {
         "metric": METRIC, "value": value, "unit": "bootstraps/s", "n_gpus": D.ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
@@ -449,6 +516,7 @@ def main():
                   "latency_ms_p50": statistics.median(lat), "latency_ms_p99": float(np.percentile(lat, 99)),
                   "batched_over_plain": value / plain_value / D.ws},
         "batch_latency_ms_p50": statistics.median(step_ms), "batch_latency_ms_p99": float(np.percentile(step_ms, 99)),
+        "serving": serving,
         "checks": {"decrypt_ok": "%d/%d" % (dec_ok, B), "steps_repeatable": bool(same), "e2e_equal": bool(e2e_same),
                    "plain_equal": bool(plain_ok), "kernel_ms": {"blind_rotate": statistics.mean(br_ms),
                                                                 "keyswitch": statistics.mean(ks_ms)}},

@@ -219,6 +219,42 @@ int fheacc_kernel_times(fheacc_ctx *ctx, float ms[2]);
  * the denominator of the integer roofline. */
 int fheacc_measure_imad_rate(fheacc_ctx *ctx, double *imad_per_s);
 
+/* ----------------------------------------------------------------- serving
+ * A continuous-batching request loop over the gate bootstrap (no counterpart
+ * in the reference, whose FPGA driver runs one fixed-width batch at a time,
+ * myfpga.cpp:1130-1660). A request is a gate circuit: num_inputs LWE
+ * ciphertexts ([num_inputs][n+1] host words), then num_gates gates; gate g
+ * computes node num_inputs + g = eval_bootstrap(node in1[g], node in2[g],
+ * gate_types[g]) with in1[g] != in2[g] < num_inputs + g. The last num_outputs
+ * nodes are written to `out` ([num_outputs][n+1]) when the request completes.
+ * All nodes of an admitted request live in a device pool of pool_ciphertexts
+ * slots; a request is admitted when the pool has room for all its nodes, in
+ * arrival order. A worker thread runs rounds: every gate of every admitted
+ * request whose inputs are ready (up to max_batch) goes into one batched
+ * launch; requests arriving meanwhile join the next round. Keys must be
+ * uploaded before fheacc_server_create; the context must outlive the server
+ * and not be used for other work while the server runs. */
+typedef struct fheacc_server fheacc_server;
+typedef struct fheacc_request_done {
+    uint64_t request_id;
+    int32_t status;          /* FHEACC_OK or an error code */
+    double queue_ms;         /* submission to admission */
+    double latency_ms;       /* submission to completion */
+} fheacc_request_done;
+typedef struct fheacc_server_stats_t {
+    uint64_t rounds, gates;  /* batched launches and gates run so far */
+    double busy_s;           /* wall time of the rounds */
+    uint64_t waiting, active, free_slots;
+} fheacc_server_stats_t;
+int fheacc_server_create(fheacc_ctx *ctx, size_t max_batch, size_t pool_ciphertexts, fheacc_server **out);
+int fheacc_server_submit(fheacc_server *srv, const uint64_t *inputs, uint32_t num_inputs, const int32_t *gate_types,
+                         const uint32_t *in1, const uint32_t *in2, uint32_t num_gates, uint32_t num_outputs,
+                         uint64_t *out, uint64_t *request_id);
+/* Up to `max` completed requests (waits up to timeout_ms for the first). */
+int fheacc_server_poll(fheacc_server *srv, fheacc_request_done *done, size_t max, size_t *n_done, uint32_t timeout_ms);
+int fheacc_server_stats(fheacc_server *srv, fheacc_server_stats_t *stats);
+int fheacc_server_destroy(fheacc_server *srv);
+
 /* Wait until the most recent asynchronous call of the context (and every
  * blocking call) has finished, at most timeout_ms (0 = no limit). */
 int fheacc_sync(fheacc_ctx *ctx, uint32_t timeout_ms);
