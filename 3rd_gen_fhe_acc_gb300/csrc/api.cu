@@ -68,8 +68,38 @@ int mark_done(Context &c, cudaStream_t st, int rc)
 
 uint32_t shoup32_companion(uint64_t w, uint64_t Q) { return (uint32_t)((w << 32) / Q); }
 
+uint64_t shoup64_companion(uint64_t w, uint64_t Q) { return (uint64_t)(((unsigned __int128)w << 64) / Q); }
+
+int build_tables64(Context &c)
+{
+    host::Tables T;
+    T.build(c.p);
+    const int N = c.p.N;
+    const uint64_t Q = c.p.Q;
+    std::vector<ulonglong2> fw(N), iw(N);
+    for (int i = 0; i < N; i++) {
+        fw[i] = make_ulonglong2(T.rou[i], shoup64_companion(T.rou[i], Q));
+        iw[i] = make_ulonglong2(T.irou[i], shoup64_companion(T.irou[i], Q));
+    }
+    cudaError_t e = cudaMalloc(&c.d_tw64, N * sizeof(ulonglong2));
+    if (e == cudaSuccess) e = cudaMalloc(&c.d_itw64, N * sizeof(ulonglong2));
+    if (e == cudaSuccess) e = cudaMemcpy(c.d_tw64, fw.data(), N * sizeof(ulonglong2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(c.d_itw64, iw.data(), N * sizeof(ulonglong2), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return c.cuda_fail(e, "twiddle upload");
+    dev::Ntt64Consts &k = c.nc64;
+    k.Q = Q;
+    k.twoQ = 2 * Q;
+    k.iN = c.p.iN;
+    k.iNs = shoup64_companion(c.p.iN, Q);
+    k.iw1N = host::mulmod(T.irou[1], c.p.iN, Q);
+    k.iw1Ns = shoup64_companion(k.iw1N, Q);
+    k.mu64 = c.dp.mu64;
+    return FHEACC_OK;
+}
+
 int build_tables(Context &c)
 {
+    if (c.wide) return build_tables64(c);
     host::Tables T;
     T.build(c.p);
     const int N = c.p.N;
@@ -135,8 +165,11 @@ int fheacc_create(const fheacc_params *p, int device, fheacc_ctx **out)
         g_create_error = std::string("invalid parameter set: ") + (why ? why : "derivation failed");
         return FHEACC_EINVAL;
     }
-    if (pp.N != 1024 || pp.Q >= (1ULL << 27) || pp.digitG < 2 || pp.digitG > 4) {
-        g_create_error = "unsupported parameter set: this build runs N = 1024, Q < 2^27, digitG 2..4";
+    const bool narrow = pp.N == 1024 && pp.Q < (1ULL << 27) && pp.digitG >= 2 && pp.digitG <= 4;
+    const bool wide = pp.N == 2048 && pp.Q < (1ULL << 58) && pp.digitG >= 1 && pp.digitG <= 8;
+    if (!narrow && !wide) {
+        g_create_error = "unsupported parameter set: the device paths run N = 1024 with Q < 2^27 (digitG 2..4) "
+                         "and N = 2048 with Q < 2^58 (digitG <= 8)";
         return FHEACC_EINVAL;
     }
     int ndev = 0;
@@ -153,9 +186,10 @@ int fheacc_create(const fheacc_params *p, int device, fheacc_ctx **out)
     }
     c->p = pp;
     c->device = device;
+    c->wide = wide;
     DeviceGuard g(device);
     DevParams &d = c->dp;
-    d.n = pp.n; d.N = pp.N; d.logN = 10; d.q = pp.q; d.embed = 2u * (uint32_t)pp.N / pp.q; d.Q = pp.Q;
+    d.n = pp.n; d.N = pp.N; d.logN = wide ? 11 : 10; d.q = pp.q; d.embed = 2u * (uint32_t)pp.N / pp.q; d.Q = pp.Q;
     d.BG_bits = pp.BG_bits; d.digitG = pp.digitG; d.Br = pp.Br; d.digitR = pp.digitR;
     d.Bks = pp.Bks; d.digitKS = pp.digitKS; d.Bks_R_bits = pp.Bks_R_bits; d.digitKS_R = pp.digitKS_R;
     for (int i = 0; i < 6; i++) d.gate_constant[i] = pp.gate_constant[i];
@@ -199,6 +233,10 @@ int fheacc_destroy(fheacc_ctx *ctx)
     if (c->stream) cudaStreamSynchronize(c->stream);
     cudaFree(c->d_fwd_tw);
     cudaFree(c->d_inv_tw);
+    cudaFree(c->d_tw64);
+    cudaFree(c->d_itw64);
+    cudaFree(c->d_btkey64);
+    cudaFree(c->d_kskey64);
     cudaFree(c->d_btkey);
     cudaFree(c->d_kskey);
     cudaFree(c->d_subs);
@@ -240,6 +278,35 @@ int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t w
     const size_t n = c.p.n, dR = c.p.digitR, Br = c.p.Br;
     const size_t rw = (size_t)c.p.digitG * 4 * c.p.N;
     const uint64_t Q = c.p.Q;
+    if (c.wide) {
+        // device order, one step (all residues) per chunk, Shoup pairs made on the GPU
+        if (!c.d_btkey64) {
+            cudaError_t e = cudaMalloc(&c.d_btkey64, words * sizeof(ulonglong2));
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                c.d_btkey64 = nullptr;
+                return c.fail(FHEACC_ENOMEM, "device memory for the bootstrap key");
+            }
+            c.btkey_bytes = words * sizeof(ulonglong2);
+        }
+        std::vector<uint64_t> stage(Br * rw);
+        uint64_t *d_stage = nullptr;
+        cudaError_t e = cudaMalloc(&d_stage, Br * rw * sizeof(uint64_t));
+        if (e != cudaSuccess) return c.cuda_fail(e, "key staging");
+        int rc = FHEACC_OK;
+        for (size_t i = 0; i < n && !rc; i++) {
+            for (size_t j = 0; j < dR && !rc; j++) {
+                for (size_t r = 0; r < Br; r++)
+                    std::memcpy(stage.data() + r * rw, btkey + ((r * dR + j) * n + i) * rw, rw * sizeof(uint64_t));
+                e = cudaMemcpy(d_stage, stage.data(), Br * rw * sizeof(uint64_t), cudaMemcpyHostToDevice);
+                if (e != cudaSuccess) rc = c.cuda_fail(e, "key upload");
+                else rc = launch_shoup_pairs64(c, d_stage, c.d_btkey64 + (i * dR + j) * Br * rw, Br * rw, c.stream);
+                if (!rc && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = c.cuda_fail(cudaGetLastError(), "key pairs");
+            }
+        }
+        cudaFree(d_stage);
+        return rc;
+    }
     if (!c.d_btkey) {
         cudaError_t e = cudaMalloc(&c.d_btkey, words * sizeof(uint32_t));
         if (e != cudaSuccess) {
@@ -272,6 +339,28 @@ int fheacc_upload_lwe_ks_key(fheacc_ctx *ctx, const uint64_t *kskey, size_t word
     if (!kskey || words != fheacc_lwe_ks_key_words(&c.p)) return c.fail(FHEACC_EINVAL, "LWE key-switch key size mismatch");
     DeviceGuard g(c.device);
     const size_t rows = (size_t)c.p.Bks * c.p.digitKS * c.p.N, w = (size_t)c.p.n + 1, rs = c.dp.ks_row;
+    if (c.wide) {
+        if (!c.d_kskey64) {
+            cudaError_t e = cudaMalloc(&c.d_kskey64, rows * rs * sizeof(uint64_t));
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                c.d_kskey64 = nullptr;
+                return c.fail(FHEACC_ENOMEM, "device memory for the LWE key-switch key");
+            }
+            c.kskey_bytes = rows * rs * sizeof(uint64_t);
+        }
+        const size_t chunk = 8192;
+        std::vector<uint64_t> stage(chunk * rs, 0);
+        for (size_t r0 = 0; r0 < rows; r0 += chunk) {
+            const size_t m = std::min(chunk, rows - r0);
+            for (size_t r = 0; r < m; r++)
+                for (size_t k = 0; k < w; k++) stage[r * rs + k] = kskey[(r0 + r) * w + k] % c.p.Q;
+            cudaError_t e = cudaMemcpy(c.d_kskey64 + r0 * rs, stage.data(), m * rs * sizeof(uint64_t),
+                                       cudaMemcpyHostToDevice);
+            if (e != cudaSuccess) return c.cuda_fail(e, "key upload");
+        }
+        return FHEACC_OK;
+    }
     if (!c.d_kskey) {
         cudaError_t e = cudaMalloc(&c.d_kskey, rows * rs * sizeof(uint32_t));
         if (e != cudaSuccess) {
@@ -316,6 +405,21 @@ int fheacc_upload_subs_key(fheacc_ctx *ctx, const uint64_t *subs_key, size_t wor
 static int bootstrap_device(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
                             size_t count, uint64_t *d_out, uint32_t flags, cudaStream_t st, int max_ctas)
 {
+    if (c.wide) {
+        if (!c.d_btkey64) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
+        if (!c.d_kskey64) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
+        int rc = ensure_scratch(c, c.extract, count * kExtract64 * sizeof(uint64_t));
+        if (rc) return rc;
+        uint64_t *ext = (uint64_t *)c.extract.ptr;
+        const bool prof = (flags & FHEACC_FLAG_PROFILE) != 0;
+        if (prof) cudaEventRecord(c.prof[0], st);
+        rc = launch_blind_rotate64(c, d_c1, d_c2, d_gates, count, flags, nullptr, ext, max_ctas, st);
+        if (rc) return rc;
+        if (prof) cudaEventRecord(c.prof[1], st);
+        rc = launch_lwe_keyswitch64(c, ext, count, true, d_out, st);
+        if (prof && rc == FHEACC_OK) cudaEventRecord(c.prof[2], st);
+        return rc;
+    }
     if (!c.d_btkey) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
     if (!c.d_kskey) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
     int rc = ensure_scratch(c, c.extract, count * kExtractStride * sizeof(uint32_t));
@@ -398,7 +502,7 @@ int fheacc_ntt_forward(fheacc_ctx *ctx, uint64_t *d_polys, size_t count, void *s
     Context &c = *reinterpret_cast<Context *>(ctx);
     DeviceGuard g(c.device);
     cudaStream_t st = pick_stream(&c, stream);
-    return mark_done(c, st, launch_ntt32(c, d_polys, count, false, st));
+    return mark_done(c, st, c.wide ? launch_ntt64(c, d_polys, count, false, st) : launch_ntt32(c, d_polys, count, false, st));
 }
 
 int fheacc_ntt_inverse(fheacc_ctx *ctx, uint64_t *d_polys, size_t count, void *stream)
@@ -407,7 +511,7 @@ int fheacc_ntt_inverse(fheacc_ctx *ctx, uint64_t *d_polys, size_t count, void *s
     Context &c = *reinterpret_cast<Context *>(ctx);
     DeviceGuard g(c.device);
     cudaStream_t st = pick_stream(&c, stream);
-    return mark_done(c, st, launch_ntt32(c, d_polys, count, true, st));
+    return mark_done(c, st, c.wide ? launch_ntt64(c, d_polys, count, true, st) : launch_ntt32(c, d_polys, count, true, st));
 }
 
 int fheacc_rlwe_mult_rgsw(fheacc_ctx *ctx, const uint64_t *d_acc, const uint64_t *d_rgsw, uint64_t *d_out,
@@ -417,7 +521,8 @@ int fheacc_rlwe_mult_rgsw(fheacc_ctx *ctx, const uint64_t *d_acc, const uint64_t
     Context &c = *reinterpret_cast<Context *>(ctx);
     DeviceGuard g(c.device);
     cudaStream_t st = pick_stream(&c, stream);
-    return mark_done(c, st, launch_rlwe_mult_rgsw32(c, d_acc, d_rgsw, d_out, count, st));
+    return mark_done(c, st, c.wide ? launch_rlwe_mult_rgsw64(c, d_acc, d_rgsw, d_out, count, st)
+                                   : launch_rlwe_mult_rgsw32(c, d_acc, d_rgsw, d_out, count, st));
 }
 
 int fheacc_blind_rotate_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
@@ -427,6 +532,7 @@ int fheacc_blind_rotate_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint6
     Context &c = *reinterpret_cast<Context *>(ctx);
     DeviceGuard g(c.device);
     cudaStream_t st = pick_stream(&c, stream);
+    if (c.wide) return mark_done(c, st, launch_blind_rotate64(c, d_c1, d_c2, d_gates, count, flags, d_acc, nullptr, 0, st));
     return mark_done(c, st, launch_blind_rotate32(c, d_c1, d_c2, d_gates, count, flags, d_acc, nullptr, 0, st));
 }
 
@@ -436,9 +542,16 @@ int fheacc_lwe_keyswitch_async(fheacc_ctx *ctx, const uint64_t *d_rlwe, size_t c
     if (!ctx) return FHEACC_EINVAL;
     Context &c = *reinterpret_cast<Context *>(ctx);
     DeviceGuard g(c.device);
+    cudaStream_t st = pick_stream(&c, stream);
+    if (c.wide) {
+        int rc = ensure_scratch(c, c.extract, count * kExtract64 * sizeof(uint64_t));
+        if (rc) return rc;
+        rc = launch_extract64(c, d_rlwe, count, (uint64_t *)c.extract.ptr, st);
+        if (rc) return rc;
+        return mark_done(c, st, launch_lwe_keyswitch64(c, (uint64_t *)c.extract.ptr, count, false, d_out, st));
+    }
     int rc = ensure_scratch(c, c.extract, count * kExtractStride * sizeof(uint32_t));
     if (rc) return rc;
-    cudaStream_t st = pick_stream(&c, stream);
     rc = launch_extract_from_ntt32(c, d_rlwe, count, (uint32_t *)c.extract.ptr, st);
     if (rc) return rc;
     return mark_done(c, st, launch_lwe_keyswitch32(c, (uint32_t *)c.extract.ptr, count, false, d_out, st));

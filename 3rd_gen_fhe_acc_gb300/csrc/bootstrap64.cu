@@ -1,0 +1,451 @@
+// bootstrap64.cu -- the 64-bit-word path: N = 2048 and Q < 2^58 (the
+// n=630, Q < 2^54, BG = 2^9 x 6 parameter set), blind rotation, NTT and
+// RLWE x RGSW sub-steps, extraction, LWE key switch and modulus switch.
+//
+// Reference behaviour as in the 32-bit path: eval_bootstrap
+// (FHE_ACC_runtime/src/RLWE.cpp:726-786), RLWE_mult_RGSW (RLWE.cpp:642-704),
+// digit_decompose (RLWE.cpp:623-640), acc_initialization (RLWE.cpp:706-724),
+// LWE_keyswitch / LWE_modswitch (LWE.cpp:233-269).
+//
+// One RLWE x RGSW step runs on a CTA of 256 threads in two 128-thread groups,
+// group p owning poly p of the accumulator: inverse NTT in shared memory, then
+// for each digit h both groups transform digit h of their poly and all 256
+// threads multiply-accumulate it with the key rows. Keys are stored with their
+// Shoup companions (K, floor(K 2^64 / Q)), so every MAC product is one 64-bit
+// Shoup multiply; the 2 * digitG products of an output stay below 24Q and are
+// reduced once. As in the 32-bit kernel, steps are the outer loop over a
+// group of ciphertexts per CTA, so the CTAs stream each step's 23 RGSW keys
+// (18 MB with companions) through L2 together; accumulators live in global
+// memory (32 KB per gate).
+#include "ctx.hpp"
+#include "ntt64.cuh"
+#include <algorithm>
+
+namespace fheacc {
+namespace dev {
+
+constexpr int kMaxGroup64 = 8;
+constexpr int kT64 = 256;   // threads per CTA
+
+struct Step64Smem {
+    uint64_t acc[2][2048];   // accumulator; time domain inside a step
+    uint64_t buf[2][2048];   // digit NTTs
+};
+
+// One RLWE x RGSW step on s.acc (NTT domain, values < 2Q) with the key
+// `key` (Shoup pairs, [digitG][2][2][2048]).
+__device__ __forceinline__ void step64(Step64Smem &s, const ulonglong2 *__restrict__ key, int DG, uint32_t bg_bits,
+                                       const ulonglong2 *__restrict__ tw, const ulonglong2 *__restrict__ itw,
+                                       const Ntt64Consts &c)
+{
+    const int tid = threadIdx.x, grp = tid >> 7, gtid = tid & 127;
+    ntt64_inv_2048<128>(s.acc[grp], itw, c, gtid, 1 + grp);
+    __syncthreads();
+    uint64_t sa[8], sb[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) sa[i] = sb[i] = 0;
+    const uint64_t mask = (1ULL << bg_bits) - 1;
+    for (int h = 0; h < DG; h++) {
+        const uint32_t sh = bg_bits * h;
+        for (int e = gtid; e < 2048; e += 128) s.buf[grp][e] = (s.acc[grp][e] >> sh) & mask;
+        group_sync(1 + grp, 128);
+        ntt64_fwd_2048<128>(s.buf[grp], tw, c, gtid, 1 + grp);
+        __syncthreads();
+        const ulonglong2 *k0 = key + (size_t)(h * 2 + 0) * 2 * 2048;   // row c_text[h][0]: times digit of a
+        const ulonglong2 *k1 = key + (size_t)(h * 2 + 1) * 2 * 2048;   // row c_text[h][1]: times digit of b
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int k = tid + 256 * i;
+            const uint64_t da = s.buf[0][k], db = s.buf[1][k];
+            const ulonglong2 a0 = __ldg(k0 + k), b0 = __ldg(k0 + 2048 + k);
+            const ulonglong2 a1 = __ldg(k1 + k), b1 = __ldg(k1 + 2048 + k);
+            sa[i] += shoup64(da, a0.x, a0.y, c.Q) + shoup64(db, a1.x, a1.y, c.Q);
+            sb[i] += shoup64(da, b0.x, b0.y, c.Q) + shoup64(db, b1.x, b1.y, c.Q);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int k = tid + 256 * i;
+        s.acc[0][k] = barrett64_2q(sa[i], c.mu64, c.Q);
+        s.acc[1][k] = barrett64_2q(sb[i], c.mu64, c.Q);
+    }
+    __syncthreads();
+}
+
+// Forward / inverse NTT of count polys (u64, canonical in and out), one
+// 128-thread group per poly.
+template <bool INV>
+__global__ void __launch_bounds__(kT64) ntt64_kernel(uint64_t *polys, size_t count, const ulonglong2 *__restrict__ tw,
+                                                    const __grid_constant__ Ntt64Consts c)
+{
+    __shared__ uint64_t buf[2][2048];
+    const int grp = threadIdx.x >> 7, gtid = threadIdx.x & 127;
+    for (size_t base = (size_t)blockIdx.x * 2; base < count; base += (size_t)gridDim.x * 2) {
+        const size_t pi = base + grp;
+        const bool live = pi < count;
+        uint64_t *poly = polys + pi * 2048;
+        for (int e = gtid; e < 2048; e += 128) buf[grp][e] = live ? poly[e] : 0;
+        group_sync(1 + grp, 128);
+        if (INV) ntt64_inv_2048<128>(buf[grp], tw, c, gtid, 1 + grp);
+        else ntt64_fwd_2048<128>(buf[grp], tw, c, gtid, 1 + grp);
+        if (live) {
+            for (int e = gtid; e < 2048; e += 128) {
+                uint64_t v = buf[grp][e];
+                if (!INV) {
+                    v = barrett64_2q(v, c.mu64, c.Q);
+                    v = v >= c.Q ? v - c.Q : v;
+                }
+                poly[e] = v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// (K, floor(K 2^64 / Q)) pairs of key words (reduced mod Q first).
+__global__ void shoup_pairs64_kernel(const uint64_t *__restrict__ in, ulonglong2 *__restrict__ out, size_t n,
+                                     uint64_t Q)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const uint64_t w = in[i] % Q;
+        out[i] = make_ulonglong2(w, (uint64_t)(((unsigned __int128)w << 64) / Q));
+    }
+}
+
+// RLWE_mult_RGSW of count (acc, RGSW-pairs) in reference order; acc canonical.
+__global__ void __launch_bounds__(kT64) rlwe_mult_rgsw64_kernel(const uint64_t *__restrict__ acc_in,
+                                                               const ulonglong2 *__restrict__ rgsw, uint64_t *acc_out,
+                                                               size_t count, int DG, uint32_t bg_bits,
+                                                               const ulonglong2 *__restrict__ tw,
+                                                               const ulonglong2 *__restrict__ itw,
+                                                               const __grid_constant__ Ntt64Consts c)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Step64Smem &s = *reinterpret_cast<Step64Smem *>(smem_raw);
+    for (size_t ci = blockIdx.x; ci < count; ci += gridDim.x) {
+        for (int e = threadIdx.x; e < 4096; e += kT64) s.acc[e >> 11][e & 2047] = acc_in[ci * 4096 + e];
+        __syncthreads();
+        step64(s, rgsw + ci * (size_t)DG * 4 * 2048, DG, bg_bits, tw, itw, c);
+        for (int e = threadIdx.x; e < 4096; e += kT64) {
+            const uint64_t v = s.acc[e >> 11][e & 2047];
+            acc_out[ci * 4096 + e] = v >= c.Q ? v - c.Q : v;
+        }
+        __syncthreads();
+    }
+}
+
+struct Br64Args {
+    const uint64_t *c1, *c2;
+    const int32_t *gates;
+    size_t count;
+    const ulonglong2 *btkey;   // [(i*digitR + j)*Br + r][digitG][2][2][2048] Shoup pairs
+    uint64_t *accs;            // scratch [count][2][2048], NTT domain, values < 2Q
+    uint64_t *acc_out;         // optional canonical NTT accumulators [count][4096]
+    uint64_t *extract;         // optional [count][kExtract64]
+    int n, DG;
+    uint32_t q, embed, Br, digitR, bg_bits, flags;
+    uint64_t gate_constant[8];
+};
+
+__global__ void __launch_bounds__(kT64) br64_kernel(const __grid_constant__ Br64Args A,
+                                                   const ulonglong2 *__restrict__ tw, const ulonglong2 *__restrict__ itw,
+                                                   const __grid_constant__ Ntt64Consts c)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Step64Smem &s = *reinterpret_cast<Step64Smem *>(smem_raw);
+    uint8_t *res = smem_raw + sizeof(Step64Smem);   // [kMaxGroup64][n * digitR]
+    __shared__ uint32_t bvals[kMaxGroup64], b1s[kMaxGroup64], b2s[kMaxGroup64];
+    const int tid = threadIdx.x;
+    const int n = A.n, S = n * (int)A.digitR;
+    const uint32_t q = A.q, qmask = q - 1;
+    const size_t rgsw_pairs = (size_t)A.DG * 4 * 2048;
+    const bool compat = (A.flags & FHEACC_FLAG_FPGA_COMPAT) != 0;
+    const size_t G = gridDim.x;
+    for (size_t base = 0; base < A.count; base += G * kMaxGroup64) {
+        const size_t first = base + blockIdx.x;
+        int m = 0;
+        while (m < kMaxGroup64 && first + (size_t)m * G < A.count) m++;
+        // LWE_evaluate and residues
+        for (int k = 0; k < m; k++) {
+            const size_t gid = first + (size_t)k * G;
+            const int g = A.gates[gid];
+            const bool x2 = (g == 4 || g == 5);
+            const uint64_t *c1 = A.c1 + gid * (size_t)(n + 1), *c2 = A.c2 + gid * (size_t)(n + 1);
+            for (int i = tid; i <= n; i += kT64) {
+                const uint64_t v = x2 ? 2 * (c1[i] - c2[i]) : c1[i] + c2[i];
+                if (i < n) {
+                    uint32_t nega = (q - (uint32_t)(v & qmask)) & qmask;
+                    for (uint32_t j = 0; j < A.digitR; j++) {
+                        res[k * S + i * (int)A.digitR + (int)j] = (uint8_t)(nega % A.Br);
+                        nega /= A.Br;
+                    }
+                } else {
+                    const uint64_t gc = A.gate_constant[(unsigned)g < 6u ? g : 6];
+                    bvals[k] = (uint32_t)(v & qmask);
+                    b1s[k] = (uint32_t)(gc & qmask);
+                    b2s[k] = (b1s[k] + q / 2) & qmask;
+                }
+            }
+        }
+        __syncthreads();
+        // acc_initialization: a = 0, b = test vector, forward NTT (group 1 transforms b)
+        for (int k = 0; k < m; k++) {
+            const size_t gid = first + (size_t)k * G;
+            const uint64_t Q8 = c.Q / 8 + 1, negQ8 = c.Q - Q8;
+            const uint32_t b1 = b1s[k], b2 = b2s[k], val = bvals[k];
+            for (int e = tid; e < 2048; e += kT64) {
+                uint64_t v = 0;
+                if (e % A.embed == 0 && (uint32_t)e / A.embed < q / 2) {
+                    const uint32_t tmp = (val - (uint32_t)e / A.embed) & qmask;
+                    if (b1 < b2) v = (tmp >= b1 && tmp < b2) ? negQ8 : Q8;
+                    else v = (tmp >= b2 && tmp < b1) ? Q8 : negQ8;
+                }
+                s.buf[1][e] = v;
+            }
+            __syncthreads();
+            if (tid >= 128) ntt64_fwd_2048<128>(s.buf[1], tw, c, tid - 128, 2);
+            __syncthreads();
+            uint64_t *acc = A.accs + gid * 4096;
+            for (int e = tid; e < 2048; e += kT64) {
+                acc[e] = 0;
+                uint64_t v = barrett64_2q(s.buf[1][e], c.mu64, c.Q);
+                acc[2048 + e] = v >= c.Q ? v - c.Q : v;
+            }
+            __syncthreads();
+        }
+        // blind rotation, steps outer
+        for (int st = 0; st < S; st++) {
+            for (int k = 0; k < m; k++) {
+                const uint32_t r = res[k * S + st];
+                if (r == 0 && !compat) continue;
+                uint64_t *acc = A.accs + (first + (size_t)k * G) * 4096;
+                for (int e = tid; e < 4096; e += kT64) s.acc[e >> 11][e & 2047] = __ldcg(acc + e);
+                __syncthreads();
+                step64(s, A.btkey + ((size_t)st * A.Br + r) * rgsw_pairs, A.DG, A.bg_bits, tw, itw, c);
+                for (int e = tid; e < 4096; e += kT64) __stcg(acc + e, s.acc[e >> 11][e & 2047]);
+                __syncthreads();
+            }
+        }
+        // output
+        for (int k = 0; k < m; k++) {
+            const size_t gid = first + (size_t)k * G;
+            const uint64_t *acc = A.accs + gid * 4096;
+            if (A.extract) {
+                // NTT_a_transpose on poly a, then inverse NTT of both polys
+                for (int e = tid; e < 2048; e += kT64) {
+                    s.acc[0][e] = __ldcg(acc + 2047 - e);
+                    s.acc[1][e] = __ldcg(acc + 2048 + e);
+                }
+                __syncthreads();
+                ntt64_inv_2048<128>(s.acc[tid >> 7], itw, c, tid & 127, 1 + (tid >> 7));
+                __syncthreads();
+                uint64_t *ext = A.extract + gid * kExtract64;
+                for (int e = tid; e < 2048; e += kT64) ext[e] = s.acc[0][e];
+                if (tid == 0) ext[2048] = s.acc[1][0];
+            } else {
+                for (int e = tid; e < 4096; e += kT64) {
+                    const uint64_t v = __ldcg(acc + e);
+                    A.acc_out[gid * 4096 + e] = v >= c.Q ? v - c.Q : v;
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Extraction of canonical NTT RLWEs (u64) for the key-switch entry point.
+__global__ void __launch_bounds__(kT64) extract64_kernel(const uint64_t *__restrict__ rlwe, size_t count,
+                                                        uint64_t *__restrict__ extract,
+                                                        const ulonglong2 *__restrict__ itw,
+                                                        const __grid_constant__ Ntt64Consts c)
+{
+    __shared__ uint64_t buf[2][2048];
+    const int tid = threadIdx.x;
+    for (size_t ci = blockIdx.x; ci < count; ci += gridDim.x) {
+        const uint64_t *in = rlwe + ci * 4096;
+        for (int e = tid; e < 2048; e += kT64) {
+            buf[0][e] = in[2047 - e];
+            buf[1][e] = in[2048 + e];
+        }
+        __syncthreads();
+        ntt64_inv_2048<128>(buf[tid >> 7], itw, c, tid & 127, 1 + (tid >> 7));
+        __syncthreads();
+        uint64_t *ext = extract + ci * kExtract64;
+        for (int e = tid; e < 2048; e += kT64) ext[e] = buf[0][e];
+        if (tid == 0) ext[2048] = buf[1][0];
+        __syncthreads();
+    }
+}
+
+struct Ks64Args {
+    const uint64_t *ext;
+    size_t count;
+    const uint64_t *kskey;   // [(d*digitKS + j)*N + i][ks_row]
+    uint64_t *out;
+    int n, N, digitKS;
+    uint32_t Bks, ks_row, q, modswitch;
+    uint64_t Q;
+};
+
+__device__ __forceinline__ uint64_t scale_round64(uint64_t x, uint64_t new_mod, uint64_t old_mod)
+{
+    const unsigned __int128 num = (unsigned __int128)old_mod + 2 * (unsigned __int128)x * new_mod;
+    return (uint64_t)(num / (2 * (unsigned __int128)old_mod));
+}
+
+// LWE_keyswitch (LWE.cpp:233-253) + optional LWE_modswitch, one CTA per
+// ciphertext; 64-bit sums are folded mod Q every 256 rows (256 Q < 2^64).
+__global__ void __launch_bounds__(kT64) lwe_ks64_kernel(const __grid_constant__ Ks64Args A)
+{
+    extern __shared__ uint8_t digits[];   // [N][digitKS]
+    const int n = A.n, N = A.N, D = A.digitKS;
+    const uint64_t Q = A.Q;
+    constexpr int PT = 4;   // coefficients per thread, n + 1 <= 1024
+    for (size_t ci = blockIdx.x; ci < A.count; ci += gridDim.x) {
+        const uint64_t *ext = A.ext + ci * kExtract64;
+        for (int i = threadIdx.x; i < N; i += kT64) {
+            uint64_t a = ext[i];
+            for (int j = 0; j < D; j++) {
+                digits[i * D + j] = (uint8_t)(a % A.Bks);
+                a /= A.Bks;
+            }
+        }
+        __syncthreads();
+        uint64_t acc[PT] = {0, 0, 0, 0};
+        int rows = 0;
+        for (int i = 0; i < N; i++) {
+            for (int j = 0; j < D; j++) {
+                const uint32_t d = digits[i * D + j];
+                const uint64_t *row = A.kskey + ((size_t)(d * D + j) * N + i) * A.ks_row;
+#pragma unroll
+                for (int cc = 0; cc < PT; cc++) {
+                    const int k = threadIdx.x + cc * kT64;
+                    if (k <= n) acc[cc] += __ldg(row + k);
+                }
+                if (++rows == 256) {
+                    rows = 0;
+#pragma unroll
+                    for (int cc = 0; cc < PT; cc++) acc[cc] %= Q;
+                }
+            }
+        }
+        const uint64_t b0 = ext[N];
+        const uint64_t Q8 = Q / 8 + 1;
+        uint64_t *out = A.out + ci * (size_t)(n + 1);
+#pragma unroll
+        for (int cc = 0; cc < PT; cc++) {
+            const int k = threadIdx.x + cc * kT64;
+            if (k <= n) {
+                const uint64_t sred = acc[cc] % Q;
+                uint64_t v;
+                if (k < n) v = sred ? Q - sred : 0;
+                else v = ((b0 + Q8) % Q + Q - sred) % Q;
+                out[k] = A.modswitch ? scale_round64(v, A.q, Q) : v;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace dev
+
+static int sms_of(Context &c)
+{
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, c.device);
+    return v > 0 ? v : 1;
+}
+
+int launch_shoup_pairs64(Context &c, const uint64_t *d_in, ulonglong2 *d_out, size_t n, cudaStream_t st)
+{
+    if (!n) return FHEACC_OK;
+    unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)sms_of(c) * 32);
+    dev::shoup_pairs64_kernel<<<blocks, 256, 0, st>>>(d_in, d_out, n, c.p.Q);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "shoup pairs launch");
+}
+
+int launch_ntt64(Context &c, uint64_t *d_polys, size_t count, bool inverse, cudaStream_t st)
+{
+    if (!count) return FHEACC_OK;
+    size_t blocks = std::min<size_t>((count + 1) / 2, (size_t)sms_of(c) * 8);
+    if (inverse) dev::ntt64_kernel<true><<<(unsigned)blocks, dev::kT64, 0, st>>>(d_polys, count, c.d_itw64, c.nc64);
+    else dev::ntt64_kernel<false><<<(unsigned)blocks, dev::kT64, 0, st>>>(d_polys, count, c.d_tw64, c.nc64);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "ntt64 launch");
+}
+
+int launch_rlwe_mult_rgsw64(Context &c, const uint64_t *d_acc, const uint64_t *d_rgsw, uint64_t *d_out,
+                            size_t count, cudaStream_t st)
+{
+    if (!count) return FHEACC_OK;
+    const size_t words = count * (size_t)c.p.digitG * 4 * 2048;
+    int rc = ensure_scratch(c, c.io, words * sizeof(ulonglong2));
+    if (rc) return rc;
+    ulonglong2 *pairs = (ulonglong2 *)c.io.ptr;
+    rc = launch_shoup_pairs64(c, d_rgsw, pairs, words, st);
+    if (rc) return rc;
+    const size_t smem = sizeof(dev::Step64Smem);
+    cudaFuncSetAttribute(dev::rlwe_mult_rgsw64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    size_t blocks = std::min<size_t>(count, (size_t)sms_of(c) * 2);
+    dev::rlwe_mult_rgsw64_kernel<<<(unsigned)blocks, dev::kT64, smem, st>>>(
+        d_acc, pairs, d_out, count, (int)c.p.digitG, c.p.BG_bits, c.d_tw64, c.d_itw64, c.nc64);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "rlwe_mult_rgsw64 launch");
+}
+
+int launch_blind_rotate64(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
+                          size_t count, uint32_t flags, uint64_t *d_acc_out, uint64_t *d_extract, int max_ctas,
+                          cudaStream_t st)
+{
+    if (!count) return FHEACC_OK;
+    if (!c.d_btkey64) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
+    int rc = ensure_scratch(c, c.accs, count * 4096 * sizeof(uint64_t));
+    if (rc) return rc;
+    dev::Br64Args A{};
+    A.c1 = d_c1; A.c2 = d_c2; A.gates = d_gates; A.count = count;
+    A.btkey = c.d_btkey64; A.accs = (uint64_t *)c.accs.ptr; A.acc_out = d_acc_out; A.extract = d_extract;
+    A.n = c.p.n; A.DG = (int)c.p.digitG; A.q = c.p.q; A.embed = c.dp.embed; A.Br = c.p.Br; A.digitR = c.p.digitR;
+    A.bg_bits = c.p.BG_bits; A.flags = flags;
+    for (int i = 0; i < 8; i++) A.gate_constant[i] = c.dp.gate_constant[i];
+    const size_t smem = sizeof(dev::Step64Smem) + (size_t)dev::kMaxGroup64 * c.p.n * c.p.digitR;
+    cudaError_t e = cudaFuncSetAttribute(dev::br64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return c.cuda_fail(e, "br64 smem attribute");
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::br64_kernel, dev::kT64, smem);
+    if (per_sm < 1) per_sm = 1;
+    size_t blocks = std::min<size_t>((size_t)sms_of(c) * per_sm, count);
+    if (max_ctas > 0) blocks = std::min<size_t>(blocks, (size_t)max_ctas);
+    dev::br64_kernel<<<(unsigned)blocks, dev::kT64, smem, st>>>(A, c.d_tw64, c.d_itw64, c.nc64);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "br64 launch");
+}
+
+int launch_extract64(Context &c, const uint64_t *d_rlwe, size_t count, uint64_t *d_extract, cudaStream_t st)
+{
+    if (!count) return FHEACC_OK;
+    size_t blocks = std::min<size_t>(count, (size_t)sms_of(c) * 4);
+    dev::extract64_kernel<<<(unsigned)blocks, dev::kT64, 0, st>>>(d_rlwe, count, d_extract, c.d_itw64, c.nc64);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "extract64 launch");
+}
+
+int launch_lwe_keyswitch64(Context &c, const uint64_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
+                           cudaStream_t st)
+{
+    if (!count) return FHEACC_OK;
+    if (!c.d_kskey64) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
+    if (c.p.n + 1 > 4 * dev::kT64) return c.fail(FHEACC_EINVAL, "n too large for key switch");
+    dev::Ks64Args A{};
+    A.ext = d_extract; A.count = count; A.kskey = c.d_kskey64; A.out = d_out;
+    A.n = c.p.n; A.N = c.p.N; A.digitKS = (int)c.p.digitKS; A.Bks = c.p.Bks; A.ks_row = c.dp.ks_row;
+    A.q = c.p.q; A.modswitch = modswitch ? 1u : 0u; A.Q = c.p.Q;
+    const size_t smem = (size_t)c.p.N * c.p.digitKS;
+    size_t blocks = std::min<size_t>(count, (size_t)sms_of(c) * 8);
+    dev::lwe_ks64_kernel<<<(unsigned)blocks, dev::kT64, smem, st>>>(A);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "lwe_ks64 launch");
+}
+
+}  // namespace fheacc

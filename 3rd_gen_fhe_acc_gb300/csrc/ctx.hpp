@@ -6,6 +6,7 @@
 #include <string>
 #include "fheacc.h"
 #include "ntt32.cuh"
+#include "ntt64.cuh"
 
 namespace fheacc {
 
@@ -36,7 +37,7 @@ struct Context {
     fheacc_params p{};
     DevParams dp{};
     int device = 0;
-    bool wide = false;            // 64-bit words (Q >= 2^27) -- not yet supported on device
+    bool wide = false;            // 64-bit path: N = 2048, Q < 2^58 (else N = 1024, Q < 2^27)
     cudaStream_t stream = nullptr;  // used by the blocking host-buffer entry points
     cudaEvent_t done = nullptr;     // recorded after every asynchronous call
     cudaEvent_t prof[3] = {nullptr, nullptr, nullptr};   // FHEACC_FLAG_PROFILE marks
@@ -46,6 +47,12 @@ struct Context {
     // twiddles: (w, w') pairs indexed like the reference tables
     uint2 *d_fwd_tw = nullptr, *d_inv_tw = nullptr;
     dev::Ntt32Consts nc{};
+
+    // 64-bit path: twiddles as (w, floor(w 2^64 / Q)) pairs in reference order
+    ulonglong2 *d_tw64 = nullptr, *d_itw64 = nullptr;
+    dev::Ntt64Consts nc64{};
+    ulonglong2 *d_btkey64 = nullptr;   // Shoup pairs, [(i*digitR + j)*Br + r][digitG][2][2][N]
+    uint64_t *d_kskey64 = nullptr;     // [(d*digitKS + j)*N + i][ks_row]
 
     // keys, device layouts
     uint32_t *d_btkey = nullptr;   // [(i*digitR + j)*Br + r][digitG][2][2][N], polys B-tiled
@@ -109,10 +116,22 @@ int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, 
 int launch_extract_from_ntt32(Context &c, const uint64_t *d_rlwe, size_t count, uint32_t *d_extract,
                               cudaStream_t st);
 int launch_modswitch(Context &c, const uint64_t *d_in, size_t count, uint64_t *d_out, cudaStream_t st);
+// 64-bit path (bootstrap64.cu)
+int launch_shoup_pairs64(Context &c, const uint64_t *d_in, ulonglong2 *d_out, size_t n, cudaStream_t st);
+int launch_ntt64(Context &c, uint64_t *d_polys, size_t count, bool inverse, cudaStream_t st);
+int launch_rlwe_mult_rgsw64(Context &c, const uint64_t *d_acc, const uint64_t *d_rgsw, uint64_t *d_out,
+                            size_t count, cudaStream_t st);
+int launch_blind_rotate64(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
+                          size_t count, uint32_t flags, uint64_t *d_acc_out, uint64_t *d_extract, int max_ctas,
+                          cudaStream_t st);
+int launch_extract64(Context &c, const uint64_t *d_rlwe, size_t count, uint64_t *d_extract, cudaStream_t st);
+int launch_lwe_keyswitch64(Context &c, const uint64_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
+                           cudaStream_t st);
 // IMAD throughput probe (probe.cu)
 int measure_imad_rate(Context &c, double *imad_per_s);
 
 constexpr size_t kExtractStride = 1024 + 32;   // u32 words per extracted RLWE (N = 1024)
+constexpr size_t kExtract64 = 2048 + 8;        // u64 words per extracted RLWE (N = 2048)
 
 // Word index of element e = 32 l + r of a 1024-word poly in the "B-tiled"
 // device layout used for bootstrap keys and blind-rotation accumulators.

@@ -297,6 +297,7 @@ int fheacc_server_create(fheacc_ctx *ctx, size_t max_batch, size_t pool_cipherte
 {
     if (!ctx || !out || max_batch == 0 || pool_ciphertexts == 0 || pool_ciphertexts > 0xFFFFFFF0u) return FHEACC_EINVAL;
     Context &c = *reinterpret_cast<Context *>(ctx);
+    if (c.wide) return c.fail(FHEACC_EINVAL, "server: runs the N = 1024 parameter sets");
     if (!c.d_btkey || !c.d_kskey) return c.fail(FHEACC_ENOKEY, "server: keys must be uploaded first");
     int prev = -1;
     cudaGetDevice(&prev);

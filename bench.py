@@ -175,7 +175,7 @@ def run_reference(args):
     ks = F.keyswitch_key(P, SEEDS["kskey"], rsk, lsk)
     ora = Oracle.from_params(P)
     cores = cpu_cores()
-    per_step = args.cpu_sample or 2 * cores
+    per_step = args.cpu_sample or (2 if P.N == 1024 else 1) * cores
     times = []
     for s in range(args.warmup + args.steps):
         lo = (s * per_step) % max(args.batch - per_step, 1)
@@ -295,12 +295,20 @@ def run_serving(F, ctx, P, lsk, rate, duration, kmax=256, seed=7, max_batch=4096
             "queue_ms_p99": float(np.percentile(queue, 99)), "gpu_busy_frac": st["busy_s"] / elapsed}
 
 
+def fheacc_key_bytes(P):
+    """Device bytes of the bootstrap + key-switch keys of a parameter set."""
+    if P.N == 1024:
+        return P.Br * P.digitR * P.n * P.digitG * 4 * P.N * 4 + P.Bks * P.digitKS * P.N * ((P.n + 32) // 32 * 32) * 4
+    return P.Br * P.digitR * P.n * P.digitG * 4 * P.N * 16 + P.Bks * P.digitKS * P.N * ((P.n + 32) // 32 * 32) * 8
+
+
 def config_of(P, args):
-    return {"workload": "%d independent NAND-gate bootstraps: n=%d, N=%d, Q=%d (uint32 words), BG=2^%d x%d, "
+    return {"workload": "%d independent NAND-gate bootstraps: n=%d, N=%d, Q=%d (" + ("uint32" if P.N == 1024 else "uint64") + " words), BG=2^%d x%d, "
                         "Br=%d x%d, Bks=%d x%d, q=%d; keys and input bits from fixed seeds" % (
                             args.batch, P.n, P.N, P.Q, P.BG_bits, P.digitG, P.Br, P.digitR, P.Bks, P.digitKS, P.q),
             "batch": args.batch, "gate": "NAND", "n": P.n, "N": P.N, "Q": P.Q,
-            "l2": "flushed between timed steps (write of a 512 MiB buffer); keys (1.8 GB) exceed L2",
+            "l2": "flushed between timed steps (write of a 512 MiB buffer); keys (%.1f GB) exceed L2" % (
+                (fheacc_key_bytes(P)) / 1e9),
             "parallelism": "one batch per GPU (independent gates, no collective)"}
 
 
@@ -485,7 +493,7 @@ def main():
         from oracle_lib import Oracle
         ora = Oracle.from_params(P)
         cores = cpu_cores()
-        nsample = args.cpu_sample or 8 * cores
+        nsample = args.cpu_sample or (8 if P.N == 1024 else 2) * cores
         t0 = time.perf_counter()
         co, failed = ora.eval_bootstrap_batch(c1[:nsample], c2[:nsample], gates[:nsample], bt, ks, threads=cores)
         dt = time.perf_counter() - t0
@@ -504,7 +512,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "bootstraps/s", "n_gpus": D.ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32" if P.N == 1024 else "u64", "data": "synthetic",
         "config": config_of(P, args),
         "e2e": {"value": e2e_value, "unit": "bootstraps/s",
                 "h2d_bytes_per_step": int(2 * B * W * 8 + B * 4), "d2h_bytes_per_step": int(B * W * 8),

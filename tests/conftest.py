@@ -60,6 +60,13 @@ def keys0(F):
 
 
 @pytest.fixture(scope="session")
+def keys1(F):
+    """Preset 1 (N=2048, Q < 2^54, BG 2^9 x 6, n=630) key set; the bootstrap
+    key is 11.4 GB of host memory."""
+    return KeySet(F, 1)
+
+
+@pytest.fixture(scope="session")
 def cuda_ok():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
@@ -72,6 +79,15 @@ def ctx0(F, keys0, cuda_ok):
     ctx = F.Context(keys0.P, 0)
     ctx.upload_bootstrap_key(keys0.btkey)
     ctx.upload_keyswitch_key(keys0.kskey)
+    yield ctx
+    ctx.close()
+
+
+@pytest.fixture(scope="session")
+def ctx1(F, keys1, cuda_ok):
+    ctx = F.Context(keys1.P, 0)
+    ctx.upload_bootstrap_key(keys1.btkey)
+    ctx.upload_keyswitch_key(keys1.kskey)
     yield ctx
     ctx.close()
 

@@ -1,0 +1,81 @@
+"""The 64-bit path (N=2048, Q=18014398509404161 < 2^54, BG=2^9 x 6, n=630)
+against the oracle, bit-exact."""
+import numpy as np
+import pytest
+
+from conftest import random_gate_batch
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint64).view(np.int64)).cuda()
+
+
+def host(t):
+    return t.cpu().numpy().view(np.uint64)
+
+
+def test_wide_ntt(F, ctx1, keys1, cuda_ok):
+    torch = cuda_ok
+    o = keys1.oracle
+    Q = keys1.P.Q
+    a = np.random.default_rng(1).integers(0, Q, (5, 2048), dtype=np.uint64)
+    a[0, :4] = [0, 1, Q - 1, Q // 2]
+    d = dev(torch, a)
+    ctx1.ntt_forward(d.data_ptr(), 5)
+    torch.cuda.synchronize()
+    assert np.array_equal(host(d), np.stack([o.ntt(x) for x in a]))
+    ctx1.ntt_inverse(d.data_ptr(), 5)
+    torch.cuda.synchronize()
+    assert np.array_equal(host(d), a)
+
+
+def test_wide_rlwe_mult_rgsw(F, ctx1, keys1, cuda_ok):
+    torch = cuda_ok
+    o = keys1.oracle
+    Q = keys1.P.Q
+    rng = np.random.default_rng(2)
+    acc = rng.integers(0, Q, (3, 4096), dtype=np.uint64)
+    acc[0] = Q - 1
+    rgsw = rng.integers(0, Q, (3, 6 * 4 * 2048), dtype=np.uint64)
+    out = torch.zeros((3, 4096), dtype=torch.int64, device="cuda")
+    da, dr = dev(torch, acc), dev(torch, rgsw)
+    ctx1.rlwe_mult_rgsw(da.data_ptr(), dr.data_ptr(), out.data_ptr(), 3)
+    torch.cuda.synchronize()
+    assert np.array_equal(host(out), np.stack([o.rlwe_mult_rgsw(acc[i], rgsw[i]) for i in range(3)]))
+
+
+def test_wide_keyswitch(F, ctx1, keys1, cuda_ok):
+    torch = cuda_ok
+    o = keys1.oracle
+    rl = np.random.default_rng(3).integers(0, keys1.P.Q, (2, 4096), dtype=np.uint64)
+    dr = dev(torch, rl)
+    out = torch.zeros((2, keys1.P.n + 1), dtype=torch.int64, device="cuda")
+    ctx1.lwe_keyswitch_async(dr.data_ptr(), 2, out.data_ptr())
+    ctx1.sync()
+    assert np.array_equal(host(out), np.stack([o.lwe_keyswitch(r, keys1.kskey) for r in rl]))
+
+
+def test_wide_bootstrap_all_gates(F, ctx1, keys1):
+    x, y, g, c1, c2 = random_gate_batch(keys1, 12, seed=5, gates=[0, 1, 2, 3, 4, 5] * 2)
+    out = ctx1.eval_bootstrap_batch(c1, c2, g)
+    want, failed = keys1.oracle.eval_bootstrap_batch(c1, c2, g, keys1.btkey, keys1.kskey)
+    assert failed == 0
+    assert np.array_equal(out, want)
+    truth = np.array([F.gate_truth(int(a), b, c) for a, b, c in zip(g, x, y)], dtype=np.uint8)
+    assert np.array_equal(keys1.decrypt(out), truth)
+
+
+def test_wide_blind_rotate(F, ctx1, keys1, cuda_ok):
+    torch = cuda_ok
+    x, y, g, c1, c2 = random_gate_batch(keys1, 2, seed=6)
+    d1, d2, dg = dev(torch, c1), dev(torch, c2), torch.from_numpy(g).cuda()
+    acc = torch.zeros((2, 4096), dtype=torch.int64, device="cuda")
+    ctx1.blind_rotate_async(d1.data_ptr(), d2.data_ptr(), dg.data_ptr(), 2, acc.data_ptr())
+    ctx1.sync()
+    got = host(acc)
+    for i in range(2):
+        want, steps = keys1.oracle.blind_rotate(c1[i], c2[i], int(g[i]), keys1.btkey)
+        assert steps > 1150
+        assert np.array_equal(got[i], want)

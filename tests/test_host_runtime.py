@@ -118,3 +118,14 @@ def test_oracle_equals_reference_outputs(F, keys0):
     assert np.array_equal(out, fx["out"].astype(np.uint64))
     truth = np.array([F.gate_truth(int(a), b, c) for a, b, c in zip(g, x, y)], dtype=np.uint8)
     assert np.array_equal(keys0.decrypt(out), truth)
+
+
+def test_wide_preset_oracle_bootstrap(F, keys1):
+    """Preset 1 keys from the host generator bootstrap correctly in the oracle
+    (N=2048, Q < 2^54, BG 2^9 x 6)."""
+    x = np.array([1, 0], dtype=np.uint8)
+    y = np.array([1, 1], dtype=np.uint8)
+    c = keys1.encrypt(np.concatenate([x, y]), seed=3)
+    out, failed = keys1.oracle.eval_bootstrap_batch(c[:2], c[2:], [F.NAND, F.XOR], keys1.btkey, keys1.kskey)
+    assert failed == 0
+    assert np.array_equal(keys1.decrypt(out), [0, 1])
