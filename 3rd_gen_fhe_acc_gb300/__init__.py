@@ -114,6 +114,10 @@ def lib():
             "fheacc_bootstrap_async": (ctypes.c_int, [vp, vp, vp, vp, sz, vp, ctypes.c_uint32, vp]),
             "fheacc_bootstrap_plain_async": (ctypes.c_int, [vp, vp, vp, vp, sz, vp, ctypes.c_uint32, vp]),
             "fheacc_bootstrap_noalloc": (ctypes.c_int, [vp, vp, vp, vp, sz, vp, ctypes.c_uint32, vp]),
+            "fheacc_rlwe_substitute_async": (ctypes.c_int, [vp, vp, sz, ctypes.c_int, vp, vp]),
+            "fheacc_rlwe_keyswitch_async": (ctypes.c_int, [vp, vp, sz, vp, vp, vp]),
+            "fheacc_subs_keyswitch_async": (ctypes.c_int, [vp, vp, sz, ctypes.c_int, vp, vp]),
+            "fheacc_expand_rlwe": (ctypes.c_int, [vp, vp, vp, vp]),
             "fheacc_server_create": (ctypes.c_int, [vp, sz, sz, ctypes.POINTER(vp)]),
             "fheacc_server_submit": (ctypes.c_int, [vp, _u64p, ctypes.c_uint32, _i32p, _u32p, _u32p, ctypes.c_uint32,
                                                     ctypes.c_uint32, _u64p, ctypes.POINTER(ctypes.c_uint64)]),
@@ -396,6 +400,22 @@ class Context:
 
     def lwe_modswitch_async(self, d_in, count, d_out, stream=0):
         self.check(lib().fheacc_lwe_modswitch_async(self._h, d_in, count, d_out, stream or None))
+
+    def rlwe_substitute_async(self, d_in, count, f, d_out, stream=0):
+        """RLWE_substitute (RLWE.cpp:444) of count NTT RLWEs."""
+        self.check(lib().fheacc_rlwe_substitute_async(self._h, d_in, count, f, d_out, stream or None))
+
+    def rlwe_keyswitch_async(self, d_in, count, d_ksk, d_out, stream=0):
+        """RLWE_keyswitch (RLWE.cpp:464) with one key [digitKS_R][2][N]."""
+        self.check(lib().fheacc_rlwe_keyswitch_async(self._h, d_in, count, d_ksk, d_out, stream or None))
+
+    def subs_keyswitch_async(self, d_in, count, f, d_out, stream=0):
+        """RLWE_keyswitch(RLWE_substitute(c, f), subs_key[f]) -- the RLWESUBS op."""
+        self.check(lib().fheacc_subs_keyswitch_async(self._h, d_in, count, f, d_out, stream or None))
+
+    def expand_RLWE(self, d_in, d_out, stream=0):
+        """application::expand_RLWE (app.cpp:26): d_out = [N][2N] RLWEs."""
+        self.check(lib().fheacc_expand_rlwe(self._h, d_in, d_out, stream or None))
 
     def sync(self, timeout_ms=0):
         self.check(lib().fheacc_sync(self._h, timeout_ms))

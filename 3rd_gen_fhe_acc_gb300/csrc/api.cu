@@ -141,6 +141,24 @@ int build_tables(Context &c)
     return FHEACC_OK;
 }
 
+// NTT(-X^(N - 2^j)) for j < log2 N, as rotate_vector_gen(false) builds them
+// (params.cpp:196-207); used by expand_RLWE's RLWE_rotate_freq.
+int build_rotations(Context &c)
+{
+    host::Tables T;
+    T.build(c.p);
+    const int N = c.p.N, logN = T.logN;
+    std::vector<uint64_t> rot((size_t)logN * N, 0);
+    for (int j = 0; j < logN; j++) {
+        uint64_t *v = rot.data() + (size_t)j * N;
+        v[N - (1 << j)] = c.p.Q - 1;
+        T.ntt(v);
+    }
+    cudaError_t e = cudaMalloc(&c.d_rot, rot.size() * sizeof(uint64_t));
+    if (e == cudaSuccess) e = cudaMemcpy(c.d_rot, rot.data(), rot.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "rotation tables");
+}
+
 // Copies `words` 32-bit words from a host vector into device memory in chunks.
 int upload_u32(Context &c, uint32_t *dst, const uint32_t *src, size_t words)
 {
@@ -216,6 +234,7 @@ int fheacc_create(const fheacc_params *p, int device, fheacc_ctx **out)
         return FHEACC_EIO;
     }
     int rc = build_tables(*c);
+    if (rc == FHEACC_OK) rc = build_rotations(*c);
     if (rc != FHEACC_OK) {
         g_create_error = c->err;
         fheacc_destroy(reinterpret_cast<fheacc_ctx *>(c));
@@ -237,6 +256,8 @@ int fheacc_destroy(fheacc_ctx *ctx)
     cudaFree(c->d_itw64);
     cudaFree(c->d_btkey64);
     cudaFree(c->d_kskey64);
+    cudaFree(c->d_subs64);
+    cudaFree(c->d_rot);
     cudaFree(c->d_btkey);
     cudaFree(c->d_kskey);
     cudaFree(c->d_subs);
@@ -388,6 +409,28 @@ int fheacc_upload_subs_key(fheacc_ctx *ctx, const uint64_t *subs_key, size_t wor
     Context &c = *reinterpret_cast<Context *>(ctx);
     if (!subs_key || words != fheacc_subs_key_words(&c.p)) return c.fail(FHEACC_EINVAL, "substitute key size mismatch");
     DeviceGuard g(c.device);
+    if (c.wide) {
+        if (!c.d_subs64) {
+            cudaError_t e = cudaMalloc(&c.d_subs64, words * sizeof(ulonglong2));
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                c.d_subs64 = nullptr;
+                return c.fail(FHEACC_ENOMEM, "device memory for the substitute key");
+            }
+            c.subs_bytes = words * sizeof(ulonglong2);
+        }
+        uint64_t *d_stage = nullptr;
+        cudaError_t e = cudaMalloc(&d_stage, words * sizeof(uint64_t));
+        if (e == cudaSuccess) e = cudaMemcpy(d_stage, subs_key, words * sizeof(uint64_t), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(d_stage);
+            return c.cuda_fail(e, "substitute key upload");
+        }
+        int rc = launch_shoup_pairs64(c, d_stage, c.d_subs64, words, c.stream);
+        if (!rc && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = c.cuda_fail(cudaGetLastError(), "key pairs");
+        cudaFree(d_stage);
+        return rc;
+    }
     if (!c.d_subs) {
         cudaError_t e = cudaMalloc(&c.d_subs, words * sizeof(uint32_t));
         if (e != cudaSuccess) {
@@ -604,6 +647,72 @@ int fheacc_measure_imad_rate(fheacc_ctx *ctx, double *imad_per_s)
     Context &c = *reinterpret_cast<Context *>(ctx);
     DeviceGuard g(c.device);
     return measure_imad_rate(c, imad_per_s);
+}
+
+static const void *subs_key_level(Context &c, int f)
+{
+    const size_t per = (size_t)c.p.digitKS_R * 2 * c.p.N;
+    if (c.wide) return c.d_subs64 ? (const void *)(c.d_subs64 + (size_t)f * per) : nullptr;
+    return c.d_subs ? (const void *)(c.d_subs + (size_t)f * per) : nullptr;
+}
+
+int fheacc_rlwe_substitute_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t count, int f, uint64_t *d_out,
+                                 void *stream)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    DeviceGuard g(c.device);
+    cudaStream_t st = pick_stream(&c, stream);
+    return mark_done(c, st, launch_expand(c, 0, d_in, d_out, count, f, nullptr, nullptr, st));
+}
+
+int fheacc_rlwe_keyswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t count, const uint64_t *d_ksk,
+                                uint64_t *d_out, void *stream)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    if (count && !d_ksk) return c.fail(FHEACC_EINVAL, "null key");
+    DeviceGuard g(c.device);
+    cudaStream_t st = pick_stream(&c, stream);
+    const size_t words = (size_t)c.p.digitKS_R * 2 * c.p.N;
+    int rc = ensure_scratch(c, c.io, words * (c.wide ? sizeof(ulonglong2) : sizeof(uint32_t)));
+    if (rc) return rc;
+    rc = c.wide ? launch_shoup_pairs64(c, d_ksk, (ulonglong2 *)c.io.ptr, words, st)
+                : launch_to_u32(c, d_ksk, (uint32_t *)c.io.ptr, words, st);
+    if (rc) return rc;
+    return mark_done(c, st, launch_expand(c, 1, d_in, d_out, count, 0, c.io.ptr, nullptr, st));
+}
+
+int fheacc_subs_keyswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t count, int f, uint64_t *d_out,
+                                void *stream)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    const int logN = c.wide ? 11 : 10;
+    if (f < 0 || f >= logN) return c.fail(FHEACC_EINVAL, "substitution factor out of range");
+    const void *key = subs_key_level(c, f);
+    if (!key) return c.fail(FHEACC_ENOKEY, "substitute key not uploaded");
+    DeviceGuard g(c.device);
+    cudaStream_t st = pick_stream(&c, stream);
+    return mark_done(c, st, launch_expand(c, 2, d_in, d_out, count, f, key, nullptr, st));
+}
+
+int fheacc_expand_rlwe(fheacc_ctx *ctx, const uint64_t *d_in, uint64_t *d_out, void *stream)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    if (!d_in || !d_out) return c.fail(FHEACC_EINVAL, "null buffer");
+    if (!subs_key_level(c, 0)) return c.fail(FHEACC_ENOKEY, "substitute key not uploaded");
+    DeviceGuard g(c.device);
+    cudaStream_t st = pick_stream(&c, stream);
+    const int N = c.p.N, logN = c.wide ? 11 : 10;
+    cudaError_t e = cudaMemcpyAsync(d_out, d_in, 2 * (size_t)N * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return c.cuda_fail(e, "expand copy");
+    for (int f = 0; f < logN; f++) {
+        int rc = launch_expand(c, 3, d_out, d_out, 0, f, subs_key_level(c, f), c.d_rot + (size_t)f * N, st);
+        if (rc) return rc;
+    }
+    return mark_done(c, st, FHEACC_OK);
 }
 
 int fheacc_sync(fheacc_ctx *ctx, uint32_t timeout_ms)

@@ -52,6 +52,8 @@ struct Context {
     ulonglong2 *d_tw64 = nullptr, *d_itw64 = nullptr;
     dev::Ntt64Consts nc64{};
     ulonglong2 *d_btkey64 = nullptr;   // Shoup pairs, [(i*digitR + j)*Br + r][digitG][2][2][N]
+    ulonglong2 *d_subs64 = nullptr;    // Shoup pairs, [logN][digitKS_R][2][N]
+    uint64_t *d_rot = nullptr;         // [logN][N]: NTT(-X^(N - 2^j)), rotate_vector_gen(false)
     uint64_t *d_kskey64 = nullptr;     // [(d*digitKS + j)*N + i][ks_row]
 
     // keys, device layouts
@@ -127,6 +129,11 @@ int launch_blind_rotate64(Context &c, const uint64_t *d_c1, const uint64_t *d_c2
 int launch_extract64(Context &c, const uint64_t *d_rlwe, size_t count, uint64_t *d_extract, cudaStream_t st);
 int launch_lwe_keyswitch64(Context &c, const uint64_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
                            cudaStream_t st);
+// automorphism / key switch / expand (expand.cu); mode: 0 SUBS, 1 KS,
+// 2 SUBS_KS, 3 EXPAND (one level f, in place on d_out)
+int launch_expand(Context &c, int mode, const uint64_t *d_in, uint64_t *d_out, size_t count, int f,
+                  const void *ksk, const uint64_t *d_rot, cudaStream_t st);
+int launch_to_u32(Context &c, const uint64_t *d_in, uint32_t *d_out, size_t n, cudaStream_t st);
 // IMAD throughput probe (probe.cu)
 int measure_imad_rate(Context &c, double *imad_per_s);
 

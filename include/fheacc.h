@@ -255,6 +255,25 @@ int fheacc_server_poll(fheacc_server *srv, fheacc_request_done *done, size_t max
 int fheacc_server_stats(fheacc_server *srv, fheacc_server_stats_t *stats);
 int fheacc_server_destroy(fheacc_server *srv);
 
+/* ------------------------------------------------- automorphism and expand
+ * DEVICE buffers of canonical NTT-domain RLWEs ([count][2N] words),
+ * asynchronous on `stream`. f is the substitution factor: X -> X^(N/2^f + 1),
+ * 0 <= f < log2 N. */
+/* RLWE_substitute (RLWE.cpp:444-462). */
+int fheacc_rlwe_substitute_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t count, int f, uint64_t *d_out,
+                                 void *stream);
+/* RLWE_keyswitch (RLWE.cpp:464-510) of every input with one key given in the
+ * reference layout [digitKS_R][2][N] (device words). */
+int fheacc_rlwe_keyswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t count, const uint64_t *d_ksk,
+                                uint64_t *d_out, void *stream);
+/* RLWE_keyswitch(RLWE_substitute(c, f), subs_key[f]) with the uploaded
+ * substitute key: the FPGA's RLWESUBS instruction (myfpga.cpp:1708-1745). */
+int fheacc_subs_keyswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t count, int f, uint64_t *d_out,
+                                void *stream);
+/* application::expand_RLWE (app.cpp:26-76): d_out = [N] RLWEs. Replaces
+ * fpga_expand_RLWE (myfpga.cpp:1662-1790). Needs the substitute key. */
+int fheacc_expand_rlwe(fheacc_ctx *ctx, const uint64_t *d_in, uint64_t *d_out, void *stream);
+
 /* Wait until the most recent asynchronous call of the context (and every
  * blocking call) has finished, at most timeout_ms (0 = no limit). */
 int fheacc_sync(fheacc_ctx *ctx, uint32_t timeout_ms);
