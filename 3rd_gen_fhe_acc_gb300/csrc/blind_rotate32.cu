@@ -101,6 +101,49 @@ __device__ __forceinline__ void named_barrier(int id, int threads)
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
 }
 
+// Plans the next pipeline period (run by one thread). ctl: [0, 1] cursor
+// (step, ciphertext) of the last item taken by the inverse-NTT warps; [2, 3]
+// item of the digit warps; [4] slot; [5] cursor exhausted; [6] this period's
+// inverse-NTT item valid; [7] stop. On the first call ctl[6] is 0 and the
+// digit warps have no item. An item whose ciphertext is still held by the
+// digit warps waits one period.
+__device__ __noinline__ void pipe_schedule(int *ctl, const uint8_t *res, int m, int S, bool compat)
+{
+    // the inverse-NTT item of the period just run moves to the digit warps
+    if (ctl[6]) {
+        ctl[2] = ctl[0];
+        ctl[3] = ctl[1];
+    } else {
+        ctl[2] = -1;
+        ctl[3] = -1;
+    }
+    int ns = ctl[0], nk = ctl[1];
+    bool found = false;
+    if (!ctl[5]) {
+        for (;;) {
+            if (++nk == m) {
+                nk = 0;
+                ++ns;
+            }
+            if (ns >= S) break;
+            if (compat || res[nk * S + ns]) {
+                found = true;
+                break;
+            }
+        }
+        if (!found) ctl[5] = 1;
+    }
+    const bool hv = found && !(ctl[3] >= 0 && ctl[3] == nk);
+    if (hv) {
+        ctl[0] = ns;
+        ctl[1] = nk;
+    }
+    ctl[6] = hv;
+    ctl[7] = !hv && ctl[3] < 0 && ctl[5];
+    // slot: the inverse-NTT warps alternate slots every period
+    ctl[4] ^= 1;
+}
+
 template <int DG, int MINB>
 __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
     br32_pipe_kernel(const __grid_constant__ PipeArgs A, const __grid_constant__ Ntt32Consts c,
@@ -112,6 +155,7 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PipeSmem<DG> &s = *reinterpret_cast<PipeSmem<DG> *>(smem_raw);
     uint8_t *res = smem_raw + sizeof(PipeSmem<DG>);   // [kMaxGroup][n * digitR] residues
+    __shared__ int ctl[8];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = A.n, S = n * (int)A.digitR;
     const uint32_t q = A.q, qmask = q - 1;
@@ -169,45 +213,32 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
         }
         __syncthreads();
 
-        // ---- pipeline over the (step, ciphertext) items of the group
-        int hs = 0, hk = -1;   // cursor: last item taken by the inverse-NTT warps
-        int gs = -1, gk = -1;  // item of the digit warps (gk < 0: none)
-        int sh = 0;            // slot written by the inverse-NTT warps this period
-        bool hdone = (m == 0);
+        // ---- pipeline over the (step, ciphertext) items of the group. Thread 0
+        // schedules: it picks the next item of the inverse-NTT warps after each
+        // period and publishes the period's plan in shared memory.
+        if (threadIdx.x == 0) {
+            ctl[0] = 0; ctl[1] = -1;      // cursor (step, ciphertext) of the last item taken
+            ctl[2] = -1; ctl[3] = -1;     // item of the digit warps (ciphertext < 0: none)
+            ctl[4] = 0;                   // slot written by the inverse-NTT warps
+            ctl[5] = m == 0;              // no more items for the inverse-NTT warps
+            ctl[6] = 0; ctl[7] = 0;       // this period: inverse-NTT item valid, stop
+            pipe_schedule(ctl, res, m, S, compat);
+        }
+        __syncthreads();
         for (;;) {
-            int ns = hs, nk = hk;
-            bool found = false;
-            if (!hdone) {
-                for (;;) {
-                    if (++nk == m) {
-                        nk = 0;
-                        ++ns;
-                    }
-                    if (ns >= S) break;
-                    if (compat || res[nk * S + ns]) {
-                        found = true;
-                        break;
-                    }
-                }
-                if (!found) hdone = true;
-            }
-            const bool hv = found && !(gk >= 0 && gk == nk);
-            if (hv) {
-                hs = ns;
-                hk = nk;
-            }
-            if (!hv && gk < 0 && hdone) break;
-
+            if (ctl[7]) break;
+            const int sh = ctl[4];
             if (warp >= GW) {
-                if (hv) {
+                if (ctl[6]) {
                     const int hp = warp - GW;
                     uint32_t x[32];
-                    load_btile(x, A.accs + (first + (size_t)hk * G) * 2048 + hp * 1024, lane);
+                    load_btile(x, A.accs + (first + (size_t)ctl[1] * G) * 2048 + hp * 1024, lane);
                     uint32_t *ts = s.tslot[sh][hp];
                     ntt_inv_1024(x, c, inv_tw, ts, lane);
                     store_row(ts, lane, x);
                 }
-            } else if (gk >= 0) {
+            } else if (ctl[3] >= 0) {
+                const int gk = ctl[3], gs = ctl[2];
                 const int p = warp / DG, h = warp % DG;
                 const uint32_t shift = A.bg_bits * h, mask = (1u << A.bg_bits) - 1;
                 uint32_t x[32];
@@ -244,14 +275,8 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
                 }
             }
             __syncthreads();
-            if (hv) {
-                gs = hs;
-                gk = hk;
-            } else {
-                gs = -1;
-                gk = -1;
-            }
-            sh ^= 1;
+            if (threadIdx.x == 0) pipe_schedule(ctl, res, m, S, compat);
+            __syncthreads();
         }
 
         // ---- epilogue: NTT accumulators out, or extraction for the key switch
