@@ -214,6 +214,12 @@ int fheacc_create(const fheacc_params *p, int device, fheacc_ctx **out)
     d.gate_constant[6] = d.gate_constant[7] = 0;
     d.mu64 = (uint64_t)(((unsigned __int128)1 << 64) / pp.Q);
     d.ks_row = (uint32_t)(((pp.n + 1) + 31) / 32 * 32);
+    if (!wide) {
+        d.key_factor = (uint32_t)host::mulmod(((uint64_t)1 << 32) % pp.Q, pp.iN, pp.Q);
+        uint32_t inv = 1;   // Q^-1 mod 2^32 by Newton iteration (Q odd)
+        for (int it = 0; it < 5; it++) inv *= 2u - (uint32_t)pp.Q * inv;
+        d.qinv_neg = 0u - inv;
+    }
     e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         g_create_error = std::string("stream creation failed: ") + cudaGetErrorString(e);
@@ -337,14 +343,20 @@ int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t w
         }
         c.btkey_bytes = words * sizeof(uint32_t);
     }
-    // host [r][j][i] -> device [(i * digitR + j) * Br + r], one step (all r) per chunk
+    // host [r][j][i] -> device [(i * digitR + j) * Br + r], one step (all r) per
+    // chunk; words times 2^32 N^-1 mod Q (see DevParams::key_factor)
+    const uint64_t kf = c.dp.key_factor, kfs = shoup32_companion(kf, Q);
     std::vector<uint32_t> stage(Br * rw);
     for (size_t i = 0; i < n; i++) {
         for (size_t j = 0; j < dR; j++) {
             for (size_t r = 0; r < Br; r++) {
                 const uint64_t *src = btkey + ((r * dR + j) * n + i) * rw;
                 uint32_t *dst = stage.data() + r * rw;
-                for (size_t x = 0; x < rw; x++) dst[(x & ~(size_t)1023) + btile_index(x & 1023)] = (uint32_t)(src[x] % Q);
+                for (size_t x = 0; x < rw; x++) {
+                    const uint64_t a = src[x] % Q;
+                    uint64_t v = a * kf - ((a * kfs) >> 32) * Q;   // Shoup: [0, 2Q)
+                    dst[(x & ~(size_t)1023) + btile_index(x & 1023)] = (uint32_t)(v >= Q ? v - Q : v);
+                }
             }
             int rc = upload_u32(c, c.d_btkey + (i * dR + j) * Br * rw, stage.data(), Br * rw);
             if (rc) return rc;

@@ -24,10 +24,19 @@
 //   inverse-NTT warps (2): load acc of item k+1, inverse NTT of a and b,
 //                          canonical time-domain coefficients -> tslot[k+1 & 1]
 //   digit warps (2*digitG): item k: digit h of poly p from tslot[k & 1],
-//                          forward NTT -> dbuf; named barrier; multiply-
-//                          accumulate with the item's RGSW key (64-bit sums,
-//                          one Barrett reduction per output) -> acc (global)
+//                          forward NTT (first two stages by table lookup,
+//                          ntt_fwd_1024_digit) -> dbuf; named barrier;
+//                          multiply-accumulate with the item's RGSW key
+//                          (64-bit sums, one Montgomery reduction per output)
+//                          -> acc (global)
 // An item whose ciphertext is still in the digit stage waits one period.
+//
+// Scaling. The bootstrap key is uploaded times 2^32 N^-1 mod Q: the Montgomery
+// reduction of the sums removes the 2^32, and the N^-1 the reference's iNTT
+// applies is already in the accumulator, so the inverse transforms skip it
+// (ntt_inv_1024_noscale). The initial accumulator is the reference's test
+// vector times N^-1; canonical NTT-domain accumulators are multiplied by N on
+// the way out. All results are the reference's values mod Q.
 //
 // Global layouts. Accumulators and bootstrap-key polys are stored "B-tiled":
 // element 32 l + r of a poly sits at word ((r / 4) * 32 + l) * 4 + r % 4, so a
@@ -54,7 +63,10 @@ struct PipeArgs {
     uint32_t *extract;       // optional: [count][kExtractStride]
     int n;
     uint32_t q, embed, Br, digitR, bg_bits, flags;
-    uint64_t mu64;
+    uint32_t qinv_neg;         // -Q^-1 mod 2^32 (keys carry 2^32 N^-1, see DevParams::key_factor)
+    uint32_t tv_pos, tv_neg;   // test-vector values +-(Q/8 + 1) times N^-1
+    uint32_t nmul, nmuls;      // N mod Q and its Shoup companion (canonical accumulators out)
+    uint32_t w21, w31;         // rou[2] rou[1], rou[3] rou[1] mod Q (digit tables)
     uint64_t gate_constant[8];
 };
 
@@ -66,6 +78,14 @@ struct PipeSmem {
     uint32_t tslot[2][2][kN32];   // time-domain accumulators, one slot per pipeline stage
     uint32_t dbuf[2 * DG][kN32];  // digit NTT outputs / transposes of the digit warps
 };
+
+// Bytes of dynamic shared memory before the digit tables: PipeSmem, then the
+// residue table [kMaxGroup][n * digitR], rounded up to 16.
+template <int DG>
+__host__ __device__ constexpr size_t pipe_tables_offset(size_t steps)
+{
+    return sizeof(PipeSmem<DG>) + ((size_t)kMaxGroup * steps + 15) / 16 * 16;
+}
 
 __device__ __forceinline__ void load_btile(uint32_t (&x)[32], const uint32_t *src, int lane)
 {
@@ -99,6 +119,44 @@ __device__ __forceinline__ void store_btile(uint32_t *dst, const uint32_t (&x)[3
 __device__ __forceinline__ void named_barrier(int id, int threads)
 {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
+// Montgomery reduction of a multiply-accumulate sum s < 2^62: s 2^-32 mod Q
+// in [0, 2Q). The sum of 2 digitG products (NTT digits < 21Q, keys < Q) is
+// below 168 Q^2, so (s + m Q) / 2^32 < 6.25 Q before the two conditional
+// subtractions.
+__device__ __forceinline__ uint32_t mont_reduce_2q(uint64_t s, uint32_t Q, uint32_t qinv_neg)
+{
+    const uint32_t m = (uint32_t)s * qinv_neg;
+    uint32_t r = (uint32_t)((s + (uint64_t)m * Q) >> 32);
+    r = min(r, r - 4 * Q);
+    return min(r, r - 2 * Q);
+}
+
+// Multiply-accumulate of one 4-element chunk u (elements 32 (u % 32) + 4 (u / 32)
+// + 0..3 of both output polys): acc[P][e] = sum over (p, h) of dbuf[p][h][e] *
+// key[h][p][P][e], Montgomery-reduced.
+template <int DG>
+__device__ __forceinline__ void mac_chunk(int u, const uint4 *__restrict__ key,
+                                          const uint32_t (*dbuf)[kN32], uint4 *acc, uint32_t Q, uint32_t qinv_neg)
+{
+    const int pa = sw_chunk(u & 31, u >> 5);
+    uint64_t sa[4] = {0, 0, 0, 0}, sb[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int qi = 0; qi < 2 * DG; qi++) {
+        const int pp = qi / DG, hh = qi % DG;
+        const uint4 dv = *reinterpret_cast<const uint4 *>(dbuf[pp * DG + hh] + pa);
+        const uint4 a4 = __ldg(key + ((hh * 2 + pp) * 2 + 0) * 256 + u);
+        const uint4 b4 = __ldg(key + ((hh * 2 + pp) * 2 + 1) * 256 + u);
+        sa[0] += (uint64_t)dv.x * a4.x; sb[0] += (uint64_t)dv.x * b4.x;
+        sa[1] += (uint64_t)dv.y * a4.y; sb[1] += (uint64_t)dv.y * b4.y;
+        sa[2] += (uint64_t)dv.z * a4.z; sb[2] += (uint64_t)dv.z * b4.z;
+        sa[3] += (uint64_t)dv.w * a4.w; sb[3] += (uint64_t)dv.w * b4.w;
+    }
+    __stcg(acc + u, make_uint4(mont_reduce_2q(sa[0], Q, qinv_neg), mont_reduce_2q(sa[1], Q, qinv_neg),
+                               mont_reduce_2q(sa[2], Q, qinv_neg), mont_reduce_2q(sa[3], Q, qinv_neg)));
+    __stcg(acc + 256 + u, make_uint4(mont_reduce_2q(sb[0], Q, qinv_neg), mont_reduce_2q(sb[1], Q, qinv_neg),
+                                     mont_reduce_2q(sb[2], Q, qinv_neg), mont_reduce_2q(sb[3], Q, qinv_neg)));
 }
 
 // Plans the next pipeline period (run by one thread). ctl: [0, 1] cursor
@@ -163,6 +221,19 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
     const bool compat = (A.flags & FHEACC_FLAG_FPGA_COMPAT) != 0;
     const size_t G = gridDim.x;
 
+    // digit tables (ntt_fwd_1024_digit): t1 [BG], t23 [BG], t123 [BG]
+    const int BG = 1 << A.bg_bits;
+    uint32_t *t1 = reinterpret_cast<uint32_t *>(smem_raw + pipe_tables_offset<DG>(S));
+    uint2 *t23 = reinterpret_cast<uint2 *>(t1 + BG), *t123 = t23 + BG;
+    for (int y = threadIdx.x; y < BG; y += blockDim.x) {
+        const uint64_t Q = c.Q;
+        t1[y] = (uint32_t)((uint64_t)y * c.fw[1] % Q);
+        t23[y] = make_uint2((uint32_t)((uint64_t)y * c.fw[2] % Q), (uint32_t)((uint64_t)y * c.fw[3] % Q));
+        t123[y] = make_uint2((uint32_t)((uint64_t)y * A.w21 % Q), (uint32_t)((uint64_t)y * A.w31 % Q));
+    }
+    const DigitTables dt{t1, t23, t123};
+    __syncthreads();
+
     for (size_t base = 0; base < A.count; base += G * kMaxGroup) {
         const size_t first = base + blockIdx.x;
         int m = 0;
@@ -187,7 +258,7 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
             const uint32_t bval = (uint32_t)(vb & qmask);
             const uint64_t gc = A.gate_constant[(unsigned)g < 6u ? g : 6];
             const uint32_t b1 = (uint32_t)(gc & qmask), b2 = (b1 + q / 2) & qmask;
-            const uint32_t Q8 = c.Q / 8 + 1, negQ8 = c.Q - Q8;
+            const uint32_t Q8 = A.tv_pos, negQ8 = A.tv_neg;
             uint32_t x[32];
 #pragma unroll
             for (int r = 0; r < 32; r++) {
@@ -234,7 +305,7 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
                     uint32_t x[32];
                     load_btile(x, A.accs + (first + (size_t)ctl[1] * G) * 2048 + hp * 1024, lane);
                     uint32_t *ts = s.tslot[sh][hp];
-                    ntt_inv_1024(x, c, inv_tw, ts, lane);
+                    ntt_inv_1024_noscale(x, c, inv_tw, ts, lane);
                     store_row(ts, lane, x);
                 }
             } else if (ctl[3] >= 0) {
@@ -245,34 +316,13 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
                 load_row(x, s.tslot[sh ^ 1][p], lane);
 #pragma unroll
                 for (int r = 0; r < 32; r++) x[r] = (x[r] >> shift) & mask;
-                ntt_fwd_1024(x, c, fwd_tw, s.dbuf[warp], lane);
+                ntt_fwd_1024_digit(x, c, fwd_tw, s.dbuf[warp], dt, lane);
                 store_row(s.dbuf[warp], lane, x);
-                named_barrier(1, GT);
                 const uint32_t rr = res[gk * S + gs];
                 const uint4 *key = reinterpret_cast<const uint4 *>(A.btkey + ((size_t)gs * A.Br + rr) * rgsw_words);
                 uint4 *acc = reinterpret_cast<uint4 *>(A.accs + (first + (size_t)gk * G) * 2048);
-                for (int u = threadIdx.x; u < 256; u += GT) {
-                    const int pa = sw_chunk(u & 31, u >> 5);   // elements 32 (u % 32) + 4 (u / 32) + 0..3
-                    uint64_t sa[4] = {0, 0, 0, 0}, sb[4] = {0, 0, 0, 0};
-#pragma unroll 1
-                    for (int pp = 0; pp < 2; pp++) {
-#pragma unroll
-                        for (int hh = 0; hh < DG; hh++) {
-                            const uint4 dv = *reinterpret_cast<const uint4 *>(s.dbuf[pp * DG + hh] + pa);
-                            const uint4 ka = __ldg(key + ((hh * 2 + pp) * 2 + 0) * 256 + u);
-                            const uint4 kb = __ldg(key + ((hh * 2 + pp) * 2 + 1) * 256 + u);
-                            sa[0] += (uint64_t)dv.x * ka.x; sb[0] += (uint64_t)dv.x * kb.x;
-                            sa[1] += (uint64_t)dv.y * ka.y; sb[1] += (uint64_t)dv.y * kb.y;
-                            sa[2] += (uint64_t)dv.z * ka.z; sb[2] += (uint64_t)dv.z * kb.z;
-                            sa[3] += (uint64_t)dv.w * ka.w; sb[3] += (uint64_t)dv.w * kb.w;
-                        }
-                    }
-                    __stcg(acc + u, make_uint4(barrett64_lazy(sa[0], A.mu64, c.Q), barrett64_lazy(sa[1], A.mu64, c.Q),
-                                               barrett64_lazy(sa[2], A.mu64, c.Q), barrett64_lazy(sa[3], A.mu64, c.Q)));
-                    __stcg(acc + 256 + u,
-                           make_uint4(barrett64_lazy(sb[0], A.mu64, c.Q), barrett64_lazy(sb[1], A.mu64, c.Q),
-                                      barrett64_lazy(sb[2], A.mu64, c.Q), barrett64_lazy(sb[3], A.mu64, c.Q)));
-                }
+                named_barrier(1, GT);
+                for (int u = threadIdx.x; u < 256; u += GT) mac_chunk<DG>(u, key, s.dbuf, acc, c.Q, A.qinv_neg);
             }
             __syncthreads();
             if (threadIdx.x == 0) pipe_schedule(ctl, res, m, S, compat);
@@ -289,7 +339,7 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
                 if (P == 0) load_btile_reversed(x, acc, lane);
                 else load_btile(x, acc, lane);
                 uint32_t *buf = warp < GW ? s.dbuf[warp] : s.tslot[0][warp - GW];
-                ntt_inv_1024(x, c, inv_tw, buf, lane);
+                ntt_inv_1024_noscale(x, c, inv_tw, buf, lane);
                 uint32_t *ext = A.extract + gid * kExtractStride;
                 if (P == 0) {
 #pragma unroll
@@ -301,7 +351,10 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
                 load_btile(x, acc, lane);
                 uint64_t *out = A.acc_out + gid * 2048 + P * 1024 + 32 * lane;
 #pragma unroll
-                for (int r = 0; r < 32; r++) out[r] = min(x[r], x[r] - c.Q);
+                for (int r = 0; r < 32; r++) {
+                    const uint32_t v = shoup32(x[r], A.nmul, A.nmuls, c.Q);   // times N: the key factor's N^-1 out
+                    out[r] = min(v, v - c.Q);
+                }
             }
         }
         __syncthreads();
@@ -321,22 +374,49 @@ template <int DG, int MINB>
 static int launch_pipe_dg(Context &c, const dev::PipeArgs &A, int max_ctas, cudaStream_t st)
 {
     constexpr int threads = 32 * (2 * DG + 2);
-    const size_t smem = sizeof(dev::PipeSmem<DG>) + (size_t)dev::kMaxGroup * c.p.n * c.p.digitR;
-    cudaError_t e = cudaFuncSetAttribute(dev::br32_pipe_kernel<DG, MINB>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    auto kern = dev::br32_pipe_kernel<DG, MINB>;
+    const size_t smem = dev::pipe_tables_offset<DG>((size_t)c.p.n * c.p.digitR) + 20 * ((size_t)1 << c.p.BG_bits);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return c.cuda_fail(e, "blind rotation smem attribute");
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::br32_pipe_kernel<DG, MINB>, threads, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
     if (per_sm < 1) per_sm = 1;
-    // at least two ciphertexts per CTA keep both pipeline stages busy
     if (c.tune.br_ctas_per_sm > 0) per_sm = std::min(per_sm, c.tune.br_ctas_per_sm);
+    // at least two ciphertexts per CTA keep both pipeline stages busy
     size_t blocks = std::min<size_t>((size_t)sm_count(c) * per_sm, (A.count + 1) / 2);
     if (max_ctas > 0) blocks = std::min<size_t>(blocks, (size_t)max_ctas);
     blocks = std::max<size_t>(blocks, 1);
-    dev::br32_pipe_kernel<DG, MINB><<<(unsigned)blocks, threads, smem, st>>>(A, c.nc, c.d_fwd_tw, c.d_inv_tw,
-                                                                            (uint32_t)((1ULL << 32) / c.p.Q));
+    kern<<<(unsigned)blocks, threads, smem, st>>>(A, c.nc, c.d_fwd_tw, c.d_inv_tw, (uint32_t)((1ULL << 32) / c.p.Q));
     e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "blind rotation launch");
+}
+
+// Parameter-set fields of PipeArgs.
+static void fill_pipe_params(Context &c, dev::PipeArgs &A, uint32_t flags)
+{
+    const uint64_t Q = c.p.Q;
+    A.btkey = c.d_btkey;
+    A.n = c.p.n; A.q = c.p.q; A.embed = c.dp.embed; A.Br = c.p.Br; A.digitR = c.p.digitR;
+    A.bg_bits = c.p.BG_bits; A.flags = flags;
+    A.qinv_neg = c.dp.qinv_neg;
+    A.tv_pos = (uint32_t)((unsigned __int128)(Q / 8 + 1) * c.p.iN % Q);
+    A.tv_neg = (uint32_t)(Q - A.tv_pos);
+    A.nmul = (uint32_t)(c.p.N % Q);
+    A.nmuls = (uint32_t)(((uint64_t)A.nmul << 32) / Q);
+    A.w21 = (uint32_t)((uint64_t)c.nc.fw[2] * c.nc.fw[1] % Q);
+    A.w31 = (uint32_t)((uint64_t)c.nc.fw[3] * c.nc.fw[1] % Q);
+    for (int i = 0; i < 8; i++) A.gate_constant[i] = c.dp.gate_constant[i];
+}
+
+static int launch_pipe(Context &c, const dev::PipeArgs &A, int max_ctas, cudaStream_t st)
+{
+    const bool three = c.tune.br_regs_for_3 != 0;
+    switch (c.p.digitG) {
+    case 2: return three ? launch_pipe_dg<2, 3>(c, A, max_ctas, st) : launch_pipe_dg<2, 2>(c, A, max_ctas, st);
+    case 3: return three ? launch_pipe_dg<3, 3>(c, A, max_ctas, st) : launch_pipe_dg<3, 2>(c, A, max_ctas, st);
+    case 4: return three ? launch_pipe_dg<4, 3>(c, A, max_ctas, st) : launch_pipe_dg<4, 2>(c, A, max_ctas, st);
+    default: return c.fail(FHEACC_EINVAL, "digitG must be 2..4 for the 32-bit path");
+    }
 }
 
 int launch_blind_rotate32(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
@@ -349,17 +429,9 @@ int launch_blind_rotate32(Context &c, const uint64_t *d_c1, const uint64_t *d_c2
     if (rc) return rc;
     dev::PipeArgs A{};
     A.c1 = d_c1; A.c2 = d_c2; A.gates = d_gates; A.count = count;
-    A.btkey = c.d_btkey; A.accs = (uint32_t *)c.accs.ptr; A.acc_out = d_acc_out; A.extract = d_extract;
-    A.n = c.p.n; A.q = c.p.q; A.embed = c.dp.embed; A.Br = c.p.Br; A.digitR = c.p.digitR;
-    A.bg_bits = c.p.BG_bits; A.flags = flags; A.mu64 = c.dp.mu64;
-    for (int i = 0; i < 8; i++) A.gate_constant[i] = c.dp.gate_constant[i];
-    const bool three = c.tune.br_regs_for_3 != 0;
-    switch (c.p.digitG) {
-    case 2: return three ? launch_pipe_dg<2, 3>(c, A, max_ctas, st) : launch_pipe_dg<2, 2>(c, A, max_ctas, st);
-    case 3: return three ? launch_pipe_dg<3, 3>(c, A, max_ctas, st) : launch_pipe_dg<3, 2>(c, A, max_ctas, st);
-    case 4: return three ? launch_pipe_dg<4, 3>(c, A, max_ctas, st) : launch_pipe_dg<4, 2>(c, A, max_ctas, st);
-    default: return c.fail(FHEACC_EINVAL, "digitG must be 2..4 for the 32-bit path");
-    }
+    A.accs = (uint32_t *)c.accs.ptr; A.acc_out = d_acc_out; A.extract = d_extract;
+    fill_pipe_params(c, A, flags);
+    return launch_pipe(c, A, max_ctas, st);
 }
 
 }  // namespace fheacc
@@ -383,17 +455,9 @@ int launch_blind_rotate32_indexed(Context &c, const uint64_t *d_c1, const uint64
     if (!c.d_btkey) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
     dev::PipeArgs A{};
     A.c1 = d_c1; A.c2 = d_c2; A.idx1 = d_idx1; A.idx2 = d_idx2; A.gates = d_gates; A.count = count;
-    A.btkey = c.d_btkey; A.accs = accs; A.acc_out = nullptr; A.extract = d_extract;
-    A.n = c.p.n; A.q = c.p.q; A.embed = c.dp.embed; A.Br = c.p.Br; A.digitR = c.p.digitR;
-    A.bg_bits = c.p.BG_bits; A.flags = flags; A.mu64 = c.dp.mu64;
-    for (int i = 0; i < 8; i++) A.gate_constant[i] = c.dp.gate_constant[i];
-    const bool three = c.tune.br_regs_for_3 != 0;
-    switch (c.p.digitG) {
-    case 2: return three ? launch_pipe_dg<2, 3>(c, A, 0, st) : launch_pipe_dg<2, 2>(c, A, 0, st);
-    case 3: return three ? launch_pipe_dg<3, 3>(c, A, 0, st) : launch_pipe_dg<3, 2>(c, A, 0, st);
-    case 4: return three ? launch_pipe_dg<4, 3>(c, A, 0, st) : launch_pipe_dg<4, 2>(c, A, 0, st);
-    default: return c.fail(FHEACC_EINVAL, "digitG must be 2..4 for the 32-bit path");
-    }
+    A.accs = accs; A.acc_out = nullptr; A.extract = d_extract;
+    fill_pipe_params(c, A, flags);
+    return launch_pipe(c, A, 0, st);
 }
 
 }  // namespace fheacc

@@ -19,6 +19,10 @@ struct DevParams {
     uint64_t gate_constant[8];  // entries 6, 7 are 0 (guard for bad gate codes)
     uint64_t mu64;              // floor(2^64 / Q), Barrett constant
     uint32_t ks_row;            // padded words per LWE key-switch row (>= n+1, multiple of 32)
+    // 32-bit path: bootstrap-key words are stored times key_factor = 2^32 N^-1
+    // mod Q, so a Montgomery reduction (qinv_neg = -Q^-1 mod 2^32) of the
+    // multiply-accumulate sums both reduces them and carries the iNTT's N^-1.
+    uint32_t key_factor, qinv_neg;
 };
 
 // Launch-shape choices of the blind-rotation kernel (set by fheacc_set_option

@@ -217,6 +217,78 @@ __device__ __forceinline__ void ntt_fwd_1024(uint32_t (&x)[32], const Ntt32Const
     fwd_stage_B<9>(x, fwd_tw, lane, c.Q, c.twoQ);
 }
 
+// Products of a gadget digit (y < BG) with the three twiddles of the first two
+// forward stages, which are the same for every lane: w1 = rou[1] (stage t =
+// 512), w2 = rou[2] and w3 = rou[3] (stage t = 256). The tables hold, for
+// y < BG:  t1[y] = y w1,  t23[y] = (y w2, y w3),  t123[y] = (y w2 w1, y w3 w1),
+// all canonical mod Q.
+struct DigitTables {
+    const uint32_t *t1;
+    const uint2 *t23, *t123;
+};
+
+// Forward NTT of a digit polynomial: x in layout A with values < BG -> layout
+// B, values < 19Q + BG, same result mod Q as ntt_fwd_1024. The first two
+// stages form, for r < 8, the radix-4 group (x0, x1, x2, x3) = x[r, r+8, r+16,
+// r+24]:
+//   x[r]      = x0 + w1 x2 + w2 x1 + w2 w1 x3
+//   x[r + 8]  = x0 + w1 x2 - w2 x1 - w2 w1 x3
+//   x[r + 16] = x0 - w1 x2 + w3 x1 - w3 w1 x3
+//   x[r + 24] = x0 - w1 x2 - w3 x1 + w3 w1 x3
+// with the five products read from DigitTables (three shared-memory loads
+// instead of four Shoup multiplies), each output below 3Q + BG.
+__device__ __forceinline__ void ntt_fwd_1024_digit(uint32_t (&x)[32], const Ntt32Consts &c,
+                                                   const uint2 *__restrict__ fwd_tw, uint32_t *buf,
+                                                   const DigitTables &T, int lane)
+{
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+        const uint32_t x0 = x[r], x1 = x[r + 8], x2 = x[r + 16], x3 = x[r + 24];
+        const uint32_t a = T.t1[x2];
+        const uint2 bd = T.t23[x1], ce = T.t123[x3];
+        x[r] = x0 + a + bd.x + ce.x;
+        x[r + 8] = x0 + a + (c.twoQ - bd.x - ce.x);
+        x[r + 16] = x0 + (c.twoQ - a - ce.y) + bd.y;
+        x[r + 24] = x0 + (c.twoQ - a - bd.y) + ce.y;
+    }
+    fwd_stage_A<2>(x, c);
+    fwd_stage_A<3>(x, c);
+    fwd_stage_A<4>(x, c);
+    transpose_A_to_B(x, buf, lane);
+    fwd_stage_B<5>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<6>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<7>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<8>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<9>(x, fwd_tw, lane, c.Q, c.twoQ);
+}
+
+// Inverse NTT without the final N^-1: x in layout B (values < 2Q) -> layout
+// A, canonical, equal to N * (the reference's iNTT) mod Q. Used on
+// accumulators that already carry the factor N^-1 (bootstrap keys uploaded
+// times N^-1).
+__device__ __forceinline__ void ntt_inv_1024_noscale(uint32_t (&x)[32], const Ntt32Consts &c,
+                                                     const uint2 *__restrict__ inv_tw, uint32_t *buf, int lane)
+{
+    inv_stage_B<1>(x, inv_tw, lane, c.Q, c.twoQ);
+    inv_stage_B<2>(x, inv_tw, lane, c.Q, c.twoQ);
+    inv_stage_B<4>(x, inv_tw, lane, c.Q, c.twoQ);
+    inv_stage_B<8>(x, inv_tw, lane, c.Q, c.twoQ);
+    inv_stage_B<16>(x, inv_tw, lane, c.Q, c.twoQ);
+    transpose_B_to_A(x, buf, lane);
+    inv_stage_A<1>(x, c);
+    inv_stage_A<2>(x, c);
+    inv_stage_A<4>(x, c);
+    inv_stage_A<8>(x, c);
+#pragma unroll
+    for (int r = 0; r < 16; r++) {
+        uint32_t u = x[r] + x[r + 16];
+        u = min(u, u - c.twoQ);
+        const uint32_t v = shoup32(x[r] - x[r + 16] + c.twoQ, c.iw[1], c.iws[1], c.Q);
+        x[r] = min(u, u - c.Q);
+        x[r + 16] = min(v, v - c.Q);
+    }
+}
+
 // Inverse NTT: x in layout B (values < 2Q, bit-reversed order) -> layout A,
 // canonical time-domain coefficients (times N^-1).
 __device__ __forceinline__ void ntt_inv_1024(uint32_t (&x)[32], const Ntt32Consts &c,
