@@ -135,6 +135,7 @@ def lib():
             "fheacc_kernel_times": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_float)]),
             "fheacc_set_option": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
             "fheacc_measure_imad_rate": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
+            "fheacc_measure_components": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -434,6 +435,13 @@ class Context:
         v = ctypes.c_double()
         self.check(lib().fheacc_measure_imad_rate(self._h, ctypes.byref(v)))
         return v.value
+
+    def measure_components(self):
+        """SM ns per unit of the blind-rotation step's pieces run alone:
+        dict(ntt_fwd, ntt_digit, intt, mac) (fheacc_measure_components)."""
+        v = (ctypes.c_double * 4)()
+        self.check(lib().fheacc_measure_components(self._h, v))
+        return dict(ntt_fwd=v[0], ntt_digit=v[1], intt=v[2], mac=v[3])
 
 
 # ------------------------------------------------------------------ serving

@@ -661,6 +661,14 @@ int fheacc_measure_imad_rate(fheacc_ctx *ctx, double *imad_per_s)
     return measure_imad_rate(c, imad_per_s);
 }
 
+int fheacc_measure_components(fheacc_ctx *ctx, double ns[4])
+{
+    if (!ctx || !ns) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    DeviceGuard g(c.device);
+    return measure_components(c, ns);
+}
+
 static const void *subs_key_level(Context &c, int f)
 {
     const size_t per = (size_t)c.p.digitKS_R * 2 * c.p.N;

@@ -121,44 +121,6 @@ __device__ __forceinline__ void named_barrier(int id, int threads)
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
 }
 
-// Montgomery reduction of a multiply-accumulate sum s < 2^62: s 2^-32 mod Q
-// in [0, 2Q). The sum of 2 digitG products (NTT digits < 21Q, keys < Q) is
-// below 168 Q^2, so (s + m Q) / 2^32 < 6.25 Q before the two conditional
-// subtractions.
-__device__ __forceinline__ uint32_t mont_reduce_2q(uint64_t s, uint32_t Q, uint32_t qinv_neg)
-{
-    const uint32_t m = (uint32_t)s * qinv_neg;
-    uint32_t r = (uint32_t)((s + (uint64_t)m * Q) >> 32);
-    r = min(r, r - 4 * Q);
-    return min(r, r - 2 * Q);
-}
-
-// Multiply-accumulate of one 4-element chunk u (elements 32 (u % 32) + 4 (u / 32)
-// + 0..3 of both output polys): acc[P][e] = sum over (p, h) of dbuf[p][h][e] *
-// key[h][p][P][e], Montgomery-reduced.
-template <int DG>
-__device__ __forceinline__ void mac_chunk(int u, const uint4 *__restrict__ key,
-                                          const uint32_t (*dbuf)[kN32], uint4 *acc, uint32_t Q, uint32_t qinv_neg)
-{
-    const int pa = sw_chunk(u & 31, u >> 5);
-    uint64_t sa[4] = {0, 0, 0, 0}, sb[4] = {0, 0, 0, 0};
-#pragma unroll
-    for (int qi = 0; qi < 2 * DG; qi++) {
-        const int pp = qi / DG, hh = qi % DG;
-        const uint4 dv = *reinterpret_cast<const uint4 *>(dbuf[pp * DG + hh] + pa);
-        const uint4 a4 = __ldg(key + ((hh * 2 + pp) * 2 + 0) * 256 + u);
-        const uint4 b4 = __ldg(key + ((hh * 2 + pp) * 2 + 1) * 256 + u);
-        sa[0] += (uint64_t)dv.x * a4.x; sb[0] += (uint64_t)dv.x * b4.x;
-        sa[1] += (uint64_t)dv.y * a4.y; sb[1] += (uint64_t)dv.y * b4.y;
-        sa[2] += (uint64_t)dv.z * a4.z; sb[2] += (uint64_t)dv.z * b4.z;
-        sa[3] += (uint64_t)dv.w * a4.w; sb[3] += (uint64_t)dv.w * b4.w;
-    }
-    __stcg(acc + u, make_uint4(mont_reduce_2q(sa[0], Q, qinv_neg), mont_reduce_2q(sa[1], Q, qinv_neg),
-                               mont_reduce_2q(sa[2], Q, qinv_neg), mont_reduce_2q(sa[3], Q, qinv_neg)));
-    __stcg(acc + 256 + u, make_uint4(mont_reduce_2q(sb[0], Q, qinv_neg), mont_reduce_2q(sb[1], Q, qinv_neg),
-                                     mont_reduce_2q(sb[2], Q, qinv_neg), mont_reduce_2q(sb[3], Q, qinv_neg)));
-}
-
 // Plans the next pipeline period (run by one thread). ctl: [0, 1] cursor
 // (step, ciphertext) of the last item taken by the inverse-NTT warps; [2, 3]
 // item of the digit warps; [4] slot; [5] cursor exhausted; [6] this period's

@@ -140,6 +140,7 @@ int launch_expand(Context &c, int mode, const uint64_t *d_in, uint64_t *d_out, s
 int launch_to_u32(Context &c, const uint64_t *d_in, uint32_t *d_out, size_t n, cudaStream_t st);
 // IMAD throughput probe (probe.cu)
 int measure_imad_rate(Context &c, double *imad_per_s);
+int measure_components(Context &c, double ns[4]);
 
 constexpr size_t kExtractStride = 1024 + 32;   // u32 words per extracted RLWE (N = 1024)
 constexpr size_t kExtract64 = 2048 + 8;        // u64 words per extracted RLWE (N = 2048)

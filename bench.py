@@ -303,9 +303,11 @@ def fheacc_key_bytes(P):
 
 
 def config_of(P, args):
-    return {"workload": "%d independent NAND-gate bootstraps: n=%d, N=%d, Q=%d (" + ("uint32" if P.N == 1024 else "uint64") + " words), BG=2^%d x%d, "
-                        "Br=%d x%d, Bks=%d x%d, q=%d; keys and input bits from fixed seeds" % (
-                            args.batch, P.n, P.N, P.Q, P.BG_bits, P.digitG, P.Br, P.digitR, P.Bks, P.digitKS, P.q),
+    word = "uint32" if P.N == 1024 else "uint64"
+    return {"workload": ("%d independent NAND-gate bootstraps: n=%d, N=%d, Q=%d (%s words), BG=2^%d x%d, "
+                         "Br=%d x%d, Bks=%d x%d, q=%d; keys and input bits from fixed seeds") % (
+                            args.batch, P.n, P.N, P.Q, word, P.BG_bits, P.digitG, P.Br, P.digitR, P.Bks, P.digitKS,
+                            P.q),
             "batch": args.batch, "gate": "NAND", "n": P.n, "N": P.N, "Q": P.Q,
             "l2": "flushed between timed steps (write of a 512 MiB buffer); keys (%.1f GB) exceed L2" % (
                 (fheacc_key_bytes(P)) / 1e9),
@@ -381,6 +383,7 @@ def main():
 
     # timed region: K steps, device-resident inputs
     imad = ctx.measure_imad_rate()
+    comp = ctx.measure_components() if P.N == 1024 else None
     clocks = ClockSampler(dev_id)
     clocks.start()
     step_ms, br_ms, ks_ms = [], [], []
@@ -477,6 +480,16 @@ def main():
         "peak_source": "IMAD rate measured in this run (%.1f T lane-op/s) / 4 IMAD issue slots per Shoup "
                        "modular multiply (mul.hi counts 2)" % (imad / 1e12),
     }
+    if comp:
+        # SM time of one step's pieces run alone vs the pipeline's SM time per step
+        sms = torch.cuda.get_device_properties(dev_id).multi_processor_count
+        step_sum = 2 * dG * comp["ntt_digit"] + 2 * comp["intt"] + comp["mac"]
+        step_pipe = br_s * 1e9 * sms / total_steps
+        roofline["components"] = {
+            "unit": "SM ns per unit, each piece run alone at the kernel's occupancy (fheacc_measure_components)",
+            "ntt_fwd_ns": comp["ntt_fwd"], "ntt_digit_ns": comp["ntt_digit"], "intt_ns": comp["intt"],
+            "mac_step_ns": comp["mac"], "step_sum_ns": step_sum, "step_pipeline_ns": step_pipe,
+            "overlap_frac": step_sum / step_pipe}
     roofline_hbm = {
         "bound": "hbm", "achieved": btkey_bytes / br_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
         "frac": btkey_bytes / br_s / 1e9 / hbm_peak, "traffic": traffic,

@@ -218,6 +218,12 @@ int fheacc_kernel_times(fheacc_ctx *ctx, float ms[2]);
  * operations per second) with a short dependent-chain kernel of this library;
  * the denominator of the integer roofline. */
 int fheacc_measure_imad_rate(fheacc_ctx *ctx, double *imad_per_s);
+/* SM time, in ns per unit per SM, of the pieces of one blind-rotation step run
+ * alone at the blind-rotation kernel's occupancy: ns[0] forward NTT, ns[1]
+ * digit NTT (table-driven first stages), ns[2] inverse NTT, ns[3] multiply-
+ * accumulate of one RLWE x RGSW step with keys streamed from L2. 32-bit
+ * parameter sets with the bootstrap key uploaded. */
+int fheacc_measure_components(fheacc_ctx *ctx, double ns[4]);
 
 /* ----------------------------------------------------------------- serving
  * A continuous-batching request loop over the gate bootstrap (no counterpart

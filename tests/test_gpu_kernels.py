@@ -124,3 +124,17 @@ def test_lwe_keyswitch_and_modswitch(F, ctx0, keys0, cuda_ok):
     ctx0.sync()
     assert np.array_equal(host(me)[0], o.lwe_modswitch(edge[0]))
     assert host(me)[0, 1] == keys0.P.q
+
+
+@pytest.mark.gpu
+def test_throughput_probes(F, ctx0, cuda_ok):
+    """The roofline probes run on the device and give plausible figures: an
+    IMAD rate within a factor of a few of 64 lanes per SM per clock, and NTT /
+    MAC SM times in the hundreds of ns."""
+    imad = ctx0.measure_imad_rate()
+    assert 1e12 < imad < 1e14
+    comp = ctx0.measure_components()
+    for k in ("ntt_fwd", "ntt_digit", "intt", "mac"):
+        assert 10.0 < comp[k] < 100000.0, comp
+    # the table-driven first stages make the digit transform no slower
+    assert comp["ntt_digit"] < 1.2 * comp["ntt_fwd"], comp
