@@ -29,6 +29,8 @@ FLAG_PROFILE = 2
 NOALLOC_MAX_GATES = 64
 OPT_BR_REGS_FOR_3 = 1
 OPT_BR_CTAS_PER_SM = 2
+OPT_BR_GROUP = 3
+GRAPH_CONCURRENT = 1
 
 OK = 0
 EINVAL, ENOMEM, ENODEV, EIO, ETIMEDOUT, ENOKEY, EBUSY = -22, -12, -19, -5, -110, -126, -16
@@ -65,6 +67,11 @@ class RequestDone(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [("rounds", ctypes.c_uint64), ("gates", ctypes.c_uint64), ("busy_s", ctypes.c_double),
                 ("waiting", ctypes.c_uint64), ("active", ctypes.c_uint64), ("free_slots", ctypes.c_uint64)]
+
+
+class TuneTrial(ctypes.Structure):
+    _fields_ = [("regs_for_3", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("group", ctypes.c_int32),
+                ("ms", ctypes.c_float)]
 
 
 class FheaccError(RuntimeError):
@@ -136,6 +143,14 @@ def lib():
             "fheacc_set_option": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
             "fheacc_measure_imad_rate": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
             "fheacc_measure_components": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
+            "fheacc_autotune": (ctypes.c_int, [vp, sz, ctypes.POINTER(TuneTrial), ctypes.c_int,
+                                               ctypes.POINTER(ctypes.c_int)]),
+            "fheacc_graph_create": (ctypes.c_int, [ctypes.POINTER(vp), ctypes.c_uint32]),
+            "fheacc_graph_add_bootstrap": (ctypes.c_int, [vp, vp, vp, vp, vp, sz, vp]),
+            "fheacc_graph_launch": (ctypes.c_int, [vp, vp]),
+            "fheacc_graph_batches": (sz, [vp]),
+            "fheacc_graph_last_error": (ctypes.c_char_p, [vp]),
+            "fheacc_graph_destroy": (ctypes.c_int, [vp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -442,6 +457,53 @@ class Context:
         v = (ctypes.c_double * 4)()
         self.check(lib().fheacc_measure_components(self._h, v))
         return dict(ntt_fwd=v[0], ntt_digit=v[1], intt=v[2], mac=v[3])
+
+    def autotune(self, count, max_trials=64):
+        """Times the blind rotation's launch options on a synthetic batch of
+        `count` gates and keeps the fastest (fheacc_autotune). Returns the
+        trials as dicts (regs_for_3, ctas_per_sm, group, ms)."""
+        arr = (TuneTrial * max_trials)()
+        n = ctypes.c_int()
+        self.check(lib().fheacc_autotune(self._h, count, arr, max_trials, ctypes.byref(n)))
+        return [{k: getattr(arr[i], k) for k, _ in TuneTrial._fields_} for i in range(min(n.value, max_trials))]
+
+
+class Graph:
+    """Batched bootstraps over one or more contexts replayed with one CUDA-graph
+    launch (fheacc_graph_*). add() takes device pointers (ints) that must stay
+    valid while the graph is used."""
+
+    def __init__(self, concurrent=False):
+        h = ctypes.c_void_p()
+        _check(lib().fheacc_graph_create(ctypes.byref(h), GRAPH_CONCURRENT if concurrent else 0))
+        self._h = h
+        self._ctxs = []
+
+    def _check(self, rc):
+        if rc != OK:
+            raise FheaccError(rc, (lib().fheacc_graph_last_error(self._h) or b"").decode())
+
+    def add(self, ctx, d_c1, d_c2, d_gates, count, d_out):
+        self._check(lib().fheacc_graph_add_bootstrap(self._h, ctx.handle, d_c1, d_c2, d_gates, count, d_out))
+        self._ctxs.append(ctx)
+
+    def launch(self, stream=0):
+        self._check(lib().fheacc_graph_launch(self._h, stream or None))
+
+    @property
+    def batches(self):
+        return lib().fheacc_graph_batches(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fheacc_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ------------------------------------------------------------------ serving

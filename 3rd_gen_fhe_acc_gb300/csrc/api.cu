@@ -36,24 +36,62 @@ int ensure_scratch(Context &c, Scratch &s, size_t bytes)
     return FHEACC_OK;
 }
 
+
+int bootstrap_device_with(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
+                          size_t count, uint64_t *d_out, uint32_t flags, void *accs, void *extract,
+                          cudaStream_t st)
+{
+    flags &= ~(uint32_t)FHEACC_FLAG_PROFILE;
+    if (c.wide) {
+        if (!c.d_btkey64) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
+        if (!c.d_kskey64) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
+        int rc = launch_blind_rotate64_with(c, d_c1, d_c2, d_gates, count, flags, (uint64_t *)accs, nullptr,
+                                            (uint64_t *)extract, 0, st);
+        return rc ? rc : launch_lwe_keyswitch64(c, (const uint64_t *)extract, count, true, d_out, st);
+    }
+    if (!c.d_btkey) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
+    if (!c.d_kskey) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
+    int rc = launch_blind_rotate32_with(c, d_c1, d_c2, d_gates, count, flags, (uint32_t *)accs, (uint32_t *)extract,
+                                        st);
+    return rc ? rc : launch_lwe_keyswitch32(c, (const uint32_t *)extract, count, true, d_out, st);
+}
+
+int bootstrap_device(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
+                     size_t count, uint64_t *d_out, uint32_t flags, cudaStream_t st, int max_ctas)
+{
+    if (c.wide) {
+        if (!c.d_btkey64) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
+        if (!c.d_kskey64) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
+        int rc = ensure_scratch(c, c.extract, count * kExtract64 * sizeof(uint64_t));
+        if (rc) return rc;
+        uint64_t *ext = (uint64_t *)c.extract.ptr;
+        const bool prof = (flags & FHEACC_FLAG_PROFILE) != 0;
+        if (prof) cudaEventRecord(c.prof[0], st);
+        rc = launch_blind_rotate64(c, d_c1, d_c2, d_gates, count, flags, nullptr, ext, max_ctas, st);
+        if (rc) return rc;
+        if (prof) cudaEventRecord(c.prof[1], st);
+        rc = launch_lwe_keyswitch64(c, ext, count, true, d_out, st);
+        if (prof && rc == FHEACC_OK) cudaEventRecord(c.prof[2], st);
+        return rc;
+    }
+    if (!c.d_btkey) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
+    if (!c.d_kskey) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
+    int rc = ensure_scratch(c, c.extract, count * kExtractStride * sizeof(uint32_t));
+    if (rc) return rc;
+    uint32_t *ext = (uint32_t *)c.extract.ptr;
+    const bool prof = (flags & FHEACC_FLAG_PROFILE) != 0;
+    if (prof) cudaEventRecord(c.prof[0], st);
+    rc = launch_blind_rotate32(c, d_c1, d_c2, d_gates, count, flags, nullptr, ext, max_ctas, st);
+    if (rc) return rc;
+    if (prof) cudaEventRecord(c.prof[1], st);
+    rc = launch_lwe_keyswitch32(c, ext, count, true, d_out, st);
+    if (prof && rc == FHEACC_OK) cudaEventRecord(c.prof[2], st);
+    return rc;
+}
+
 }  // namespace fheacc
 
 namespace {
-
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev)
-    {
-        cudaGetDevice(&prev);
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceGuard()
-    {
-        int cur = -1;
-        cudaGetDevice(&cur);
-        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-    }
-};
 
 // NULL selects the legacy default stream, as in the CUDA runtime API.
 cudaStream_t pick_stream(Context *, void *stream) { return (cudaStream_t)stream; }
@@ -457,39 +495,6 @@ int fheacc_upload_subs_key(fheacc_ctx *ctx, const uint64_t *subs_key, size_t wor
     return upload_u32(c, c.d_subs, stage.data(), words);
 }
 
-static int bootstrap_device(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
-                            size_t count, uint64_t *d_out, uint32_t flags, cudaStream_t st, int max_ctas)
-{
-    if (c.wide) {
-        if (!c.d_btkey64) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
-        if (!c.d_kskey64) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
-        int rc = ensure_scratch(c, c.extract, count * kExtract64 * sizeof(uint64_t));
-        if (rc) return rc;
-        uint64_t *ext = (uint64_t *)c.extract.ptr;
-        const bool prof = (flags & FHEACC_FLAG_PROFILE) != 0;
-        if (prof) cudaEventRecord(c.prof[0], st);
-        rc = launch_blind_rotate64(c, d_c1, d_c2, d_gates, count, flags, nullptr, ext, max_ctas, st);
-        if (rc) return rc;
-        if (prof) cudaEventRecord(c.prof[1], st);
-        rc = launch_lwe_keyswitch64(c, ext, count, true, d_out, st);
-        if (prof && rc == FHEACC_OK) cudaEventRecord(c.prof[2], st);
-        return rc;
-    }
-    if (!c.d_btkey) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
-    if (!c.d_kskey) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
-    int rc = ensure_scratch(c, c.extract, count * kExtractStride * sizeof(uint32_t));
-    if (rc) return rc;
-    uint32_t *ext = (uint32_t *)c.extract.ptr;
-    const bool prof = (flags & FHEACC_FLAG_PROFILE) != 0;
-    if (prof) cudaEventRecord(c.prof[0], st);
-    rc = launch_blind_rotate32(c, d_c1, d_c2, d_gates, count, flags, nullptr, ext, max_ctas, st);
-    if (rc) return rc;
-    if (prof) cudaEventRecord(c.prof[1], st);
-    rc = launch_lwe_keyswitch32(c, ext, count, true, d_out, st);
-    if (prof && rc == FHEACC_OK) cudaEventRecord(c.prof[2], st);
-    return rc;
-}
-
 int fheacc_bootstrap_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
                            size_t count, uint64_t *d_out, uint32_t flags, void *stream)
 {
@@ -632,6 +637,10 @@ int fheacc_set_option(fheacc_ctx *ctx, int option, int value)
     case FHEACC_OPT_BR_CTAS_PER_SM:
         if (value < 0 || value > 32) return c.fail(FHEACC_EINVAL, "CTAs per SM out of range");
         c.tune.br_ctas_per_sm = value;
+        return FHEACC_OK;
+    case FHEACC_OPT_BR_GROUP:
+        if (value < 0 || value > 64) return c.fail(FHEACC_EINVAL, "group size out of range");
+        c.tune.br_group = value;
         return FHEACC_OK;
     default:
         return c.fail(FHEACC_EINVAL, "unknown option");

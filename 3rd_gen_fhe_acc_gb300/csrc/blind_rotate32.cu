@@ -11,7 +11,8 @@
 // NTT_leading_stage.sv, poly_mult_RLWE.sv and accumulator.sv.
 //
 // Schedule. The grid is persistent; CTA b owns the group of ciphertexts
-// b, b + grid, b + 2 grid, ... (at most kMaxGroup per chunk). Steps are the
+// b, b + grid, b + 2 grid, ... (the launcher fits the group size to the
+// batch: the fewest chunks of at most kMaxGroup, or the tuned cap). Steps are the
 // OUTER loop: a CTA applies step s to every ciphertext of its group before
 // step s + 1, so all CTAs walk through the bootstrapping key together and the
 // 23 RGSW keys of a step (1.5 MB) are fetched from HBM about once and then
@@ -50,7 +51,7 @@
 namespace fheacc {
 namespace dev {
 
-constexpr int kMaxGroup = 12;   // ciphertexts per CTA and chunk (residue table in shared memory)
+constexpr int kMaxGroup = 24;   // ciphertexts per CTA and chunk (residue table in shared memory)
 
 struct PipeArgs {
     const uint64_t *c1, *c2;
@@ -61,6 +62,7 @@ struct PipeArgs {
     uint32_t *accs;          // scratch [count][2][1024], B-tiled, values < 2Q
     uint64_t *acc_out;       // optional: canonical NTT accumulators [count][2048]
     uint32_t *extract;       // optional: [count][kExtractStride]
+    int group;               // ciphertexts per CTA and chunk (<= kMaxGroup)
     int n;
     uint32_t q, embed, Br, digitR, bg_bits, flags;
     uint32_t qinv_neg;         // -Q^-1 mod 2^32 (keys carry 2^32 N^-1, see DevParams::key_factor)
@@ -80,11 +82,11 @@ struct PipeSmem {
 };
 
 // Bytes of dynamic shared memory before the digit tables: PipeSmem, then the
-// residue table [kMaxGroup][n * digitR], rounded up to 16.
+// residue table [group][n * digitR], rounded up to 16.
 template <int DG>
-__host__ __device__ constexpr size_t pipe_tables_offset(size_t steps)
+__host__ __device__ constexpr size_t pipe_tables_offset(int group, size_t steps)
 {
-    return sizeof(PipeSmem<DG>) + ((size_t)kMaxGroup * steps + 15) / 16 * 16;
+    return sizeof(PipeSmem<DG>) + ((size_t)group * steps + 15) / 16 * 16;
 }
 
 __device__ __forceinline__ void load_btile(uint32_t (&x)[32], const uint32_t *src, int lane)
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
     constexpr int GT = 32 * GW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PipeSmem<DG> &s = *reinterpret_cast<PipeSmem<DG> *>(smem_raw);
-    uint8_t *res = smem_raw + sizeof(PipeSmem<DG>);   // [kMaxGroup][n * digitR] residues
+    uint8_t *res = smem_raw + sizeof(PipeSmem<DG>);   // [group][n * digitR] residues
     __shared__ int ctl[8];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = A.n, S = n * (int)A.digitR;
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
 
     // digit tables (ntt_fwd_1024_digit): t1 [BG], t23 [BG], t123 [BG]
     const int BG = 1 << A.bg_bits;
-    uint32_t *t1 = reinterpret_cast<uint32_t *>(smem_raw + pipe_tables_offset<DG>(S));
+    uint32_t *t1 = reinterpret_cast<uint32_t *>(smem_raw + pipe_tables_offset<DG>(A.group, S));
     uint2 *t23 = reinterpret_cast<uint2 *>(t1 + BG), *t123 = t23 + BG;
     for (int y = threadIdx.x; y < BG; y += blockDim.x) {
         const uint64_t Q = c.Q;
@@ -196,10 +198,10 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
     const DigitTables dt{t1, t23, t123};
     __syncthreads();
 
-    for (size_t base = 0; base < A.count; base += G * kMaxGroup) {
+    for (size_t base = 0; base < A.count; base += G * (size_t)A.group) {
         const size_t first = base + blockIdx.x;
         int m = 0;
-        while (m < kMaxGroup && first + (size_t)m * G < A.count) m++;
+        while (m < A.group && first + (size_t)m * G < A.count) m++;
 
         // ---- prologue: LWE_evaluate, residues, acc_initialization (one warp per ciphertext)
         for (int k = warp; k < m; k += NW) {
@@ -333,11 +335,14 @@ static int sm_count(Context &c)
 }
 
 template <int DG, int MINB>
-static int launch_pipe_dg(Context &c, const dev::PipeArgs &A, int max_ctas, cudaStream_t st)
+static int launch_pipe_dg(Context &c, dev::PipeArgs A, int max_ctas, cudaStream_t st)
 {
     constexpr int threads = 32 * (2 * DG + 2);
     auto kern = dev::br32_pipe_kernel<DG, MINB>;
-    const size_t smem = dev::pipe_tables_offset<DG>((size_t)c.p.n * c.p.digitR) + 20 * ((size_t)1 << c.p.BG_bits);
+    const size_t steps = (size_t)c.p.n * c.p.digitR, tables = 20 * ((size_t)1 << c.p.BG_bits);
+    const int cap = c.tune.br_group > 0 ? std::min(c.tune.br_group, dev::kMaxGroup) : dev::kMaxGroup;
+    // residency with the largest group allowed; the group is then fitted to the batch
+    size_t smem = dev::pipe_tables_offset<DG>(cap, steps) + tables;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return c.cuda_fail(e, "blind rotation smem attribute");
     int per_sm = 0;
@@ -348,6 +353,10 @@ static int launch_pipe_dg(Context &c, const dev::PipeArgs &A, int max_ctas, cuda
     size_t blocks = std::min<size_t>((size_t)sm_count(c) * per_sm, (A.count + 1) / 2);
     if (max_ctas > 0) blocks = std::min<size_t>(blocks, (size_t)max_ctas);
     blocks = std::max<size_t>(blocks, 1);
+    // equal groups: the fewest chunks of at most `cap` ciphertexts per CTA
+    const size_t chunks = (A.count + blocks * cap - 1) / (blocks * cap);
+    A.group = (int)((A.count + blocks * chunks - 1) / (blocks * chunks));
+    smem = dev::pipe_tables_offset<DG>(A.group, steps) + tables;
     kern<<<(unsigned)blocks, threads, smem, st>>>(A, c.nc, c.d_fwd_tw, c.d_inv_tw, (uint32_t)((1ULL << 32) / c.p.Q));
     e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "blind rotation launch");

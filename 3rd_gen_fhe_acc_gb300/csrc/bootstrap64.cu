@@ -143,6 +143,7 @@ struct Br64Args {
     uint64_t *accs;            // scratch [count][2][2048], NTT domain, values < 2Q
     uint64_t *acc_out;         // optional canonical NTT accumulators [count][4096]
     uint64_t *extract;         // optional [count][kExtract64]
+    int group;                 // ciphertexts per CTA and chunk (<= kMaxGroup64)
     int n, DG;
     uint32_t q, embed, Br, digitR, bg_bits, flags;
     uint64_t gate_constant[8];
@@ -154,7 +155,7 @@ __global__ void __launch_bounds__(kT64) br64_kernel(const __grid_constant__ Br64
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Step64Smem &s = *reinterpret_cast<Step64Smem *>(smem_raw);
-    uint8_t *res = smem_raw + sizeof(Step64Smem);   // [kMaxGroup64][n * digitR]
+    uint8_t *res = smem_raw + sizeof(Step64Smem);   // [group][n * digitR]
     __shared__ uint32_t bvals[kMaxGroup64], b1s[kMaxGroup64], b2s[kMaxGroup64];
     const int tid = threadIdx.x;
     const int n = A.n, S = n * (int)A.digitR;
@@ -162,10 +163,10 @@ __global__ void __launch_bounds__(kT64) br64_kernel(const __grid_constant__ Br64
     const size_t rgsw_pairs = (size_t)A.DG * 4 * 2048;
     const bool compat = (A.flags & FHEACC_FLAG_FPGA_COMPAT) != 0;
     const size_t G = gridDim.x;
-    for (size_t base = 0; base < A.count; base += G * kMaxGroup64) {
+    for (size_t base = 0; base < A.count; base += G * (size_t)A.group) {
         const size_t first = base + blockIdx.x;
         int m = 0;
-        while (m < kMaxGroup64 && first + (size_t)m * G < A.count) m++;
+        while (m < A.group && first + (size_t)m * G < A.count) m++;
         // LWE_evaluate and residues
         for (int k = 0; k < m; k++) {
             const size_t gid = first + (size_t)k * G;
@@ -403,20 +404,38 @@ int launch_blind_rotate64(Context &c, const uint64_t *d_c1, const uint64_t *d_c2
     if (!c.d_btkey64) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
     int rc = ensure_scratch(c, c.accs, count * 4096 * sizeof(uint64_t));
     if (rc) return rc;
+    return launch_blind_rotate64_with(c, d_c1, d_c2, d_gates, count, flags, (uint64_t *)c.accs.ptr, d_acc_out,
+                                      d_extract, max_ctas, st);
+}
+
+int launch_blind_rotate64_with(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
+                               size_t count, uint32_t flags, uint64_t *accs, uint64_t *d_acc_out,
+                               uint64_t *d_extract, int max_ctas, cudaStream_t st)
+{
+    if (!count) return FHEACC_OK;
+    if (!c.d_btkey64) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
     dev::Br64Args A{};
     A.c1 = d_c1; A.c2 = d_c2; A.gates = d_gates; A.count = count;
-    A.btkey = c.d_btkey64; A.accs = (uint64_t *)c.accs.ptr; A.acc_out = d_acc_out; A.extract = d_extract;
+    A.btkey = c.d_btkey64; A.accs = accs; A.acc_out = d_acc_out; A.extract = d_extract;
     A.n = c.p.n; A.DG = (int)c.p.digitG; A.q = c.p.q; A.embed = c.dp.embed; A.Br = c.p.Br; A.digitR = c.p.digitR;
     A.bg_bits = c.p.BG_bits; A.flags = flags;
     for (int i = 0; i < 8; i++) A.gate_constant[i] = c.dp.gate_constant[i];
-    const size_t smem = sizeof(dev::Step64Smem) + (size_t)dev::kMaxGroup64 * c.p.n * c.p.digitR;
+    const int cap = c.tune.br_group > 0 ? std::min(c.tune.br_group, dev::kMaxGroup64) : dev::kMaxGroup64;
+    const size_t steps = (size_t)c.p.n * c.p.digitR;
+    size_t smem = sizeof(dev::Step64Smem) + (size_t)cap * steps;
     cudaError_t e = cudaFuncSetAttribute(dev::br64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return c.cuda_fail(e, "br64 smem attribute");
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::br64_kernel, dev::kT64, smem);
     if (per_sm < 1) per_sm = 1;
+    if (c.tune.br_ctas_per_sm > 0) per_sm = std::min(per_sm, c.tune.br_ctas_per_sm);
     size_t blocks = std::min<size_t>((size_t)sms_of(c) * per_sm, count);
     if (max_ctas > 0) blocks = std::min<size_t>(blocks, (size_t)max_ctas);
+    blocks = std::max<size_t>(blocks, 1);
+    // equal groups: the fewest chunks of at most `cap` ciphertexts per CTA
+    const size_t chunks = (count + blocks * cap - 1) / (blocks * cap);
+    A.group = (int)((count + blocks * chunks - 1) / (blocks * chunks));
+    smem = sizeof(dev::Step64Smem) + (size_t)A.group * steps;
     dev::br64_kernel<<<(unsigned)blocks, dev::kT64, smem, st>>>(A, c.d_tw64, c.d_itw64, c.nc64);
     e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "br64 launch");

@@ -30,6 +30,23 @@ struct DevParams {
 struct Tuning {
     int br_regs_for_3 = 0;    // compile-time register budget for 3 CTAs/SM (else 2)
     int br_ctas_per_sm = 0;   // cap on resident CTAs per SM (0: occupancy limit)
+    int br_group = 0;         // cap on ciphertexts per CTA and chunk (0: kernel maximum)
+};
+
+// Makes `dev` current for a scope and restores the caller's device.
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
 };
 
 struct Scratch {
@@ -130,6 +147,10 @@ int launch_rlwe_mult_rgsw64(Context &c, const uint64_t *d_acc, const uint64_t *d
 int launch_blind_rotate64(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
                           size_t count, uint32_t flags, uint64_t *d_acc_out, uint64_t *d_extract, int max_ctas,
                           cudaStream_t st);
+// The same with caller-supplied accumulator scratch (count * 4096 u64 words).
+int launch_blind_rotate64_with(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
+                               size_t count, uint32_t flags, uint64_t *accs, uint64_t *d_acc_out,
+                               uint64_t *d_extract, int max_ctas, cudaStream_t st);
 int launch_extract64(Context &c, const uint64_t *d_rlwe, size_t count, uint64_t *d_extract, cudaStream_t st);
 int launch_lwe_keyswitch64(Context &c, const uint64_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
                            cudaStream_t st);
@@ -144,6 +165,26 @@ int measure_components(Context &c, double ns[4]);
 
 constexpr size_t kExtractStride = 1024 + 32;   // u32 words per extracted RLWE (N = 1024)
 constexpr size_t kExtract64 = 2048 + 8;        // u64 words per extracted RLWE (N = 2048)
+
+// Device scratch of one batched bootstrap of `count` gates: blind-rotation
+// accumulators and extracted RLWEs (bytes of each).
+inline size_t bootstrap_accs_bytes(const Context &c, size_t count)
+{
+    return c.wide ? count * 4096 * sizeof(uint64_t) : count * 2048 * sizeof(uint32_t);
+}
+inline size_t bootstrap_extract_bytes(const Context &c, size_t count)
+{
+    return c.wide ? count * kExtract64 * sizeof(uint64_t) : count * kExtractStride * sizeof(uint32_t);
+}
+// Batched gate bootstrap (blind rotation, key switch, modulus switch) on `st`
+// with caller-supplied scratch of the sizes above; no allocation, no host
+// synchronisation, so it can be captured into a CUDA graph (api.cu).
+int bootstrap_device_with(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
+                          size_t count, uint64_t *d_out, uint32_t flags, void *accs, void *extract,
+                          cudaStream_t st);
+// The same with the context's own scratch (grown on demand).
+int bootstrap_device(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
+                     size_t count, uint64_t *d_out, uint32_t flags, cudaStream_t st, int max_ctas);
 
 // Word index of element e = 32 l + r of a 1024-word poly in the "B-tiled"
 // device layout used for bootstrap keys and blind-rotation accumulators.

@@ -295,6 +295,215 @@ def run_serving(F, ctx, P, lsk, rate, duration, kmax=256, seed=7, max_batch=4096
             "queue_ms_p99": float(np.percentile(queue, 99)), "gpu_busy_frac": st["busy_s"] / elapsed}
 
 
+def run_mixed(args):
+    """Uneven batching (one CUDA-graph launch per step): requests of geometric
+    size (mean 64, from a seed) until 3000 N=1024 and 700 N=2048 gates, the two
+    parameter sets as two contexts, each autotuned for its batch, both batches
+    captured into one graph."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build_product()
+    import importlib
+    F = importlib.import_module("3rd_gen_fhe_acc_gb300")
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(args.mixed_seed)
+    sets = []
+    for preset, total in ((0, args.mixed_narrow), (1, args.mixed_wide)):
+        counts = []
+        while sum(counts) < total:
+            counts.append(int(min(rng.geometric(1.0 / 64), total - sum(counts))))
+        sets.append({"preset": preset, "P": F.params_preset(preset), "counts": counts, "total": total})
+    arrival = [(si, ri) for si, st_ in enumerate(sets) for ri in range(len(st_["counts"]))]
+    rng.shuffle(arrival)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    t_setup = time.perf_counter()
+    for si, S in enumerate(sets):
+        P, B = S["P"], S["total"]
+        # the set's requests laid out in arrival order
+        order = [ri for (sj, ri) in arrival if sj == si]
+        offs, off = {}, 0
+        for ri in order:
+            offs[ri] = off
+            off += S["counts"][ri]
+        S["offsets"] = offs
+        lsk = F.LWE_secretkey(P, SEEDS["lwe_sk"])
+        rsk = F.RLWE_secretkey(P, SEEDS["rlwe_sk"])
+        x = rng.integers(0, 2, B).astype(np.uint8)
+        y = rng.integers(0, 2, B).astype(np.uint8)
+        g = rng.integers(0, 6, B).astype(np.int32)
+        c = F.LWE_encrypt(P, SEEDS["enc"] + 31 * si, lsk, np.concatenate([x, y]))
+        S.update(lsk=lsk, x=x, y=y, g=g, c1=c[:B].copy(), c2=c[B:].copy(),
+                 truth=np.array([F.gate_truth(int(a), b, d) for a, b, d in zip(g, x, y)], dtype=np.uint8))
+        S["bt"] = F.bootstrap_key(P, SEEDS["btkey"], lsk, rsk)
+        S["ks"] = F.keyswitch_key(P, SEEDS["kskey"], rsk, lsk)
+        ctx = F.Context(P, 0)
+        ctx.upload_bootstrap_key(S["bt"])
+        ctx.upload_keyswitch_key(S["ks"])
+        S["ctx"] = ctx
+        S["d1"] = torch.from_numpy(S["c1"].view(np.int64)).cuda()
+        S["d2"] = torch.from_numpy(S["c2"].view(np.int64)).cuda()
+        S["dg"] = torch.from_numpy(g).cuda()
+        S["dout"] = torch.zeros_like(S["d1"])
+    setup_s = time.perf_counter() - t_setup
+
+    # one launch per set, untuned and tuned: reference outputs and per-set times
+    def alone(S, reps=3):
+        ts = []
+        for r in range(reps):
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            S["ctx"].bootstrap_async(S["d1"].data_ptr(), S["d2"].data_ptr(), S["dg"].data_ptr(), S["total"],
+                                     S["dout"].data_ptr(), 0, stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if r:
+                ts.append(e0.elapsed_time(e1))
+        return min(ts)
+
+    for S in sets:
+        S["untuned_ms"] = alone(S)
+        S["ref_out"] = S["dout"].cpu().numpy().view(np.uint64).copy()
+        S["trials"] = S["ctx"].autotune(S["total"])
+        S["tuned_ms"] = alone(S)
+        S["tuned_same"] = np.array_equal(S["dout"].cpu().numpy().view(np.uint64), S["ref_out"])
+        best = min(S["trials"], key=lambda t: t["ms"])
+        S["best"] = {k: best[k] for k in ("regs_for_3", "ctas_per_sm", "group")}
+
+    graph = F.Graph()
+    for S in sets:
+        graph.add(S["ctx"], S["d1"].data_ptr(), S["d2"].data_ptr(), S["dg"].data_ptr(), S["total"],
+                  S["dout"].data_ptr())
+    # the same batches as concurrent branches (reported beside the serial graph)
+    cgraph = F.Graph(concurrent=True)
+    for S in sets:
+        cgraph.add(S["ctx"], S["d1"].data_ptr(), S["d2"].data_ptr(), S["dg"].data_ptr(), S["total"],
+                   S["dout"].data_ptr())
+    conc_ms = []
+    for r in range(3):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        cgraph.launch(stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if r:
+            conc_ms.append(e0.elapsed_time(e1))
+    conc_same = all(np.array_equal(S["dout"].cpu().numpy().view(np.uint64), S["ref_out"]) for S in sets)
+    cgraph.close()
+    for S in sets:
+        S["dout"].zero_()
+    for _ in range(args.warmup):
+        flush.fill_(1)
+        graph.launch(stream.cuda_stream)
+    torch.cuda.synchronize()
+    outs_ok = all(np.array_equal(S["dout"].cpu().numpy().view(np.uint64), S["ref_out"]) for S in sets)
+    clocks = ClockSampler(0)
+    clocks.start()
+    step_ms = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        graph.launch(stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    total = sum(S["total"] for S in sets)
+    value = total * args.steps / (sum(step_ms) / 1e3)
+
+    # e2e: pinned host inputs -> device, graph, outputs -> host, every step
+    pins = []
+    for S in sets:
+        pins.append([torch.from_numpy(S["c1"].view(np.int64)).pin_memory(),
+                     torch.from_numpy(S["c2"].view(np.int64)).pin_memory(),
+                     torch.from_numpy(S["g"]).pin_memory(), torch.zeros_like(S["dout"], device="cpu").pin_memory()])
+    h2d = sum(p[0].numel() * 8 + p[1].numel() * 8 + p[2].numel() * 4 for p in pins)
+    d2h = sum(p[3].numel() * 8 for p in pins)
+    e2e = []
+    for s_ in range(args.warmup + args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for S, p in zip(sets, pins):
+            S["d1"].copy_(p[0], non_blocking=True)
+            S["d2"].copy_(p[1], non_blocking=True)
+            S["dg"].copy_(p[2], non_blocking=True)
+        graph.launch(stream.cuda_stream)
+        for S, p in zip(sets, pins):
+            p[3].copy_(S["dout"], non_blocking=True)
+        torch.cuda.synchronize()
+        if s_ >= args.warmup:
+            e2e.append(time.perf_counter() - t0)
+    e2e_value = total * args.steps / sum(e2e)
+    dec_ok = {}
+    per_request_ok = True
+    for S, p in zip(sets, pins):
+        o = p[3].numpy().view(np.uint64)
+        dec = F.LWE_decrypt(S["P"], S["lsk"], o)
+        dec_ok["N=%d" % S["P"].N] = "%d/%d" % (int((dec == S["truth"]).sum()), S["total"])
+        per_request_ok &= np.array_equal(o, S["ref_out"])
+        for ri, off in S["offsets"].items():   # every request's slice
+            k = S["counts"][ri]
+            per_request_ok &= bool((dec[off:off + k] == S["truth"][off:off + k]).all())
+
+    cpu = None
+    if not args.no_cpu:
+        import __graft_entry__ as ge
+        ge._build_oracle()
+        from oracle_lib import Oracle
+        cores = cpu_cores()
+        rates, samples = [], []
+        for S in sets:
+            ora = Oracle.from_params(S["P"])
+            ns = (8 if S["P"].N == 1024 else 1) * cores
+            t0 = time.perf_counter()
+            co, failed = ora.eval_bootstrap_batch(S["c1"][:ns], S["c2"][:ns], S["g"][:ns], S["bt"], S["ks"],
+                                                  threads=cores)
+            dt = time.perf_counter() - t0
+            rates.append(ns / dt)
+            samples.append("%d N=%d gates in %.1f s (%s)" % (ns, S["P"].N, dt, "bit-exact" if np.array_equal(
+                co, S["ref_out"][:ns]) and failed == 0 else "MISMATCH"))
+        cpu_value = total / sum(S["total"] / r for S, r in zip(sets, rates))
+        cpu = {"value": cpu_value, "unit": "bootstraps/s", "cores": cores, "kind": "port",
+               "sample": "oracle eval_bootstrap (C restatement of RLWE.cpp:726-786) on %d threads: %s; mixed rate "
+                         "= harmonic combination over the batch" % (cores, "; ".join(samples))}
+    line = {
+        "metric": "gate bootstraps/sec on 1 GB300, uneven batch in one CUDA-graph launch (bit-exact)",
+        "value": value, "unit": "bootstraps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": statistics.mean(step_ms), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32+u64", "data": "synthetic",
+        "config": {"workload": "uneven batch: %d N=1024 (n=500, Q<2^27, BG=2^7 x4) + %d N=2048 (n=630, Q<2^54, "
+                               "BG=2^9 x6) gate bootstraps from %d requests of geometric size (mean 64), seed %d, "
+                               "one CUDA-graph launch" % (sets[0]["total"], sets[1]["total"],
+                                                          sum(len(S["counts"]) for S in sets), args.mixed_seed),
+                   "requests": {"N=%d" % S["P"].N: len(S["counts"]) for S in sets},
+                   "l2": "flushed between timed steps (write of a 512 MiB buffer)",
+                   "parallelism": "one graph per GPU; the two parameter sets run as concurrent branches"},
+        "e2e": {"value": e2e_value, "unit": "bootstraps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": 1e3 * statistics.mean(e2e)},
+        "per_set": {"N=%d" % S["P"].N: {"gates": S["total"], "alone_untuned_ms": S["untuned_ms"],
+                                         "alone_tuned_ms": S["tuned_ms"], "autotuned": S["best"],
+                                         "trials": len(S["trials"])} for S in sets},
+        "graph_vs_sum_of_alone": sum(S["tuned_ms"] for S in sets) / statistics.mean(step_ms),
+        "concurrent_branches": {"ms_per_step": min(conc_ms), "bitexact": bool(conc_same),
+                                "note": "the two sets as concurrent graph branches; the persistent grids then "
+                                        "share SMs unevenly"},
+        "cpu_baseline": cpu, "clocks": clk, "gpu_launches": 4 * args.steps,
+        "checks": {"decrypt_ok": dec_ok, "graph_equals_separate_launches": bool(outs_ok),
+                   "tuned_equals_untuned": all(S["tuned_same"] for S in sets),
+                   "every_request_decrypts": bool(per_request_ok), "setup_s": setup_s},
+    }
+    print(json.dumps(line))
+    for S in sets:
+        S["ctx"].close()
+    return 0
+
+
 def fheacc_key_bytes(P):
     """Device bytes of the bootstrap + key-switch keys of a parameter set."""
     if P.N == 1024:
@@ -329,6 +538,11 @@ def main():
                     help="sweep serving rates (PSI queries through the continuous-batching server) and exit")
     ap.add_argument("--serve-rate", type=float, default=20000.0, help="offered bootstraps/s of the serving sample")
     ap.add_argument("--serve-seconds", type=float, default=8.0)
+    ap.add_argument("--mixed", action="store_true",
+                    help="uneven batch of two parameter sets in one CUDA-graph launch (N=1024 + N=2048) and exit")
+    ap.add_argument("--mixed-narrow", type=int, default=3000)
+    ap.add_argument("--mixed-wide", type=int, default=700)
+    ap.add_argument("--mixed-seed", type=int, default=2024)
     ap.add_argument("--profile-case", action="store_true",
                     help="only run the small profiling case (n=64, 608 gates, 2 launches) and exit")
     args = ap.parse_args()
@@ -337,6 +551,8 @@ def main():
         return run_reference(args)
     if args.profile_case:
         return profile_case()
+    if args.mixed:
+        return run_mixed(args)
 
     import torch
     import __graft_entry__
@@ -454,8 +670,13 @@ def main():
     modmul_per_step = (2 + 2 * dG) * (N // 2) * logN + 2 * (2 * dG) * N + 2 * N
     br_s = statistics.mean(br_ms) / 1e3
     achieved_modmul = total_steps * modmul_per_step / br_s
-    peak_modmul = imad / 4.0
-    rgsw_bytes = 2 * dG * 2 * N * 4
+    # IMAD issue slots per Shoup modular multiply: 32-bit words 4 (mul.hi counts
+    # 2); 64-bit words 16 (the 128-bit quotient estimate takes three wide and one
+    # high 32-bit product, each 2 slots, and the two low 64-bit products 4 each)
+    slots = 4.0 if N == 1024 else 16.0
+    peak_modmul = imad / slots
+    word = 4 if N == 1024 else 8
+    rgsw_bytes = 2 * dG * 2 * N * word
     btkey_bytes = P.Br * P.digitR * P.n * rgsw_bytes
     traffic = None
     if os.path.exists(TRAFFIC_FILE):
@@ -477,8 +698,8 @@ def main():
         "kernel": "br32_pipe_kernel", "kernel_ms": statistics.mean(br_ms),
         "work": "%d RLWE x RGSW steps x %d modular multiplies (NTT butterflies, MAC products, N^-1 scaling)" % (
             total_steps, modmul_per_step),
-        "peak_source": "IMAD rate measured in this run (%.1f T lane-op/s) / 4 IMAD issue slots per Shoup "
-                       "modular multiply (mul.hi counts 2)" % (imad / 1e12),
+        "peak_source": "IMAD rate measured in this run (%.1f T lane-op/s) / %d IMAD issue slots per %d-bit Shoup "
+                       "modular multiply" % (imad / 1e12, slots, 32 if N == 1024 else 64),
     }
     if comp:
         # SM time of one step's pieces run alone vs the pipeline's SM time per step
@@ -516,9 +737,9 @@ def main():
                "bitexact_vs_gpu": "%d/%d" % (int((co == out0[:nsample]).all(axis=1).sum()), nsample)}
 
     serving = None
-    if D.ws == 1 and args.serve_seconds > 0:
+    if D.ws == 1 and args.serve_seconds > 0 and P.N == 1024:   # the server runs the 32-bit sets
         serving = run_serving(F, ctx, P, lsk, args.serve_rate, args.serve_seconds)
-    if args.serve:
+    if args.serve and P.N == 1024:
         sweep = [run_serving(F, ctx, P, lsk, r, 10.0) for r in (1e3, 5e3, 1e4, 2e4, 3e4, 4e4, 6e4, 1e5)]
         print(json.dumps({"serving_sweep": sweep}))
 

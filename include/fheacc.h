@@ -205,9 +205,15 @@ int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t cou
 /* Launch-shape options of the blind-rotation kernel.
  *  FHEACC_OPT_BR_REGS_FOR_3 : 1 = build for 3 resident CTAs per SM (64
  *                             registers per thread), 0 = 2 CTAs per SM
- *  FHEACC_OPT_BR_CTAS_PER_SM: cap on resident CTAs per SM, 0 = occupancy limit */
+ *  FHEACC_OPT_BR_CTAS_PER_SM: cap on resident CTAs per SM, 0 = occupancy limit
+ *  FHEACC_OPT_BR_GROUP      : cap on the ciphertexts a CTA carries through the
+ *                             bootstrap key together (its step-outer group;
+ *                             0 = the kernel's maximum, 24 for 32-bit words,
+ *                             8 for 64-bit); the launch fits equal groups to
+ *                             the batch under the cap */
 #define FHEACC_OPT_BR_REGS_FOR_3  1
 #define FHEACC_OPT_BR_CTAS_PER_SM 2
+#define FHEACC_OPT_BR_GROUP       3
 int fheacc_set_option(fheacc_ctx *ctx, int option, int value);
 
 /* Per-kernel device times (ms) of the most recent call made with
@@ -224,6 +230,45 @@ int fheacc_measure_imad_rate(fheacc_ctx *ctx, double *imad_per_s);
  * accumulate of one RLWE x RGSW step with keys streamed from L2. 32-bit
  * parameter sets with the bootstrap key uploaded. */
 int fheacc_measure_components(fheacc_ctx *ctx, double ns[4]);
+
+/* Picks the blind rotation's launch options (the three FHEACC_OPT_BR_* above)
+ * for batches of `count` gates: times every candidate on a synthetic batch of
+ * that size (uniform LWE inputs mod q, the six gates in turn) with this
+ * context's keys, and leaves the fastest set on the context. `trials` (may be
+ * NULL) receives up to max_trials of the candidates with their times and
+ * *n_trials (may be NULL) their number. Results are unchanged by the options;
+ * only the launch shape differs. The reference has no counterpart (the FPGA
+ * runtime's in-flight count is a constant, myfpga.cpp:1533). */
+typedef struct fheacc_tune_trial {
+    int regs_for_3;    /* FHEACC_OPT_BR_REGS_FOR_3 value */
+    int ctas_per_sm;   /* FHEACC_OPT_BR_CTAS_PER_SM value */
+    int group;         /* FHEACC_OPT_BR_GROUP value */
+    float ms;          /* one bootstrap of the synthetic batch, best of two */
+} fheacc_tune_trial;
+int fheacc_autotune(fheacc_ctx *ctx, size_t count, fheacc_tune_trial *trials, int max_trials, int *n_trials);
+
+/* ------------------------------------------------------------------- graphs
+ * A fixed set of batched gate bootstraps, over one or more contexts (parameter
+ * sets, e.g. an N = 1024 and an N = 2048 context) of one device, replayed with
+ * one CUDA-graph launch. Batches run in the order they were added; with
+ * FHEACC_GRAPH_CONCURRENT each context's batches form their own branch and the
+ * branches run concurrently (useful for small batches; large ones finish
+ * sooner in order, as each fills the GPU on its own). The graph is
+ * captured at the first launch after an add, owns its scratch, and reads the
+ * device buffers given to fheacc_graph_add_bootstrap at every launch (they and
+ * the contexts must outlive the graph). Outputs equal fheacc_bootstrap_async
+ * on the same inputs. No counterpart in the reference, whose runtime holds one
+ * parameter set per process (params.h). */
+typedef struct fheacc_graph fheacc_graph;
+#define FHEACC_GRAPH_CONCURRENT 1u
+int fheacc_graph_create(fheacc_graph **out, uint32_t flags);
+int fheacc_graph_add_bootstrap(fheacc_graph *g, fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2,
+                               const int32_t *d_gates, size_t count, uint64_t *d_out);
+/* Enqueues the whole graph on `stream` (NULL: the legacy default stream). */
+int fheacc_graph_launch(fheacc_graph *g, void *stream);
+size_t fheacc_graph_batches(const fheacc_graph *g);
+const char *fheacc_graph_last_error(const fheacc_graph *g);
+int fheacc_graph_destroy(fheacc_graph *g);
 
 /* ----------------------------------------------------------------- serving
  * A continuous-batching request loop over the gate bootstrap (no counterpart
