@@ -108,6 +108,10 @@ def lib():
             "fheacc_lwe_encrypt": (ctypes.c_int, [P, ctypes.c_uint64, _u64p, _u8p, sz, _u64p]),
             "fheacc_lwe_decrypt": (ctypes.c_int, [P, _u64p, _u64p, sz, _u8p]),
             "fheacc_rlwe_encrypt": (ctypes.c_int, [P, ctypes.c_uint64, _u64p, _u64p, _u64p]),
+            "fheacc_rgsw_encrypt": (ctypes.c_int, [P, ctypes.c_uint64, _u64p, _u64p, _u64p]),
+            "fheacc_cmux_async": (ctypes.c_int, [vp, vp, vp, sz, vp, ctypes.c_int, vp, sz, vp]),
+            "fheacc_rlwe_blind_rotate_async": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, vp, sz, vp]),
+            "fheacc_homo_expand": (ctypes.c_int, [vp, vp, vp, vp, vp]),
             "fheacc_rlwe_phase": (ctypes.c_int, [P, _u64p, _u64p, _u64p]),
             "fheacc_create": (ctypes.c_int, [P, ctypes.c_int, ctypes.POINTER(vp)]),
             "fheacc_destroy": (ctypes.c_int, [vp]),
@@ -260,6 +264,14 @@ def RLWE_encrypt(p, seed, rlwe_sk, msg_ntt):
     out = np.zeros(2 * p.N, dtype=np.uint64)
     msg_ntt = np.ascontiguousarray(msg_ntt, dtype=np.uint64)
     _check(lib().fheacc_rlwe_encrypt(ctypes.byref(p), seed, _p64(rlwe_sk), _p64(msg_ntt), _p64(out)))
+    return out
+
+
+def RGSW_encrypt(p, seed, rlwe_sk, msg_ntt):
+    """RGSW_ciphertext(m, z) (RLWE.cpp:561-577): [digitG][2][2][N] words."""
+    out = np.zeros(p.digitG * 4 * p.N, dtype=np.uint64)
+    msg_ntt = np.ascontiguousarray(msg_ntt, dtype=np.uint64)
+    _check(lib().fheacc_rgsw_encrypt(ctypes.byref(p), seed, _p64(rlwe_sk), _p64(msg_ntt), _p64(out)))
     return out
 
 
@@ -432,6 +444,20 @@ class Context:
     def expand_RLWE(self, d_in, d_out, stream=0):
         """application::expand_RLWE (app.cpp:26): d_out = [N][2N] RLWEs."""
         self.check(lib().fheacc_expand_rlwe(self._h, d_in, d_out, stream or None))
+
+    def CMUX(self, d_c0, d_c1, d_sel, d_out, count, in_stride=0, sel_shared=True, stream=0):
+        """RLWE::CMUX (RLWE.cpp:788) of count pairs (fheacc_cmux_async)."""
+        self.check(lib().fheacc_cmux_async(self._h, d_c0, d_c1, in_stride, d_sel, 1 if sel_shared else 0, d_out,
+                                           count, stream or None))
+
+    def blind_rotate_RLWE(self, d_in, d_rgsws, forward, d_out, count=1, stream=0):
+        """RLWE::blind_rotate (RLWE.cpp:824): log2 N CMUXes with rotations."""
+        self.check(lib().fheacc_rlwe_blind_rotate_async(self._h, d_in, d_rgsws, 1 if forward else 0, d_out, count,
+                                                        stream or None))
+
+    def homo_expand(self, d_packed, d_enc_sec, d_out, stream=0):
+        """application::homo_expand (app.cpp:78): digitG RLWEs -> N RGSWs."""
+        self.check(lib().fheacc_homo_expand(self._h, d_packed, d_enc_sec, d_out, stream or None))
 
     def sync(self, timeout_ms=0):
         self.check(lib().fheacc_sync(self._h, timeout_ms))

@@ -186,14 +186,20 @@ int build_rotations(Context &c)
     host::Tables T;
     T.build(c.p);
     const int N = c.p.N, logN = T.logN;
-    std::vector<uint64_t> rot((size_t)logN * N, 0);
+    std::vector<uint64_t> rot((size_t)logN * N, 0), fwd((size_t)logN * N, 0);
     for (int j = 0; j < logN; j++) {
         uint64_t *v = rot.data() + (size_t)j * N;
         v[N - (1 << j)] = c.p.Q - 1;
         T.ntt(v);
+        uint64_t *w = fwd.data() + (size_t)j * N;   // rotate_vector_gen(true): NTT(X^(2^j))
+        w[1 << j] = 1;
+        T.ntt(w);
     }
     cudaError_t e = cudaMalloc(&c.d_rot, rot.size() * sizeof(uint64_t));
     if (e == cudaSuccess) e = cudaMemcpy(c.d_rot, rot.data(), rot.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&c.d_rot_fwd, fwd.size() * sizeof(uint64_t));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(c.d_rot_fwd, fwd.data(), fwd.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "rotation tables");
 }
 
@@ -302,6 +308,7 @@ int fheacc_destroy(fheacc_ctx *ctx)
     cudaFree(c->d_kskey64);
     cudaFree(c->d_subs64);
     cudaFree(c->d_rot);
+    cudaFree(c->d_rot_fwd);
     cudaFree(c->d_btkey);
     cudaFree(c->d_kskey);
     cudaFree(c->d_subs);
@@ -581,8 +588,9 @@ int fheacc_rlwe_mult_rgsw(fheacc_ctx *ctx, const uint64_t *d_acc, const uint64_t
     Context &c = *reinterpret_cast<Context *>(ctx);
     DeviceGuard g(c.device);
     cudaStream_t st = pick_stream(&c, stream);
-    return mark_done(c, st, c.wide ? launch_rlwe_mult_rgsw64(c, d_acc, d_rgsw, d_out, count, st)
-                                   : launch_rlwe_mult_rgsw32(c, d_acc, d_rgsw, d_out, count, st));
+    const size_t stride = (size_t)c.p.digitG * 4 * c.p.N;
+    return mark_done(c, st, c.wide ? launch_rlwe_mult_rgsw64(c, d_acc, d_rgsw, d_out, count, stride, st)
+                                   : launch_rlwe_mult_rgsw32(c, d_acc, d_rgsw, d_out, count, stride, st));
 }
 
 int fheacc_blind_rotate_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
@@ -726,14 +734,13 @@ int fheacc_subs_keyswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t co
     return mark_done(c, st, launch_expand(c, 2, d_in, d_out, count, f, key, nullptr, st));
 }
 
-int fheacc_expand_rlwe(fheacc_ctx *ctx, const uint64_t *d_in, uint64_t *d_out, void *stream)
+}  // extern "C"
+
+namespace fheacc {
+
+int expand_device(Context &c, const uint64_t *d_in, uint64_t *d_out, cudaStream_t st)
 {
-    if (!ctx) return FHEACC_EINVAL;
-    Context &c = *reinterpret_cast<Context *>(ctx);
-    if (!d_in || !d_out) return c.fail(FHEACC_EINVAL, "null buffer");
     if (!subs_key_level(c, 0)) return c.fail(FHEACC_ENOKEY, "substitute key not uploaded");
-    DeviceGuard g(c.device);
-    cudaStream_t st = pick_stream(&c, stream);
     const int N = c.p.N, logN = c.wide ? 11 : 10;
     cudaError_t e = cudaMemcpyAsync(d_out, d_in, 2 * (size_t)N * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) return c.cuda_fail(e, "expand copy");
@@ -741,7 +748,21 @@ int fheacc_expand_rlwe(fheacc_ctx *ctx, const uint64_t *d_in, uint64_t *d_out, v
         int rc = launch_expand(c, 3, d_out, d_out, 0, f, subs_key_level(c, f), c.d_rot + (size_t)f * N, st);
         if (rc) return rc;
     }
-    return mark_done(c, st, FHEACC_OK);
+    return FHEACC_OK;
+}
+
+}  // namespace fheacc
+
+extern "C" {
+
+int fheacc_expand_rlwe(fheacc_ctx *ctx, const uint64_t *d_in, uint64_t *d_out, void *stream)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    if (!d_in || !d_out) return c.fail(FHEACC_EINVAL, "null buffer");
+    DeviceGuard g(c.device);
+    cudaStream_t st = pick_stream(&c, stream);
+    return mark_done(c, st, expand_device(c, d_in, d_out, st));
 }
 
 int fheacc_sync(fheacc_ctx *ctx, uint32_t timeout_ms)

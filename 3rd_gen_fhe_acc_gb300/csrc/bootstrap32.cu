@@ -56,6 +56,7 @@ template <int DG>
 __global__ void __launch_bounds__(256) rlwe_mult_rgsw32_kernel(const uint64_t *__restrict__ acc_in,
                                                               const uint64_t *__restrict__ rgsw,
                                                               uint64_t *__restrict__ acc_out, size_t count,
+                                                              size_t rgsw_stride,
                                                               const __grid_constant__ Ntt32Consts c,
                                                               const uint2 *__restrict__ fwd_tw,
                                                               const uint2 *__restrict__ inv_tw, uint32_t bg_bits,
@@ -71,7 +72,7 @@ __global__ void __launch_bounds__(256) rlwe_mult_rgsw32_kernel(const uint64_t *_
             s.acc[P][pad32(k)] = (uint32_t)in[e];
         }
         __syncthreads();
-        KeyU64Ref key{rgsw + ci * (size_t)DG * 4 * 1024};
+        KeyU64Ref key{rgsw + ci * rgsw_stride};
         rlwe_x_rgsw_step<DG>(s, c, fwd_tw, inv_tw, key, bg_bits, mu64, warp, lane);
         uint64_t *out = acc_out + ci * 2048;
         for (int e = threadIdx.x; e < 2048; e += blockDim.x) {
@@ -149,25 +150,25 @@ int launch_ntt32(Context &c, uint64_t *d_polys, size_t count, bool inverse, cuda
 
 template <int DG>
 static int launch_mult_rgsw_dg(Context &c, const uint64_t *d_acc, const uint64_t *d_rgsw, uint64_t *d_out,
-                               size_t count, cudaStream_t st)
+                               size_t count, size_t stride, cudaStream_t st)
 {
     const size_t smem = dev::step_smem_bytes<DG>();
     cudaFuncSetAttribute(dev::rlwe_mult_rgsw32_kernel<DG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     size_t blocks = std::min<size_t>(count, (size_t)num_sms(c) * 4);
     dev::rlwe_mult_rgsw32_kernel<DG><<<(unsigned)blocks, 256, smem, st>>>(
-        d_acc, d_rgsw, d_out, count, c.nc, c.d_fwd_tw, c.d_inv_tw, c.p.BG_bits, c.dp.mu64);
+        d_acc, d_rgsw, d_out, count, stride, c.nc, c.d_fwd_tw, c.d_inv_tw, c.p.BG_bits, c.dp.mu64);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "rlwe_mult_rgsw32 launch");
 }
 
 int launch_rlwe_mult_rgsw32(Context &c, const uint64_t *d_acc, const uint64_t *d_rgsw, uint64_t *d_out,
-                            size_t count, cudaStream_t st)
+                            size_t count, size_t stride, cudaStream_t st)
 {
     if (!count) return FHEACC_OK;
     switch (c.p.digitG) {
-    case 2: return launch_mult_rgsw_dg<2>(c, d_acc, d_rgsw, d_out, count, st);
-    case 3: return launch_mult_rgsw_dg<3>(c, d_acc, d_rgsw, d_out, count, st);
-    case 4: return launch_mult_rgsw_dg<4>(c, d_acc, d_rgsw, d_out, count, st);
+    case 2: return launch_mult_rgsw_dg<2>(c, d_acc, d_rgsw, d_out, count, stride, st);
+    case 3: return launch_mult_rgsw_dg<3>(c, d_acc, d_rgsw, d_out, count, stride, st);
+    case 4: return launch_mult_rgsw_dg<4>(c, d_acc, d_rgsw, d_out, count, stride, st);
     default: return c.fail(FHEACC_EINVAL, "digitG must be 2..4 for the 32-bit path");
     }
 }

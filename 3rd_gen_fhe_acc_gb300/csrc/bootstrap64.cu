@@ -116,7 +116,7 @@ __global__ void shoup_pairs64_kernel(const uint64_t *__restrict__ in, ulonglong2
 // RLWE_mult_RGSW of count (acc, RGSW-pairs) in reference order; acc canonical.
 __global__ void __launch_bounds__(kT64) rlwe_mult_rgsw64_kernel(const uint64_t *__restrict__ acc_in,
                                                                const ulonglong2 *__restrict__ rgsw, uint64_t *acc_out,
-                                                               size_t count, int DG, uint32_t bg_bits,
+                                                               size_t count, size_t rgsw_stride, int DG, uint32_t bg_bits,
                                                                const ulonglong2 *__restrict__ tw,
                                                                const ulonglong2 *__restrict__ itw,
                                                                const __grid_constant__ Ntt64Consts c)
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(kT64) rlwe_mult_rgsw64_kernel(const uint64_t *
     for (size_t ci = blockIdx.x; ci < count; ci += gridDim.x) {
         for (int e = threadIdx.x; e < 4096; e += kT64) s.acc[e >> 11][e & 2047] = acc_in[ci * 4096 + e];
         __syncthreads();
-        step64(s, rgsw + ci * (size_t)DG * 4 * 2048, DG, bg_bits, tw, itw, c);
+        step64(s, rgsw + ci * rgsw_stride, DG, bg_bits, tw, itw, c);
         for (int e = threadIdx.x; e < 4096; e += kT64) {
             const uint64_t v = s.acc[e >> 11][e & 2047];
             acc_out[ci * 4096 + e] = v >= c.Q ? v - c.Q : v;
@@ -378,10 +378,12 @@ int launch_ntt64(Context &c, uint64_t *d_polys, size_t count, bool inverse, cuda
 }
 
 int launch_rlwe_mult_rgsw64(Context &c, const uint64_t *d_acc, const uint64_t *d_rgsw, uint64_t *d_out,
-                            size_t count, cudaStream_t st)
+                            size_t count, size_t stride, cudaStream_t st)
 {
     if (!count) return FHEACC_OK;
-    const size_t words = count * (size_t)c.p.digitG * 4 * 2048;
+    const size_t rw = (size_t)c.p.digitG * 4 * 2048;
+    if (stride != 0 && stride != rw) return c.fail(FHEACC_EINVAL, "RGSW stride: 0 or one RGSW");
+    const size_t words = (stride ? count : 1) * rw;
     int rc = ensure_scratch(c, c.io, words * sizeof(ulonglong2));
     if (rc) return rc;
     ulonglong2 *pairs = (ulonglong2 *)c.io.ptr;
@@ -391,7 +393,7 @@ int launch_rlwe_mult_rgsw64(Context &c, const uint64_t *d_acc, const uint64_t *d
     cudaFuncSetAttribute(dev::rlwe_mult_rgsw64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     size_t blocks = std::min<size_t>(count, (size_t)sms_of(c) * 2);
     dev::rlwe_mult_rgsw64_kernel<<<(unsigned)blocks, dev::kT64, smem, st>>>(
-        d_acc, pairs, d_out, count, (int)c.p.digitG, c.p.BG_bits, c.d_tw64, c.d_itw64, c.nc64);
+        d_acc, pairs, d_out, count, stride, (int)c.p.digitG, c.p.BG_bits, c.d_tw64, c.d_itw64, c.nc64);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "rlwe_mult_rgsw64 launch");
 }

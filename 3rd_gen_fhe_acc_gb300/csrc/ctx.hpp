@@ -75,6 +75,7 @@ struct Context {
     ulonglong2 *d_btkey64 = nullptr;   // Shoup pairs, [(i*digitR + j)*Br + r][digitG][2][2][N]
     ulonglong2 *d_subs64 = nullptr;    // Shoup pairs, [logN][digitKS_R][2][N]
     uint64_t *d_rot = nullptr;         // [logN][N]: NTT(-X^(N - 2^j)), rotate_vector_gen(false)
+    uint64_t *d_rot_fwd = nullptr;     // [logN][N]: NTT(X^(2^j)), rotate_vector_gen(true)
     uint64_t *d_kskey64 = nullptr;     // [(d*digitKS + j)*N + i][ks_row]
 
     // keys, device layouts
@@ -89,6 +90,7 @@ struct Context {
     Scratch accs;                  // blind-rotation accumulators, [count][2][N] u32
     Scratch extract;               // extracted RLWEs between blind rotation and key switch
     Scratch io;                    // device staging for the host-buffer entry points
+    Scratch psi;                   // CMUX / blind-rotation / homo_expand intermediates (psi.cu)
 
     size_t device_bytes() const
     {
@@ -112,8 +114,10 @@ int ensure_scratch(Context &c, Scratch &s, size_t bytes);
 
 // launchers (bootstrap32.cu)
 int launch_ntt32(Context &c, uint64_t *d_polys, size_t count, bool inverse, cudaStream_t st);
+// RLWE_mult_RGSW of count accumulators (canonical NTT RLWEs, u64); RGSW i at
+// d_rgsw + i * rgsw_stride words (reference layout; stride 0: one shared RGSW).
 int launch_rlwe_mult_rgsw32(Context &c, const uint64_t *d_acc, const uint64_t *d_rgsw, uint64_t *d_out,
-                            size_t count, cudaStream_t st);
+                            size_t count, size_t rgsw_stride, cudaStream_t st);
 // Blind rotation; writes either NTT accumulators (d_acc_out, [count][2N] u64)
 // or the extracted time-domain RLWE for the key switch (d_extract, u32
 // [count][N + 32]: a[N] after NTT_a_transpose, then b[0]).
@@ -143,7 +147,9 @@ int launch_modswitch(Context &c, const uint64_t *d_in, size_t count, uint64_t *d
 int launch_shoup_pairs64(Context &c, const uint64_t *d_in, ulonglong2 *d_out, size_t n, cudaStream_t st);
 int launch_ntt64(Context &c, uint64_t *d_polys, size_t count, bool inverse, cudaStream_t st);
 int launch_rlwe_mult_rgsw64(Context &c, const uint64_t *d_acc, const uint64_t *d_rgsw, uint64_t *d_out,
-                            size_t count, cudaStream_t st);
+                            size_t count, size_t rgsw_stride, cudaStream_t st);
+// expand_RLWE (app.cpp:26-76) of one NTT RLWE into N (d_out: [N][2N]).
+int expand_device(Context &c, const uint64_t *d_in, uint64_t *d_out, cudaStream_t st);
 int launch_blind_rotate64(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
                           size_t count, uint32_t flags, uint64_t *d_acc_out, uint64_t *d_extract, int max_ctas,
                           cudaStream_t st);

@@ -24,7 +24,7 @@ namespace host {
 
 enum : uint64_t {
     TAG_LWE_SK = 1, TAG_RLWE_SK = 2, TAG_BTKEY = 3, TAG_LWE_KS = 4,
-    TAG_SUBS = 5, TAG_LWE_ENC = 6, TAG_RLWE_ENC = 7,
+    TAG_SUBS = 5, TAG_LWE_ENC = 6, TAG_RLWE_ENC = 7, TAG_RGSW_ENC = 8,
 };
 
 static inline uint64_t mix64(uint64_t z)
@@ -311,6 +311,31 @@ extern "C" int fheacc_rlwe_encrypt(const fheacc_params *p, uint64_t seed, const 
     Rng r(seed, TAG_RLWE_ENC, 0);
     rlwe_encrypt_zero(*p, T, r, rlwe_sk_ntt, out);
     for (int i = 0; i < p->N; i++) out[p->N + i] = addmod(out[p->N + i], msg_ntt[i] % p->Q, p->Q);
+    return FHEACC_OK;
+}
+
+extern "C" int fheacc_rgsw_encrypt(const fheacc_params *p, uint64_t seed, const uint64_t *rlwe_sk_ntt,
+                                   const uint64_t *msg_ntt, uint64_t *out)
+{
+    // RGSW_ciphertext(m, z) (RLWE.cpp:561-577): row h holds two encryptions of
+    // zero, with m * BG^h added to a (c_text[h][0]) and to b (c_text[h][1]).
+    if (!params_ok(p) || !rlwe_sk_ntt || !msg_ntt || !out) return FHEACC_EINVAL;
+    Tables T;
+    T.build(*p);
+    const int N = p->N;
+    const uint64_t Q = p->Q, BG = (1ULL << p->BG_bits) % Q;
+    std::vector<uint64_t> m(N);
+    for (int i = 0; i < N; i++) m[i] = msg_ntt[i] % Q;
+    for (uint64_t h = 0; h < p->digitG; h++) {
+        for (int row = 0; row < 2; row++) {
+            uint64_t *c = out + (h * 2 + row) * 2 * (size_t)N;
+            Rng rng(seed, TAG_RGSW_ENC, h * 2 + row);
+            rlwe_encrypt_zero(*p, T, rng, rlwe_sk_ntt, c);
+            uint64_t *dst = row == 0 ? c : c + N;
+            for (int i = 0; i < N; i++) dst[i] = addmod(dst[i], m[i], Q);
+        }
+        for (int i = 0; i < N; i++) m[i] = mulmod(m[i], BG, Q);
+    }
     return FHEACC_OK;
 }
 

@@ -114,6 +114,10 @@ int fheacc_lwe_decrypt(const fheacc_params *p, const uint64_t *lwe_sk, const uin
 /* RLWE_encrypt of an NTT-domain plaintext poly, RLWE.cpp:324-344. */
 int fheacc_rlwe_encrypt(const fheacc_params *p, uint64_t seed, const uint64_t *rlwe_sk_ntt,
                         const uint64_t *msg_ntt, uint64_t *out /* 2N */);
+/* RGSW_ciphertext(m, z) (RLWE.cpp:561-577): RGSW encryption of the NTT-domain
+ * plaintext msg_ntt, reference layout [digitG][2][2][N]. */
+int fheacc_rgsw_encrypt(const fheacc_params *p, uint64_t seed, const uint64_t *rlwe_sk_ntt,
+                        const uint64_t *msg_ntt, uint64_t *out);
 /* b - a*s in NTT domain, then inverse NTT: the noisy time-domain phase
  * (RLWE_decrypt before denoise, RLWE.cpp:346-357). */
 int fheacc_rlwe_phase(const fheacc_params *p, const uint64_t *rlwe_sk_ntt, const uint64_t *ct,
@@ -246,6 +250,29 @@ typedef struct fheacc_tune_trial {
     float ms;          /* one bootstrap of the synthetic batch, best of two */
 } fheacc_tune_trial;
 int fheacc_autotune(fheacc_ctx *ctx, size_t count, fheacc_tune_trial *trials, int max_trials, int *n_trials);
+
+/* -------------------------------------------------------------- PSI (CMUX)
+ * The RLWE-level operations of the reference's PSI application. Ciphertexts
+ * are canonical NTT-domain RLWEs [2N] (u64); RGSWs in the reference layout
+ * [digitG][2][2][N]. */
+/* CMUX (RLWE.cpp:788-793) of count pairs: out[i] = RLWE_mult_RGSW(c1[i] -
+ * c0[i], sel) + c0[i]. c0[i] / c1[i] sit at d_c0 / d_c1 + i * in_stride words
+ * (0: 2N, contiguous; 4N picks the pairs (v[2i], v[2i+1]) of one array for a
+ * tree level); out is contiguous and may alias d_c0 when in_stride is 2N. One
+ * RGSW per pair, or one for all with sel_shared = 1. */
+int fheacc_cmux_async(fheacc_ctx *ctx, const uint64_t *d_c0, const uint64_t *d_c1, size_t in_stride,
+                      const uint64_t *d_sel, int sel_shared, uint64_t *d_out, size_t count, void *stream);
+/* blind_rotate (RLWE.cpp:824-838) of count RLWEs, each rotated by the
+ * private amount that log2 N RGSWs (shared by all) encode: log2 N CMUXes with
+ * the NTT-domain rotations by X^(2^i) (forward) or X^(-2^i). (The reference's
+ * fixed count of 11, params.h num_rotate_poly, is log2 N for N = 2048.) */
+int fheacc_rlwe_blind_rotate_async(fheacc_ctx *ctx, const uint64_t *d_in, const uint64_t *d_rgsws, int forward,
+                                   uint64_t *d_out, size_t count, void *stream);
+/* homo_expand (app.cpp:78-96): digitG packed RLWEs -> N RGSWs [N][digitG][2][2][N]
+ * (row j of RGSW i = (RLWE_mult_RGSW(u, enc_sec), u), u = expand_RLWE(packed
+ * [j])[i]); needs the substitute key. */
+int fheacc_homo_expand(fheacc_ctx *ctx, const uint64_t *d_packed, const uint64_t *d_enc_sec, uint64_t *d_out,
+                       void *stream);
 
 /* ------------------------------------------------------------------- graphs
  * A fixed set of batched gate bootstraps, over one or more contexts (parameter

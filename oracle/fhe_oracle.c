@@ -183,13 +183,23 @@ int ora_params_setup(ora_params *p) /* params.cpp:149-210, fhe_wo_fpga.cpp:95-11
         ora_ntt(v, N, p->Q, p->rou);
         pow2 *= 2;
     }
+    /* rotate_vector_gen(true): NTT(X^(2^j)), params.cpp:183-194 (j < log2 N,
+       where 2^j < N; the reference's fixed count of 11 fits N = 2048) */
+    p->rot_fwd = ora_alloc((size_t)p->digitN * (size_t)N);
+    pow2 = 1;
+    for (int j = 0; j < p->digitN; j++) {
+        uint64_t *v = p->rot_fwd + (size_t)j * N;
+        v[pow2] = 1;
+        ora_ntt(v, N, p->Q, p->rou);
+        pow2 *= 2;
+    }
     return 0;
 }
 
 void ora_params_free(ora_params *p)
 {
-    free(p->rou); free(p->irou); free(p->rot_bwd);
-    p->rou = p->irou = p->rot_bwd = NULL;
+    free(p->rou); free(p->irou); free(p->rot_bwd); free(p->rot_fwd);
+    p->rou = p->irou = p->rot_bwd = p->rot_fwd = NULL;
 }
 
 /* ------------------------------------------------------------ RLWE helpers */
@@ -514,4 +524,61 @@ void ora_expand_rlwe(const ora_params *p, const uint64_t *c, const uint64_t *sub
         inner *= 2;
     }
     free(s1); free(s2); free(tmp); free(df);
+}
+
+/* ------------------------------------------------------------- PSI (CMUX) */
+
+/* RLWE_rotate_freq(c, j, forward) (RLWE.cpp:411-430): times NTT(X^(+-2^j)). */
+static void rotate_freq(const ora_params *p, const uint64_t *c, int j, int forward, uint64_t *out)
+{
+    int N = p->N;
+    const uint64_t *v = (forward ? p->rot_fwd : p->rot_bwd) + (size_t)j * N;
+    for (int i = 0; i < N; i++) {
+        out[i] = mod_u128((u128)c[i] * v[i], p->Q);
+        out[N + i] = mod_u128((u128)c[N + i] * v[i], p->Q);
+    }
+}
+
+void ora_cmux(const ora_params *p, const uint64_t *c0, const uint64_t *c1, const uint64_t *sel,
+              uint64_t *out) /* RLWE.cpp:788-793 */
+{
+    size_t rw = 2 * (size_t)p->N;
+    uint64_t *diff = ora_alloc(rw), *mult = ora_alloc(rw);
+    for (size_t x = 0; x < rw; x++) diff[x] = mod_s64((int64_t)c1[x] - (int64_t)c0[x], p->Q);  /* RLWE_subtraction */
+    ora_rlwe_mult_rgsw(p, diff, sel, mult);
+    for (size_t x = 0; x < rw; x++) out[x] = (mult[x] + c0[x]) % p->Q;                        /* RLWE_addition */
+    free(diff); free(mult);
+}
+
+void ora_rlwe_blind_rotate(const ora_params *p, const uint64_t *c, int forward, const uint64_t *rgsws,
+                           uint64_t *out) /* RLWE.cpp:824-838 */
+{
+    size_t rw = 2 * (size_t)p->N;
+    size_t gw = p->digitG * 2 * rw;   /* one RGSW: [digitG][2] RLWEs */
+    uint64_t *acc = ora_alloc(rw), *tmp = ora_alloc(rw);
+    memcpy(acc, c, rw * sizeof(uint64_t));
+    for (int i = 0; i < p->digitN; i++) {
+        rotate_freq(p, acc, i, forward, tmp);
+        ora_cmux(p, acc, tmp, rgsws + (size_t)i * gw, acc);
+    }
+    memcpy(out, acc, rw * sizeof(uint64_t));
+    free(acc); free(tmp);
+}
+
+void ora_homo_expand(const ora_params *p, const uint64_t *packed, const uint64_t *enc_sec,
+                     const uint64_t *subs_key, uint64_t *out) /* app.cpp:78-96 */
+{
+    int N = p->N;
+    size_t rw = 2 * (size_t)N, dG = p->digitG;
+    uint64_t *unpacked = ora_alloc(dG * (size_t)N * rw);
+    for (size_t j = 0; j < dG; j++) ora_expand_rlwe(p, packed + j * rw, subs_key, unpacked + j * (size_t)N * rw);
+    for (int i = 0; i < N; i++) {
+        for (size_t j = 0; j < dG; j++) {
+            const uint64_t *u = unpacked + (j * (size_t)N + (size_t)i) * rw;
+            uint64_t *row = out + ((size_t)i * dG + j) * 2 * rw;          /* RGSW i, c_text[j] */
+            ora_rlwe_mult_rgsw(p, u, enc_sec, row);                        /* c_text[j][0] */
+            memcpy(row + rw, u, rw * sizeof(uint64_t));                    /* c_text[j][1] */
+        }
+    }
+    free(unpacked);
 }

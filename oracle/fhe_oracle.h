@@ -56,6 +56,7 @@ typedef struct ora_params {
     uint64_t *irou;      /* N words, psi^-bitrev(i)                        */
     int      digitN;     /* log2 N                                         */
     uint64_t *rot_bwd;   /* [digitN][N]: NTT(-X^(N-2^j))  (params.cpp:177) */
+    uint64_t *rot_fwd;   /* [digitN][N]: NTT(X^(2^j))     (params.cpp:183) */
 } ora_params;
 
 /* Miller-Rabin with a fixed witness set (exact for 64-bit inputs); stands in
@@ -132,6 +133,20 @@ void ora_rlwe_rotate_freq_bwd(const ora_params *p, const uint64_t *c, int j, uin
 /* expand_RLWE (app.cpp:26-76): out = [N] NTT RLWEs. */
 void ora_expand_rlwe(const ora_params *p, const uint64_t *c, const uint64_t *subs_key,
                      uint64_t *out);
+
+/* CMUX (RLWE.cpp:788-793): RLWE_mult_RGSW(c1 - c0, sel) + c0; NTT RLWEs,
+   sel an RGSW [digitG][2][2][N]. */
+void ora_cmux(const ora_params *p, const uint64_t *c0, const uint64_t *c1, const uint64_t *sel,
+              uint64_t *out);
+/* blind_rotate (RLWE.cpp:824-838): log2 N CMUXes with rotations by
+   X^(+-2^i); rgsws = [log2 N] RGSWs. out may alias c. */
+void ora_rlwe_blind_rotate(const ora_params *p, const uint64_t *c, int forward, const uint64_t *rgsws,
+                           uint64_t *out);
+/* homo_expand (app.cpp:78-96): digitG packed RLWEs -> N RGSWs
+   [N][digitG][2][2][N]; row j of RGSW i = (RLWE_mult_RGSW(u, enc_sec), u),
+   u = expand_RLWE(packed[j])[i]. */
+void ora_homo_expand(const ora_params *p, const uint64_t *packed, const uint64_t *enc_sec,
+                     const uint64_t *subs_key, uint64_t *out);
 
 #ifdef __cplusplus
 }

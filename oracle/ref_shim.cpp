@@ -192,4 +192,45 @@ void ref_expand_rlwe(const uint64_t *c, const uint64_t *subs, uint64_t *out)
     for (int i = 0; i < N; i++) from_rlwe((*r)[i], out + (size_t)i * 2 * N);
 }
 
+static application::substitute_key to_subs(const uint64_t *subs)
+{
+    application::substitute_key sk;
+    sk.subs_key.resize(digitN);
+    size_t kw = (size_t)digitKS_R * 2 * N;
+    for (int l = 0; l < digitN; l++) {
+        sk.subs_key[l].RLWE_kskey.resize(digitKS_R);
+        for (uint64_t i = 0; i < digitKS_R; i++)
+            sk.subs_key[l].RLWE_kskey[i] = to_rlwe(subs + l * kw + i * 2 * (size_t)N);
+    }
+    return sk;
+}
+
+void ref_cmux(const uint64_t *c0, const uint64_t *c1, const uint64_t *sel, uint64_t *out)
+{
+    from_rlwe(RLWE::CMUX(to_rlwe(c0), to_rlwe(c1), to_rgsw(sel)), out);
+}
+
+// blind_rotate (RLWE.cpp:824-838) takes exactly num_rotate_poly RGSWs (a
+// constant 11 in params.h) and exits otherwise; returns -1 without calling it.
+int ref_blind_rotate(const uint64_t *c, int forward, const uint64_t *rgsws, int count, uint64_t *out)
+{
+    if (count != (int)num_rotate_poly) return -1;
+    std::vector<RLWE::RGSW_ciphertext> C;
+    const size_t gw = digitG * 4 * (size_t)N;
+    for (int i = 0; i < count; i++) C.push_back(to_rgsw(rgsws + i * gw));
+    from_rlwe(RLWE::blind_rotate(to_rlwe(c), forward != 0, C), out);
+    return 0;
+}
+
+void ref_homo_expand(const uint64_t *packed, const uint64_t *enc_sec, const uint64_t *subs, uint64_t *out)
+{
+    auto bits = std::make_unique<std::vector<RLWE::RLWE_ciphertext>>(digitG);
+    for (uint64_t j = 0; j < digitG; j++) (*bits)[j] = to_rlwe(packed + j * 2 * (size_t)N);
+    auto r = application::homo_expand(bits, to_rgsw(enc_sec), to_subs(subs));
+    const size_t gw = digitG * 4 * (size_t)N;
+    for (int i = 0; i < N; i++)
+        for (uint64_t h = 0; h < digitG; h++)
+            for (int g = 0; g < 2; g++) from_rlwe((*r)[i].c_text[h][g], out + i * gw + (h * 2 + g) * 2 * (size_t)N);
+}
+
 }  // extern "C"

@@ -41,6 +41,7 @@ class OraParams(ctypes.Structure):
         ("gate_constant", ctypes.c_uint64 * 6),
         ("iN", ctypes.c_uint64), ("ROU", ctypes.c_uint64),
         ("rou", _u64p), ("irou", _u64p), ("digitN", ctypes.c_int), ("rot_bwd", _u64p),
+        ("rot_fwd", _u64p),
     ]
 
 
@@ -82,6 +83,9 @@ class Oracle:
             ("ora_rlwe_substitute", None, [ctypes.POINTER(OraParams), _u64p, ctypes.c_int, _u64p]),
             ("ora_rlwe_keyswitch", None, [ctypes.POINTER(OraParams), _u64p, _u64p, _u64p]),
             ("ora_expand_rlwe", None, [ctypes.POINTER(OraParams), _u64p, _u64p, _u64p]),
+            ("ora_cmux", None, [ctypes.POINTER(OraParams), _u64p, _u64p, _u64p, _u64p]),
+            ("ora_rlwe_blind_rotate", None, [ctypes.POINTER(OraParams), _u64p, ctypes.c_int, _u64p, _u64p]),
+            ("ora_homo_expand", None, [ctypes.POINTER(OraParams), _u64p, _u64p, _u64p, _u64p]),
         ]:
             f = getattr(L, name)
             f.restype = res
@@ -207,6 +211,27 @@ class Oracle:
                                p64(np.ascontiguousarray(subs_key, dtype=np.uint64)), p64(out))
         return out.reshape(self.N, 2 * self.N)
 
+    def cmux(self, c0, c1, sel):
+        out = np.zeros(2 * self.N, dtype=np.uint64)
+        self.L.ora_cmux(ctypes.byref(self.p), *(p64(np.ascontiguousarray(x, dtype=np.uint64)) for x in (c0, c1, sel)),
+                        p64(out))
+        return out
+
+    def rlwe_blind_rotate(self, c, forward, rgsws):
+        out = np.zeros(2 * self.N, dtype=np.uint64)
+        self.L.ora_rlwe_blind_rotate(ctypes.byref(self.p), p64(np.ascontiguousarray(c, dtype=np.uint64)),
+                                     1 if forward else 0, p64(np.ascontiguousarray(rgsws, dtype=np.uint64)),
+                                     p64(out))
+        return out
+
+    def homo_expand(self, packed, enc_sec, subs_key):
+        dG = int(self.p.digitG)
+        out = np.zeros(self.N * dG * 4 * self.N, dtype=np.uint64)
+        self.L.ora_homo_expand(ctypes.byref(self.p), p64(np.ascontiguousarray(packed, dtype=np.uint64)),
+                               p64(np.ascontiguousarray(enc_sec, dtype=np.uint64)),
+                               p64(np.ascontiguousarray(subs_key, dtype=np.uint64)), p64(out))
+        return out.reshape(self.N, dG * 4 * self.N)
+
 
 class RefParams(ctypes.Structure):
     _fields_ = [
@@ -243,6 +268,9 @@ class Ref:
             ("ref_rlwe_substitute", vp, [_u64p, ctypes.c_int, _u64p]),
             ("ref_rlwe_keyswitch", vp, [_u64p, _u64p, _u64p]),
             ("ref_expand_rlwe", vp, [_u64p, _u64p, _u64p]),
+            ("ref_cmux", vp, [_u64p, _u64p, _u64p, _u64p]),
+            ("ref_blind_rotate", ctypes.c_int, [_u64p, ctypes.c_int, _u64p, ctypes.c_int, _u64p]),
+            ("ref_homo_expand", vp, [_u64p, _u64p, _u64p, _u64p]),
         ]:
             f = getattr(L, name)
             f.restype = res
@@ -323,3 +351,21 @@ class Ref:
         self.L.ref_expand_rlwe(p64(np.ascontiguousarray(c, dtype=np.uint64)),
                                p64(np.ascontiguousarray(subs, dtype=np.uint64)), p64(out))
         return out.reshape(self.N, 2 * self.N)
+
+    def cmux(self, c0, c1, sel):
+        out = np.zeros(2 * self.N, dtype=np.uint64)
+        self.L.ref_cmux(*(p64(np.ascontiguousarray(x, dtype=np.uint64)) for x in (c0, c1, sel)), p64(out))
+        return out
+
+    def blind_rotate(self, c, forward, rgsws, count):
+        out = np.zeros(2 * self.N, dtype=np.uint64)
+        rc = self.L.ref_blind_rotate(p64(np.ascontiguousarray(c, dtype=np.uint64)), 1 if forward else 0,
+                                     p64(np.ascontiguousarray(rgsws, dtype=np.uint64)), count, p64(out))
+        return out, rc
+
+    def homo_expand(self, packed, enc_sec, subs):
+        dG = int(self.p.digitG)
+        out = np.zeros(self.N * dG * 4 * self.N, dtype=np.uint64)
+        self.L.ref_homo_expand(*(p64(np.ascontiguousarray(x, dtype=np.uint64)) for x in (packed, enc_sec, subs)),
+                               p64(out))
+        return out.reshape(self.N, dG * 4 * self.N)

@@ -88,3 +88,52 @@ def test_substitute_keyswitch_expand(F, keys0):
         assert np.array_equal(o.rlwe_keyswitch(s1, subs[f * kw:(f + 1) * kw]),
                               r.rlwe_keyswitch(s1, subs[f * kw:(f + 1) * kw]))
     assert np.array_equal(o.expand_rlwe(c, subs), r.expand_rlwe(c, subs))
+
+
+def test_cmux_and_homo_expand(F, keys0, pair):
+    """CMUX (RLWE.cpp:788-793) and homo_expand (app.cpp:78-96) at N=1024 on
+    uniform words (parity of the arithmetic; decryption is checked on the GPU)."""
+    o, r = pair
+    P = keys0.P
+    rng = np.random.default_rng(6)
+    rw, gw = 2 * P.N, int(P.digitG) * 4 * P.N
+    c0, c1 = rng.integers(0, P.Q, (2, rw), dtype=np.uint64)
+    sel = rng.integers(0, P.Q, gw, dtype=np.uint64)
+    assert np.array_equal(o.cmux(c0, c1, sel), r.cmux(c0, c1, sel))
+    packed = rng.integers(0, P.Q, int(P.digitG) * rw, dtype=np.uint64)
+    enc = rng.integers(0, P.Q, gw, dtype=np.uint64)
+    assert np.array_equal(o.homo_expand(packed, enc, keys0.subs), r.homo_expand(packed, enc, keys0.subs))
+
+
+def _blind_rotate_2k(q):
+    import os
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    sys.path[:0] = [here, os.path.dirname(here)]
+    from oracle_lib import Oracle, Ref, pkg
+    F = pkg()
+    P = F.params_preset(1)
+    o = Oracle.from_params(P)
+    r = Ref(o)
+    rng = np.random.default_rng(8)
+    c = rng.integers(0, P.Q, 2 * P.N, dtype=np.uint64)
+    rg = rng.integers(0, P.Q, 11 * int(P.digitG) * 4 * P.N, dtype=np.uint64)
+    ok = []
+    for fwd in (False, True):
+        ref, rc = r.blind_rotate(c, fwd, rg, 11)
+        ok.append(rc == 0 and np.array_equal(o.rlwe_blind_rotate(c, fwd, rg), ref))
+    q.put(ok)
+
+
+def test_rlwe_blind_rotate_2k(F):
+    """blind_rotate (RLWE.cpp:824-838) at N=2048, the size its fixed count of
+    11 rotations (params.h num_rotate_poly) is written for; in a separate
+    process, as the reference keeps one parameter set in its globals."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    pr = ctx.Process(target=_blind_rotate_2k, args=(q,))
+    pr.start()
+    ok = q.get(timeout=600)
+    pr.join(timeout=60)
+    assert pr.exitcode == 0 and ok == [True, True]
