@@ -202,16 +202,17 @@ def run_reference(args):
     return 0
 
 
-def profile_case():
+def profile_case(preset=0):
     """The case the committed ncu section captures use: the bench parameter
     set with n = 64 (same per-step work), 608 random gates (one wave of the
-    persistent grid), two batched launches, outputs checked by decryption."""
+    persistent grid; 912 for the 64-bit set), two batched launches, outputs
+    checked by decryption."""
     import torch
     import __graft_entry__
     __graft_entry__.build_product()
     import importlib
     F = importlib.import_module("3rd_gen_fhe_acc_gb300")
-    P = F.params_preset(0)
+    P = F.params_preset(preset)
     P.n = 64
     F.derive(P)
     lsk = F.LWE_secretkey(P, 1)
@@ -219,7 +220,7 @@ def profile_case():
     ctx = F.Context(P, 0)
     ctx.upload_bootstrap_key(F.bootstrap_key(P, 3, lsk, rsk))
     ctx.upload_keyswitch_key(F.keyswitch_key(P, 4, rsk, lsk))
-    B = 608
+    B = 608 if P.N == 1024 else 912
     rng = np.random.default_rng(0)
     bits = rng.integers(0, 2, 2 * B).astype(np.uint8)
     c = F.LWE_encrypt(P, 9, lsk, bits)
@@ -550,7 +551,7 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     if args.profile_case:
-        return profile_case()
+        return profile_case(args.preset)
     if args.mixed:
         return run_mixed(args)
 
