@@ -484,7 +484,7 @@ def run_mixed(args):
                                                           sum(len(S["counts"]) for S in sets), args.mixed_seed),
                    "requests": {"N=%d" % S["P"].N: len(S["counts"]) for S in sets},
                    "l2": "flushed between timed steps (write of a 512 MiB buffer)",
-                   "parallelism": "one graph per GPU; the two parameter sets run as concurrent branches"},
+                   "parallelism": "one graph per GPU; the two parameter sets in order on one branch"},
         "e2e": {"value": e2e_value, "unit": "bootstraps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": 1e3 * statistics.mean(e2e)},
         "per_set": {"N=%d" % S["P"].N: {"gates": S["total"], "alone_untuned_ms": S["untuned_ms"],
@@ -696,7 +696,7 @@ def main():
     roofline = {
         "bound": "int", "achieved": achieved_modmul / 1e9, "peak": peak_modmul / 1e9, "unit": "G modmul/s",
         "frac": achieved_modmul / peak_modmul, "traffic": traffic,
-        "kernel": "br32_pipe_kernel", "kernel_ms": statistics.mean(br_ms),
+        "kernel": "br32_pipe_kernel" if N == 1024 else "br64_kernel", "kernel_ms": statistics.mean(br_ms),
         "work": "%d RLWE x RGSW steps x %d modular multiplies (NTT butterflies, MAC products, N^-1 scaling)" % (
             total_steps, modmul_per_step),
         "peak_source": "IMAD rate measured in this run (%.1f T lane-op/s) / %d IMAD issue slots per %d-bit Shoup "
