@@ -31,6 +31,8 @@ OPT_BR_REGS_FOR_3 = 1
 OPT_BR_CTAS_PER_SM = 2
 OPT_BR_GROUP = 3
 GRAPH_CONCURRENT = 1
+KIND_LWE_SK, KIND_RLWE_SK, KIND_BOOTSTRAP_KEY, KIND_LWE_KS_KEY, KIND_SUBS_KEY, KIND_LWE_CT, KIND_RLWE_CT, \
+    KIND_RGSW_CT = range(1, 9)
 
 OK = 0
 EINVAL, ENOMEM, ENODEV, EIO, ETIMEDOUT, ENOKEY, EBUSY = -22, -12, -19, -5, -110, -126, -16
@@ -109,6 +111,10 @@ def lib():
             "fheacc_lwe_decrypt": (ctypes.c_int, [P, _u64p, _u64p, sz, _u8p]),
             "fheacc_rlwe_encrypt": (ctypes.c_int, [P, ctypes.c_uint64, _u64p, _u64p, _u64p]),
             "fheacc_rgsw_encrypt": (ctypes.c_int, [P, ctypes.c_uint64, _u64p, _u64p, _u64p]),
+            "fheacc_container_save": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint32, P, _u64p, sz]),
+            "fheacc_container_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint32, P, _u64p, sz]),
+            "fheacc_container_info": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint32),
+                                                     ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(sz)]),
             "fheacc_cmux_async": (ctypes.c_int, [vp, vp, vp, sz, vp, ctypes.c_int, vp, sz, vp]),
             "fheacc_rlwe_blind_rotate_async": (ctypes.c_int, [vp, vp, vp, ctypes.c_int, vp, sz, vp]),
             "fheacc_homo_expand": (ctypes.c_int, [vp, vp, vp, vp, vp]),
@@ -272,6 +278,21 @@ def RGSW_encrypt(p, seed, rlwe_sk, msg_ntt):
     out = np.zeros(p.digitG * 4 * p.N, dtype=np.uint64)
     msg_ntt = np.ascontiguousarray(msg_ntt, dtype=np.uint64)
     _check(lib().fheacc_rgsw_encrypt(ctypes.byref(p), seed, _p64(rlwe_sk), _p64(msg_ntt), _p64(out)))
+    return out
+
+
+def save(path, kind, p, words):
+    """Writes words (uint64, any shape) to the on-disk container (fheacc_container_save)."""
+    w = np.ascontiguousarray(words, dtype=np.uint64).reshape(-1)
+    _check(lib().fheacc_container_save(os.fsencode(path), kind, ctypes.byref(p), _p64(w), w.size))
+
+
+def load(path, kind, p):
+    """Reads a container written by save() for the same kind and parameter set."""
+    k, fp, n = ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_size_t()
+    _check(lib().fheacc_container_info(os.fsencode(path), ctypes.byref(k), ctypes.byref(fp), ctypes.byref(n)))
+    out = np.zeros(n.value, dtype=np.uint64)
+    _check(lib().fheacc_container_load(os.fsencode(path), kind, ctypes.byref(p), _p64(out), out.size))
     return out
 
 

@@ -16,7 +16,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfheacc.so")
 
 CUDA_SOURCES = ["api.cu", "bootstrap32.cu", "blind_rotate32.cu", "lwe_ks.cu", "probe.cu", "noalloc.cu", "server.cu", "bootstrap64.cu", "expand.cu", "graph.cu", "psi.cu"]
-HOST_SOURCES = ["host/params.cpp", "host/keygen.cpp"]
+HOST_SOURCES = ["host/params.cpp", "host/keygen.cpp", "host/container.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

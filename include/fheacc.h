@@ -251,6 +251,26 @@ typedef struct fheacc_tune_trial {
 } fheacc_tune_trial;
 int fheacc_autotune(fheacc_ctx *ctx, size_t count, fheacc_tune_trial *trials, int max_trials, int *n_trials);
 
+/* ------------------------------------------------------------- containers
+ * One self-describing file per object (host/container.cpp): a 64-byte header
+ * (magic "FHEACC01", kind, parameter-set fingerprint, word count, FNV-1a
+ * checksum) and the words in the host layouts above. The reference keeps
+ * keys only in memory and regenerates them each run. Loads fail with
+ * FHEACC_EINVAL on another kind, parameter set or size, FHEACC_EIO on a short
+ * or corrupted file. */
+#define FHEACC_KIND_LWE_SK        1u
+#define FHEACC_KIND_RLWE_SK       2u
+#define FHEACC_KIND_BOOTSTRAP_KEY 3u
+#define FHEACC_KIND_LWE_KS_KEY    4u
+#define FHEACC_KIND_SUBS_KEY      5u
+#define FHEACC_KIND_LWE_CT        6u   /* [count][n+1] */
+#define FHEACC_KIND_RLWE_CT       7u   /* [count][2N]  */
+#define FHEACC_KIND_RGSW_CT       8u   /* [count][digitG][2][2][N] */
+int fheacc_container_save(const char *path, uint32_t kind, const fheacc_params *p, const uint64_t *words,
+                          size_t count);
+int fheacc_container_load(const char *path, uint32_t kind, const fheacc_params *p, uint64_t *words, size_t count);
+int fheacc_container_info(const char *path, uint32_t *kind, uint64_t *fingerprint, size_t *count);
+
 /* -------------------------------------------------------------- PSI (CMUX)
  * The RLWE-level operations of the reference's PSI application. Ciphertexts
  * are canonical NTT-domain RLWEs [2N] (u64); RGSWs in the reference layout

@@ -129,3 +129,29 @@ def test_wide_preset_oracle_bootstrap(F, keys1):
     out, failed = keys1.oracle.eval_bootstrap_batch(c[:2], c[2:], [F.NAND, F.XOR], keys1.btkey, keys1.kskey)
     assert failed == 0
     assert np.array_equal(keys1.decrypt(out), [0, 1])
+
+
+def test_container_roundtrip_and_checks(F, keys0, tmp_path):
+    """Keys and ciphertexts written to the on-disk container read back word for
+    word; another kind, parameter set or a flipped byte is refused."""
+    P = keys0.P
+    path = str(tmp_path / "kskey.fheacc")
+    F.save(path, F.KIND_LWE_KS_KEY, P, keys0.kskey)
+    assert np.array_equal(F.load(path, F.KIND_LWE_KS_KEY, P), keys0.kskey)
+    ct = keys0.encrypt(np.array([1, 0, 1], dtype=np.uint8))
+    cpath = str(tmp_path / "ct.fheacc")
+    F.save(cpath, F.KIND_LWE_CT, P, ct)
+    back = F.load(cpath, F.KIND_LWE_CT, P).reshape(3, P.n + 1)
+    assert np.array_equal(keys0.decrypt(back), [1, 0, 1])
+    with pytest.raises(F.FheaccError) as e:
+        F.load(cpath, F.KIND_LWE_KS_KEY, P)           # wrong kind
+    assert e.value.code == F.EINVAL
+    other = F.params_preset(2)
+    with pytest.raises(F.FheaccError):
+        F.load(cpath, F.KIND_LWE_CT, other)           # other parameter set
+    raw = bytearray(open(cpath, "rb").read())
+    raw[64 + 17] ^= 0x40
+    open(cpath, "wb").write(bytes(raw))
+    with pytest.raises(F.FheaccError) as e:
+        F.load(cpath, F.KIND_LWE_CT, P)               # corrupted payload
+    assert e.value.code == F.EIO
