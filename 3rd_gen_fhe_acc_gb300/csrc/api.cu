@@ -263,6 +263,7 @@ int fheacc_create(const fheacc_params *p, int device, fheacc_ctx **out)
         uint32_t inv = 1;   // Q^-1 mod 2^32 by Newton iteration (Q odd)
         for (int it = 0; it < 5; it++) inv *= 2u - (uint32_t)pp.Q * inv;
         d.qinv_neg = 0u - inv;
+        d.last_digit_from_acc = pp.BG_bits * pp.digitG >= 64 || (pp.Q >> (pp.BG_bits * pp.digitG)) == 0;
     }
     e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -391,14 +392,40 @@ int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t w
     // host [r][j][i] -> device [(i * digitR + j) * Br + r], one step (all r) per
     // chunk; words times 2^32 N^-1 mod Q (see DevParams::key_factor)
     const uint64_t kf = c.dp.key_factor, kfs = shoup32_companion(kf, Q);
+    // row factors of the last-digit identity (DevParams::last_digit_from_acc):
+    // cf[h] = BG^(h - digitG + 1) for h < digitG - 1, cf[digitG - 1] =
+    // BG^-(digitG - 1) N. The accumulator it multiplies is stored times N^-1
+    // (as all are), so that row must not carry the key factor's N^-1.
+    const uint64_t dG = c.p.digitG, plane = 4 * (size_t)c.p.N;   // one row h: [g][P][N]
+    std::vector<uint64_t> cf(dG, 1);
+    const uint64_t bg_inv = host::powmod(((uint64_t)1 << c.p.BG_bits) % Q, Q - 2, Q);
+    for (uint64_t h = 0; h + 1 < dG; h++) cf[h] = host::powmod(bg_inv, dG - 1 - h, Q);
+    cf[dG - 1] = host::mulmod(host::powmod(bg_inv, dG - 1, Q), (uint64_t)c.p.N % Q, Q);
+    std::vector<uint64_t> cfs(dG);   // Shoup companions: a * cf mod Q for a < Q < 2^32
+    for (uint64_t h = 0; h < dG; h++) cfs[h] = shoup32_companion(cf[h], Q);
+    auto mulc = [&](uint64_t a, uint64_t h) {
+        const uint64_t v = a * cf[h] - ((a * cfs[h]) >> 32) * Q;
+        return v >= Q ? v - Q : v;
+    };
+    const bool derive = c.dp.last_digit_from_acc != 0;
     std::vector<uint32_t> stage(Br * rw);
+    std::vector<uint64_t> row(rw);
     for (size_t i = 0; i < n; i++) {
         for (size_t j = 0; j < dR; j++) {
             for (size_t r = 0; r < Br; r++) {
                 const uint64_t *src = btkey + ((r * dR + j) * n + i) * rw;
                 uint32_t *dst = stage.data() + r * rw;
+                for (size_t x = 0; x < rw; x++) row[x] = src[x] % Q;
+                if (derive) {
+                    const uint64_t *last = row.data() + (dG - 1) * plane;
+                    for (uint64_t h = 0; h + 1 < dG; h++)
+                        for (size_t x = 0; x < plane; x++)
+                            row[h * plane + x] = host::submod(row[h * plane + x], mulc(last[x], h), Q);
+                    for (size_t x = 0; x < plane; x++)
+                        row[(dG - 1) * plane + x] = mulc(row[(dG - 1) * plane + x], dG - 1);
+                }
                 for (size_t x = 0; x < rw; x++) {
-                    const uint64_t a = src[x] % Q;
+                    const uint64_t a = row[x];
                     uint64_t v = a * kf - ((a * kfs) >> 32) * Q;   // Shoup: [0, 2Q)
                     dst[(x & ~(size_t)1023) + btile_index(x & 1023)] = (uint32_t)(v >= Q ? v - Q : v);
                 }
@@ -640,7 +667,7 @@ int fheacc_set_option(fheacc_ctx *ctx, int option, int value)
     Context &c = *reinterpret_cast<Context *>(ctx);
     switch (option) {
     case FHEACC_OPT_BR_REGS_FOR_3:
-        c.tune.br_regs_for_3 = value ? 1 : 0;
+        c.tune.br_regs_for_3 = value < 0 ? -1 : value ? 1 : 0;
         return FHEACC_OK;
     case FHEACC_OPT_BR_CTAS_PER_SM:
         if (value < 0 || value > 32) return c.fail(FHEACC_EINVAL, "CTAs per SM out of range");

@@ -32,6 +32,14 @@
 //                          -> acc (global)
 // An item whose ciphertext is still in the digit stage waits one period.
 //
+// Last digit. When Q < BG^digitG the digits recompose each canonical
+// coefficient exactly, so sum_h BG^h NTT(digit_h) equals the NTT-domain
+// accumulator. The keys are uploaded with that identity folded in
+// (DevParams::last_digit_from_acc), the warps of the last digit skip their
+// transform, and the MAC multiplies the accumulator (read from global memory
+// before it is overwritten) by the last key row: 2 of the 2*digitG digit NTTs
+// of a step are saved, with results unchanged mod Q.
+//
 // Scaling. The bootstrap key is uploaded times 2^32 N^-1 mod Q: the Montgomery
 // reduction of the sums removes the 2^32, and the N^-1 the reference's iNTT
 // applies is already in the accumulator, so the inverse transforms skip it
@@ -69,24 +77,25 @@ struct PipeArgs {
     uint32_t tv_pos, tv_neg;   // test-vector values +-(Q/8 + 1) times N^-1
     uint32_t nmul, nmuls;      // N mod Q and its Shoup companion (canonical accumulators out)
     uint32_t w21, w31;         // rou[2] rou[1], rou[3] rou[1] mod Q (digit tables)
+    uint32_t derive_last;      // last digit's NTT from the accumulator (DevParams::last_digit_from_acc)
     uint64_t gate_constant[8];
 };
 
 // Shared memory of one CTA. tslot holds lane-major copies of the inverse-NTT
 // warps' registers (layout A), dbuf the digit NTT outputs as swizzled rows
 // (layout B); both double as the per-warp transpose scratch.
-template <int DG>
+template <int NB>
 struct PipeSmem {
     uint32_t tslot[2][2][kN32];   // time-domain accumulators, one slot per pipeline stage
-    uint32_t dbuf[2 * DG][kN32];  // digit NTT outputs / transposes of the digit warps
+    uint32_t dbuf[NB][kN32];      // digit NTT outputs / transposes of the digit warps
 };
 
 // Bytes of dynamic shared memory before the digit tables: PipeSmem, then the
 // residue table [group][n * digitR], rounded up to 16.
-template <int DG>
+template <int NB>
 __host__ __device__ constexpr size_t pipe_tables_offset(int group, size_t steps)
 {
-    return sizeof(PipeSmem<DG>) + ((size_t)group * steps + 15) / 16 * 16;
+    return sizeof(PipeSmem<NB>) + ((size_t)group * steps + 15) / 16 * 16;
 }
 
 __device__ __forceinline__ void load_btile(uint32_t (&x)[32], const uint32_t *src, int lane)
@@ -166,17 +175,20 @@ __device__ __noinline__ void pipe_schedule(int *ctl, const uint8_t *res, int m, 
     ctl[4] ^= 1;
 }
 
-template <int DG, int MINB>
-__global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
+// DV = 1: the last digit's NTT comes from the accumulator (2 (digitG - 1)
+// digit warps, and all warps share the MAC); DV = 0: 2 digitG digit warps.
+template <int DG, int MINB, int DV>
+__global__ void __launch_bounds__(32 * (2 * (DG - DV) + 2), MINB)
     br32_pipe_kernel(const __grid_constant__ PipeArgs A, const __grid_constant__ Ntt32Consts c,
                      const uint2 *__restrict__ fwd_tw, const uint2 *__restrict__ inv_tw, uint32_t mu32)
 {
-    constexpr int GW = 2 * DG;   // digit warps
+    constexpr int DT = DG - DV;  // digit NTTs per poly
+    constexpr int GW = 2 * DT;   // digit warps
     constexpr int NW = GW + 2;   // plus the two inverse-NTT warps
     constexpr int GT = 32 * GW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    PipeSmem<DG> &s = *reinterpret_cast<PipeSmem<DG> *>(smem_raw);
-    uint8_t *res = smem_raw + sizeof(PipeSmem<DG>);   // [group][n * digitR] residues
+    PipeSmem<GW> &s = *reinterpret_cast<PipeSmem<GW> *>(smem_raw);
+    uint8_t *res = smem_raw + sizeof(PipeSmem<GW>);   // [group][n * digitR] residues
     __shared__ int ctl[8];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = A.n, S = n * (int)A.digitR;
@@ -187,7 +199,7 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
 
     // digit tables (ntt_fwd_1024_digit): t1 [BG], t23 [BG], t123 [BG]
     const int BG = 1 << A.bg_bits;
-    uint32_t *t1 = reinterpret_cast<uint32_t *>(smem_raw + pipe_tables_offset<DG>(A.group, S));
+    uint32_t *t1 = reinterpret_cast<uint32_t *>(smem_raw + pipe_tables_offset<GW>(A.group, S));
     uint2 *t23 = reinterpret_cast<uint2 *>(t1 + BG), *t123 = t23 + BG;
     for (int y = threadIdx.x; y < BG; y += blockDim.x) {
         const uint64_t Q = c.Q;
@@ -273,8 +285,7 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
                     store_row(ts, lane, x);
                 }
             } else if (ctl[3] >= 0) {
-                const int gk = ctl[3], gs = ctl[2];
-                const int p = warp / DG, h = warp % DG;
+                const int p = warp / DT, h = warp % DT;
                 const uint32_t shift = A.bg_bits * h, mask = (1u << A.bg_bits) - 1;
                 uint32_t x[32];
                 load_row(x, s.tslot[sh ^ 1][p], lane);
@@ -282,11 +293,30 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), MINB)
                 for (int r = 0; r < 32; r++) x[r] = (x[r] >> shift) & mask;
                 ntt_fwd_1024_digit(x, c, fwd_tw, s.dbuf[warp], dt, lane);
                 store_row(s.dbuf[warp], lane, x);
-                const uint32_t rr = res[gk * S + gs];
-                const uint4 *key = reinterpret_cast<const uint4 *>(A.btkey + ((size_t)gs * A.Br + rr) * rgsw_words);
-                uint4 *acc = reinterpret_cast<uint4 *>(A.accs + (first + (size_t)gk * G) * 2048);
-                named_barrier(1, GT);
-                for (int u = threadIdx.x; u < 256; u += GT) mac_chunk<DG>(u, key, s.dbuf, acc, c.Q, A.qinv_neg);
+                if (!DV) {
+                    // the digit warps alone multiply-accumulate, after their named barrier
+                    const int gk = ctl[3], gs = ctl[2];
+                    const uint32_t rr = res[gk * S + gs];
+                    const uint4 *key =
+                        reinterpret_cast<const uint4 *>(A.btkey + ((size_t)gs * A.Br + rr) * rgsw_words);
+                    uint4 *acc = reinterpret_cast<uint4 *>(A.accs + (first + (size_t)gk * G) * 2048);
+                    named_barrier(1, GT);
+                    for (int u = threadIdx.x; u < 256; u += GT) mac_chunk<DG>(u, key, s.dbuf, acc, c.Q, A.qinv_neg);
+                }
+            }
+            if (DV) {
+                // all warps multiply-accumulate the digit warps' item once its
+                // digit NTTs are in shared memory
+                __syncthreads();
+                if (ctl[3] >= 0) {
+                    const int gk = ctl[3], gs = ctl[2];
+                    const uint32_t rr = res[gk * S + gs];
+                    const uint4 *key =
+                        reinterpret_cast<const uint4 *>(A.btkey + ((size_t)gs * A.Br + rr) * rgsw_words);
+                    uint4 *acc = reinterpret_cast<uint4 *>(A.accs + (first + (size_t)gk * G) * 2048);
+                    for (int u = threadIdx.x; u < 256; u += 32 * NW)
+                        mac_chunk<DG, true>(u, key, s.dbuf, acc, c.Q, A.qinv_neg, acc);
+                }
             }
             __syncthreads();
             if (threadIdx.x == 0) pipe_schedule(ctl, res, m, S, compat);
@@ -334,15 +364,16 @@ static int sm_count(Context &c)
     return v > 0 ? v : 1;
 }
 
-template <int DG, int MINB>
+template <int DG, int MINB, int DV>
 static int launch_pipe_dg(Context &c, dev::PipeArgs A, int max_ctas, cudaStream_t st)
 {
-    constexpr int threads = 32 * (2 * DG + 2);
-    auto kern = dev::br32_pipe_kernel<DG, MINB>;
+    constexpr int GW = 2 * (DG - DV);
+    constexpr int threads = 32 * (GW + 2);
+    auto kern = dev::br32_pipe_kernel<DG, MINB, DV>;
     const size_t steps = (size_t)c.p.n * c.p.digitR, tables = 20 * ((size_t)1 << c.p.BG_bits);
     const int cap = c.tune.br_group > 0 ? std::min(c.tune.br_group, dev::kMaxGroup) : dev::kMaxGroup;
     // residency with the largest group allowed; the group is then fitted to the batch
-    size_t smem = dev::pipe_tables_offset<DG>(cap, steps) + tables;
+    size_t smem = dev::pipe_tables_offset<GW>(cap, steps) + tables;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return c.cuda_fail(e, "blind rotation smem attribute");
     int per_sm = 0;
@@ -356,7 +387,7 @@ static int launch_pipe_dg(Context &c, dev::PipeArgs A, int max_ctas, cudaStream_
     // equal groups: the fewest chunks of at most `cap` ciphertexts per CTA
     const size_t chunks = (A.count + blocks * cap - 1) / (blocks * cap);
     A.group = (int)((A.count + blocks * chunks - 1) / (blocks * chunks));
-    smem = dev::pipe_tables_offset<DG>(A.group, steps) + tables;
+    smem = dev::pipe_tables_offset<GW>(A.group, steps) + tables;
     kern<<<(unsigned)blocks, threads, smem, st>>>(A, c.nc, c.d_fwd_tw, c.d_inv_tw, (uint32_t)((1ULL << 32) / c.p.Q));
     e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "blind rotation launch");
@@ -376,16 +407,25 @@ static void fill_pipe_params(Context &c, dev::PipeArgs &A, uint32_t flags)
     A.nmuls = (uint32_t)(((uint64_t)A.nmul << 32) / Q);
     A.w21 = (uint32_t)((uint64_t)c.nc.fw[2] * c.nc.fw[1] % Q);
     A.w31 = (uint32_t)((uint64_t)c.nc.fw[3] * c.nc.fw[1] % Q);
+    A.derive_last = c.dp.last_digit_from_acc;
     for (int i = 0; i < 8; i++) A.gate_constant[i] = c.dp.gate_constant[i];
 }
 
 static int launch_pipe(Context &c, const dev::PipeArgs &A, int max_ctas, cudaStream_t st)
 {
-    const bool three = c.tune.br_regs_for_3 != 0;
+    const bool three = c.tune.br_regs_for_3 < 0 ? A.derive_last != 0 : c.tune.br_regs_for_3 != 0;
+    if (A.derive_last) {
+        switch (c.p.digitG) {
+        case 2: return three ? launch_pipe_dg<2, 3, 1>(c, A, max_ctas, st) : launch_pipe_dg<2, 2, 1>(c, A, max_ctas, st);
+        case 3: return three ? launch_pipe_dg<3, 3, 1>(c, A, max_ctas, st) : launch_pipe_dg<3, 2, 1>(c, A, max_ctas, st);
+        case 4: return three ? launch_pipe_dg<4, 3, 1>(c, A, max_ctas, st) : launch_pipe_dg<4, 2, 1>(c, A, max_ctas, st);
+        default: break;
+        }
+    }
     switch (c.p.digitG) {
-    case 2: return three ? launch_pipe_dg<2, 3>(c, A, max_ctas, st) : launch_pipe_dg<2, 2>(c, A, max_ctas, st);
-    case 3: return three ? launch_pipe_dg<3, 3>(c, A, max_ctas, st) : launch_pipe_dg<3, 2>(c, A, max_ctas, st);
-    case 4: return three ? launch_pipe_dg<4, 3>(c, A, max_ctas, st) : launch_pipe_dg<4, 2>(c, A, max_ctas, st);
+    case 2: return three ? launch_pipe_dg<2, 3, 0>(c, A, max_ctas, st) : launch_pipe_dg<2, 2, 0>(c, A, max_ctas, st);
+    case 3: return three ? launch_pipe_dg<3, 3, 0>(c, A, max_ctas, st) : launch_pipe_dg<3, 2, 0>(c, A, max_ctas, st);
+    case 4: return three ? launch_pipe_dg<4, 3, 0>(c, A, max_ctas, st) : launch_pipe_dg<4, 2, 0>(c, A, max_ctas, st);
     default: return c.fail(FHEACC_EINVAL, "digitG must be 2..4 for the 32-bit path");
     }
 }

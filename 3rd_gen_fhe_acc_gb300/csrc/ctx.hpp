@@ -23,12 +23,20 @@ struct DevParams {
     // mod Q, so a Montgomery reduction (qinv_neg = -Q^-1 mod 2^32) of the
     // multiply-accumulate sums both reduces them and carries the iNTT's N^-1.
     uint32_t key_factor, qinv_neg;
+    // Q < BG^digitG: the gadget digits of a canonical coefficient recompose it
+    // exactly, so the last digit's NTT follows from the NTT-domain accumulator
+    // (sum_h BG^h NTT(d_h) = acc). The 32-bit key rows are then uploaded as
+    // K'_h = K_h - BG^(h-digitG+1) K_last and K'_last = BG^-(digitG-1) K_last,
+    // and the blind rotation multiplies the accumulator by K'_last instead of
+    // transforming the last digit.
+    uint32_t last_digit_from_acc;
 };
 
 // Launch-shape choices of the blind-rotation kernel (set by fheacc_set_option
 // or picked by fheacc_autotune).
 struct Tuning {
-    int br_regs_for_3 = 0;    // compile-time register budget for 3 CTAs/SM (else 2)
+    int br_regs_for_3 = -1;   // register budget for 3 CTAs/SM (1) or 2 (0); -1: 3 when the
+                              // last-digit identity applies (8-warp CTAs), else 2
     int br_ctas_per_sm = 0;   // cap on resident CTAs per SM (0: occupancy limit)
     int br_group = 0;         // cap on ciphertexts per CTA and chunk (0: kernel maximum)
 };

@@ -37,17 +37,22 @@ __device__ __forceinline__ uint32_t mont_reduce_2q(uint64_t s, uint32_t Q, uint3
 
 // Multiply-accumulate of one 4-element chunk u (elements 32 (u % 32) + 4 (u / 32)
 // + 0..3 of both output polys): acc[P][e] = sum over (p, h) of dbuf[p][h][e] *
-// key[h][p][P][e], Montgomery-reduced.
-template <int DG>
+// key[h][p][P][e], Montgomery-reduced. With acc_nd (the item's NTT-domain
+// accumulator, B-tiled, read before it is overwritten) the last digit's term
+// uses acc_nd[p] in place of its NTT (keys uploaded for that identity).
+template <int DG, bool DERIVE = false>
 __device__ __forceinline__ void mac_chunk(int u, const uint4 *__restrict__ key,
-                                          const uint32_t (*dbuf)[kN32], uint4 *acc, uint32_t Q, uint32_t qinv_neg)
+                                          const uint32_t (*dbuf)[kN32], uint4 *acc, uint32_t Q, uint32_t qinv_neg,
+                                          const uint4 *acc_nd = nullptr)
 {
+    constexpr int DT = DERIVE ? DG - 1 : DG;   // digit NTTs per poly in dbuf: [p * DT + h]
     const int pa = sw_chunk(u & 31, u >> 5);
     uint64_t sa[4] = {0, 0, 0, 0}, sb[4] = {0, 0, 0, 0};
 #pragma unroll
     for (int qi = 0; qi < 2 * DG; qi++) {
         const int pp = qi / DG, hh = qi % DG;
-        const uint4 dv = *reinterpret_cast<const uint4 *>(dbuf[pp * DG + hh] + pa);
+        const uint4 dv = (DERIVE && hh == DG - 1) ? __ldcg(acc_nd + pp * 256 + u)
+                                                  : *reinterpret_cast<const uint4 *>(dbuf[pp * DT + hh] + pa);
         const uint4 a4 = __ldg(key + ((hh * 2 + pp) * 2 + 0) * 256 + u);
         const uint4 b4 = __ldg(key + ((hh * 2 + pp) * 2 + 1) * 256 + u);
         sa[0] += (uint64_t)dv.x * a4.x; sb[0] += (uint64_t)dv.x * b4.x;

@@ -122,5 +122,6 @@ def test_autotune_keeps_results(F, small, cuda_ok):
         ctx.set_option(F.OPT_BR_CTAS_PER_SM, t["ctas_per_sm"])
         ctx.set_option(F.OPT_BR_GROUP, t["group"])
         assert np.array_equal(direct(torch, ctx, d, 300), before)
-    for o in (F.OPT_BR_REGS_FOR_3, F.OPT_BR_CTAS_PER_SM, F.OPT_BR_GROUP):
+    ctx.set_option(F.OPT_BR_REGS_FOR_3, -1)   # back to the defaults
+    for o in (F.OPT_BR_CTAS_PER_SM, F.OPT_BR_GROUP):
         ctx.set_option(o, 0)
