@@ -30,8 +30,7 @@ struct KsArgs {
     uint64_t Q;
 };
 
-constexpr int kKsThreads = 256;
-constexpr int kKsPerThread = 4;   // up to n + 1 <= 1024 coefficients
+constexpr int kKsMaxThreads = 256;   // up to n + 1 <= 1024 coefficients (4 per thread)
 
 __device__ __forceinline__ uint64_t scale_round_dev(uint64_t x, uint64_t new_mod, uint64_t old_mod)
 {
@@ -40,14 +39,23 @@ __device__ __forceinline__ uint64_t scale_round_dev(uint64_t x, uint64_t new_mod
     return (uint64_t)(num / (2 * (unsigned __int128)old_mod));
 }
 
-__global__ void __launch_bounds__(kKsThreads) lwe_ks32_kernel(const __grid_constant__ KsArgs A)
+// One CTA per ciphertext, one thread per four words of a key row (ks_row / 4
+// threads, one 128-bit load per row). The CTA puts the ciphertext's base-Bks
+// digits in shared memory, then walks the N * digitKS rows it selects
+// (kskey[d][j][i]), kKsUnroll rows per iteration so that each thread has that
+// many independent loads in flight, with 64-bit sums.
+constexpr int kKsUnroll = 8;
+
+__global__ void __launch_bounds__(kKsMaxThreads) lwe_ks32_kernel(const __grid_constant__ KsArgs A)
 {
     extern __shared__ uint8_t digits[];   // [N][digitKS]
-    const int n = A.n, N = A.N, D = A.digitKS;
+    const int n = A.n, N = A.N, D = A.digitKS, t = threadIdx.x;
     const uint32_t Q = (uint32_t)A.Q;
+    const size_t rs4 = A.ks_row / 4;
+    const uint4 *key4 = reinterpret_cast<const uint4 *>(A.kskey);
     for (size_t ci = blockIdx.x; ci < A.count; ci += gridDim.x) {
         const uint32_t *ext = A.ext + ci * kExtractStride;
-        for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        for (int i = t; i < N; i += blockDim.x) {
             uint32_t a = ext[i];
             for (int j = 0; j < D; j++) {
                 digits[i * D + j] = (uint8_t)(a % A.Bks);
@@ -55,27 +63,40 @@ __global__ void __launch_bounds__(kKsThreads) lwe_ks32_kernel(const __grid_const
             }
         }
         __syncthreads();
-        uint64_t acc[kKsPerThread] = {0, 0, 0, 0};
-        const uint32_t *key = A.kskey;
-        for (int i = 0; i < N; i++) {
-            for (int j = 0; j < D; j++) {
-                const uint32_t d = digits[i * D + j];
-                const uint32_t *row = key + ((size_t)(d * D + j) * N + i) * A.ks_row;
+        uint64_t s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+        const int total = N * D;
+        int i = 0, j = 0;   // (coefficient, digit) of row r0 + u
+        for (int r0 = 0; r0 < total; r0 += kKsUnroll) {
+            uint4 v[kKsUnroll];
 #pragma unroll
-                for (int c = 0; c < kKsPerThread; c++) {
-                    const int k = threadIdx.x + c * kKsThreads;
-                    if (k <= n) acc[c] += __ldg(row + k);
+            for (int u = 0; u < kKsUnroll; u++) {
+                v[u] = make_uint4(0, 0, 0, 0);
+                if (r0 + u < total) {
+                    const uint32_t d = digits[r0 + u];
+                    v[u] = __ldg(key4 + ((size_t)(d * D + j) * N + i) * rs4 + t);
                 }
+                if (++j == D) {
+                    j = 0;
+                    ++i;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kKsUnroll; u++) {
+                s0 += v[u].x;
+                s1 += v[u].y;
+                s2 += v[u].z;
+                s3 += v[u].w;
             }
         }
         const uint32_t b0 = ext[N];
         const uint32_t Q8 = Q / 8 + 1;
         uint64_t *out = A.out + (A.out_idx ? (size_t)A.out_idx[ci] : ci) * (size_t)(n + 1);
+        const uint64_t sums[4] = {s0, s1, s2, s3};
 #pragma unroll
-        for (int c = 0; c < kKsPerThread; c++) {
-            const int k = threadIdx.x + c * kKsThreads;
+        for (int c = 0; c < 4; c++) {
+            const int k = 4 * t + c;
             if (k <= n) {
-                const uint64_t s = acc[c] % Q;
+                const uint64_t s = sums[c] % Q;
                 uint64_t v;
                 if (k < n) v = s ? Q - s : 0;
                 else v = ((uint64_t)(b0 + Q8) % Q + Q - s) % Q;
@@ -106,7 +127,7 @@ int launch_lwe_keyswitch32_indexed(Context &c, const uint32_t *d_extract, size_t
 {
     if (!count) return FHEACC_OK;
     if (!c.d_kskey) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
-    if (c.p.n + 1 > dev::kKsThreads * dev::kKsPerThread) return c.fail(FHEACC_EINVAL, "n too large for key switch");
+    if (c.p.n + 1 > 4 * dev::kKsMaxThreads) return c.fail(FHEACC_EINVAL, "n too large for key switch");
     dev::KsArgs A{};
     A.ext = d_extract; A.count = count; A.kskey = c.d_kskey; A.out = d_out; A.out_idx = d_out_idx;
     A.n = c.p.n; A.N = c.p.N; A.digitKS = (int)c.p.digitKS; A.Bks = c.p.Bks; A.ks_row = c.dp.ks_row;
@@ -114,8 +135,9 @@ int launch_lwe_keyswitch32_indexed(Context &c, const uint32_t *d_extract, size_t
     const size_t smem = (size_t)c.p.N * c.p.digitKS;
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
-    size_t blocks = std::min<size_t>(count, (size_t)std::max(sms, 1) * 8);
-    dev::lwe_ks32_kernel<<<(unsigned)blocks, dev::kKsThreads, smem, st>>>(A);
+    const unsigned threads = (unsigned)(c.dp.ks_row / 4);   // ks_row: multiple of 32 words, > n
+    size_t blocks = std::min<size_t>(count, (size_t)std::max(sms, 1) * 16);
+    dev::lwe_ks32_kernel<<<(unsigned)blocks, threads, smem, st>>>(A);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "lwe_ks32 launch");
 }
