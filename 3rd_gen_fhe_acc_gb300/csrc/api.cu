@@ -263,8 +263,8 @@ int fheacc_create(const fheacc_params *p, int device, fheacc_ctx **out)
         uint32_t inv = 1;   // Q^-1 mod 2^32 by Newton iteration (Q odd)
         for (int it = 0; it < 5; it++) inv *= 2u - (uint32_t)pp.Q * inv;
         d.qinv_neg = 0u - inv;
-        d.last_digit_from_acc = pp.BG_bits * pp.digitG >= 64 || (pp.Q >> (pp.BG_bits * pp.digitG)) == 0;
     }
+    d.last_digit_from_acc = pp.BG_bits * pp.digitG >= 64 || (pp.Q >> (pp.BG_bits * pp.digitG)) == 0;
     e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         g_create_error = std::string("stream creation failed: ") + cudaGetErrorString(e);
@@ -364,20 +364,38 @@ int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t w
         }
         std::vector<uint64_t> stage(Br * rw);
         uint64_t *d_stage = nullptr;
+        ulonglong2 *d_cf = nullptr;
         cudaError_t e = cudaMalloc(&d_stage, Br * rw * sizeof(uint64_t));
-        if (e != cudaSuccess) return c.cuda_fail(e, "key staging");
-        int rc = FHEACC_OK;
+        if (e == cudaSuccess) e = cudaMalloc(&d_cf, c.p.digitG * sizeof(ulonglong2));
+        if (e != cudaSuccess) {
+            cudaFree(d_stage);
+            return c.cuda_fail(e, "key staging");
+        }
+        // factors of the last-digit identity (DevParams::last_digit_from_acc):
+        // BG^(h - digitG + 1) for h < digitG - 1, BG^-(digitG - 1) for the last row
+        const uint64_t dG = c.p.digitG;
+        const uint64_t bg_inv = host::powmod(((uint64_t)1 << c.p.BG_bits) % Q, Q - 2, Q);
+        std::vector<ulonglong2> cf(dG);
+        for (uint64_t h = 0; h < dG; h++) {
+            const uint64_t f = host::powmod(bg_inv, h + 1 < dG ? dG - 1 - h : dG - 1, Q);
+            cf[h] = make_ulonglong2(f, (uint64_t)(((unsigned __int128)f << 64) / Q));
+        }
+        e = cudaMemcpy(d_cf, cf.data(), dG * sizeof(ulonglong2), cudaMemcpyHostToDevice);
+        int rc = e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "key factors");
+        const bool derive = c.dp.last_digit_from_acc != 0;
         for (size_t i = 0; i < n && !rc; i++) {
             for (size_t j = 0; j < dR && !rc; j++) {
                 for (size_t r = 0; r < Br; r++)
                     std::memcpy(stage.data() + r * rw, btkey + ((r * dR + j) * n + i) * rw, rw * sizeof(uint64_t));
                 e = cudaMemcpy(d_stage, stage.data(), Br * rw * sizeof(uint64_t), cudaMemcpyHostToDevice);
                 if (e != cudaSuccess) rc = c.cuda_fail(e, "key upload");
-                else rc = launch_shoup_pairs64(c, d_stage, c.d_btkey64 + (i * dR + j) * Br * rw, Br * rw, c.stream);
+                else if (derive) rc = launch_derive_keys64(c, d_stage, Br, d_cf, c.stream);
+                if (!rc) rc = launch_shoup_pairs64(c, d_stage, c.d_btkey64 + (i * dR + j) * Br * rw, Br * rw, c.stream);
                 if (!rc && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = c.cuda_fail(cudaGetLastError(), "key pairs");
             }
         }
         cudaFree(d_stage);
+        cudaFree(d_cf);
         return rc;
     }
     if (!c.d_btkey) {

@@ -34,9 +34,13 @@ struct Step64Smem {
 
 // One RLWE x RGSW step on s.acc (NTT domain, values < 2Q) with the key
 // `key` (Shoup pairs, [digitG][2][2][2048]).
+// With acc_nd (the step's NTT-domain accumulator in global memory, read before
+// it is overwritten) the last digit's NTT is replaced by the accumulator: the
+// keys were uploaded with K'_h = K_h - BG^(h-DG+1) K_last, K'_last =
+// BG^-(DG-1) K_last (Q < BG^DG, so sum_h BG^h NTT(digit_h) = acc).
 __device__ __forceinline__ void step64(Step64Smem &s, const ulonglong2 *__restrict__ key, int DG, uint32_t bg_bits,
                                        const ulonglong2 *__restrict__ tw, const ulonglong2 *__restrict__ itw,
-                                       const Ntt64Consts &c)
+                                       const Ntt64Consts &c, const uint64_t *acc_nd = nullptr)
 {
     const int tid = threadIdx.x, grp = tid >> 7, gtid = tid & 127;
     ntt64_inv_2048<128>(s.acc[grp], itw, c, gtid, 1 + grp);
@@ -45,7 +49,8 @@ __device__ __forceinline__ void step64(Step64Smem &s, const ulonglong2 *__restri
 #pragma unroll
     for (int i = 0; i < 8; i++) sa[i] = sb[i] = 0;
     const uint64_t mask = (1ULL << bg_bits) - 1;
-    for (int h = 0; h < DG; h++) {
+    const int DH = acc_nd ? DG - 1 : DG;   // digits transformed
+    for (int h = 0; h < DH; h++) {
         const uint32_t sh = bg_bits * h;
         for (int e = gtid; e < 2048; e += 128) s.buf[grp][e] = (s.acc[grp][e] >> sh) & mask;
         group_sync(1 + grp, 128);
@@ -63,6 +68,19 @@ __device__ __forceinline__ void step64(Step64Smem &s, const ulonglong2 *__restri
             sb[i] += shoup64(da, b0.x, b0.y, c.Q) + shoup64(db, b1.x, b1.y, c.Q);
         }
         __syncthreads();
+    }
+    if (acc_nd) {
+        const ulonglong2 *k0 = key + (size_t)((DG - 1) * 2 + 0) * 2 * 2048;
+        const ulonglong2 *k1 = key + (size_t)((DG - 1) * 2 + 1) * 2 * 2048;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int k = tid + 256 * i;
+            const uint64_t da = __ldcg(acc_nd + k), db = __ldcg(acc_nd + 2048 + k);
+            const ulonglong2 a0 = __ldg(k0 + k), b0 = __ldg(k0 + 2048 + k);
+            const ulonglong2 a1 = __ldg(k1 + k), b1 = __ldg(k1 + 2048 + k);
+            sa[i] += shoup64(da, a0.x, a0.y, c.Q) + shoup64(db, a1.x, a1.y, c.Q);
+            sb[i] += shoup64(da, b0.x, b0.y, c.Q) + shoup64(db, b1.x, b1.y, c.Q);
+        }
     }
 #pragma unroll
     for (int i = 0; i < 8; i++) {
@@ -100,6 +118,29 @@ __global__ void __launch_bounds__(kT64) ntt64_kernel(uint64_t *polys, size_t cou
             }
         }
         __syncthreads();
+    }
+}
+
+// The last-digit identity on `count` RGSWs [DG][4][N] (u64, reduced in
+// place): row h < DG-1 becomes K_h - cf[h] K_last, row DG-1 becomes
+// cf[DG-1] K_last, mod Q; (cf, cfs) Shoup pairs of the factors.
+__global__ void derive_keys64_kernel(uint64_t *__restrict__ keys, size_t count, int DG, int N,
+                                     const ulonglong2 *__restrict__ cf, uint64_t Q)
+{
+    const size_t plane = 4 * (size_t)N;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count * plane;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t g = i / plane, x = i - g * plane;
+        uint64_t *rg = keys + g * (size_t)DG * plane;
+        const uint64_t last = rg[(size_t)(DG - 1) * plane + x] % Q;
+        for (int h = 0; h + 1 < DG; h++) {
+            const uint64_t k = rg[(size_t)h * plane + x] % Q;
+            uint64_t m = shoup64(last, cf[h].x, cf[h].y, Q);
+            m = m >= Q ? m - Q : m;
+            rg[(size_t)h * plane + x] = k >= m ? k - m : k + Q - m;
+        }
+        uint64_t m = shoup64(last, cf[DG - 1].x, cf[DG - 1].y, Q);
+        rg[(size_t)(DG - 1) * plane + x] = m >= Q ? m - Q : m;
     }
 }
 
@@ -144,6 +185,7 @@ struct Br64Args {
     uint64_t *acc_out;         // optional canonical NTT accumulators [count][4096]
     uint64_t *extract;         // optional [count][kExtract64]
     int group;                 // ciphertexts per CTA and chunk (<= kMaxGroup64)
+    int derive_last;           // last digit's NTT from the accumulator (DevParams::last_digit_from_acc)
     int n, DG;
     uint32_t q, embed, Br, digitR, bg_bits, flags;
     uint64_t gate_constant[8];
@@ -227,7 +269,8 @@ __global__ void __launch_bounds__(kT64, 3) br64_kernel(const __grid_constant__ B
                 uint64_t *acc = A.accs + (first + (size_t)k * G) * 4096;
                 for (int e = tid; e < 4096; e += kT64) s.acc[e >> 11][e & 2047] = __ldcg(acc + e);
                 __syncthreads();
-                step64(s, A.btkey + ((size_t)st * A.Br + r) * rgsw_pairs, A.DG, A.bg_bits, tw, itw, c);
+                step64(s, A.btkey + ((size_t)st * A.Br + r) * rgsw_pairs, A.DG, A.bg_bits, tw, itw, c,
+                       A.derive_last ? acc : nullptr);
                 for (int e = tid; e < 4096; e += kT64) __stcg(acc + e, s.acc[e >> 11][e & 2047]);
                 __syncthreads();
             }
@@ -362,6 +405,15 @@ static int sms_of(Context &c)
     return v > 0 ? v : 1;
 }
 
+int launch_derive_keys64(Context &c, uint64_t *d_keys, size_t count, const ulonglong2 *d_cf, cudaStream_t st)
+{
+    if (!count) return FHEACC_OK;
+    dev::derive_keys64_kernel<<<(unsigned)std::min<size_t>((count * 4 * c.p.N + 255) / 256, 8192), 256, 0, st>>>(
+        d_keys, count, (int)c.p.digitG, c.p.N, d_cf, c.p.Q);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "derive keys launch");
+}
+
 int launch_shoup_pairs64(Context &c, const uint64_t *d_in, ulonglong2 *d_out, size_t n, cudaStream_t st)
 {
     if (!n) return FHEACC_OK;
@@ -424,7 +476,7 @@ int launch_blind_rotate64_with(Context &c, const uint64_t *d_c1, const uint64_t 
     A.c1 = d_c1; A.c2 = d_c2; A.gates = d_gates; A.count = count;
     A.btkey = c.d_btkey64; A.accs = accs; A.acc_out = d_acc_out; A.extract = d_extract;
     A.n = c.p.n; A.DG = (int)c.p.digitG; A.q = c.p.q; A.embed = c.dp.embed; A.Br = c.p.Br; A.digitR = c.p.digitR;
-    A.bg_bits = c.p.BG_bits; A.flags = flags;
+    A.bg_bits = c.p.BG_bits; A.flags = flags; A.derive_last = (int)c.dp.last_digit_from_acc;
     for (int i = 0; i < 8; i++) A.gate_constant[i] = c.dp.gate_constant[i];
     const int cap = c.tune.br_group > 0 ? std::min(c.tune.br_group, dev::kMaxGroup64) : dev::kMaxGroup64;
     const size_t steps = (size_t)c.p.n * c.p.digitR;

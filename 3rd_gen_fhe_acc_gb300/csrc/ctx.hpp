@@ -153,6 +153,8 @@ int launch_extract_from_ntt32(Context &c, const uint64_t *d_rlwe, size_t count, 
 int launch_modswitch(Context &c, const uint64_t *d_in, size_t count, uint64_t *d_out, cudaStream_t st);
 // 64-bit path (bootstrap64.cu)
 int launch_shoup_pairs64(Context &c, const uint64_t *d_in, ulonglong2 *d_out, size_t n, cudaStream_t st);
+// The last-digit identity applied in place to count RGSWs (d_cf: digitG Shoup pairs).
+int launch_derive_keys64(Context &c, uint64_t *d_keys, size_t count, const ulonglong2 *d_cf, cudaStream_t st);
 int launch_ntt64(Context &c, uint64_t *d_polys, size_t count, bool inverse, cudaStream_t st);
 int launch_rlwe_mult_rgsw64(Context &c, const uint64_t *d_acc, const uint64_t *d_rgsw, uint64_t *d_out,
                             size_t count, size_t rgsw_stride, cudaStream_t st);
