@@ -705,7 +705,9 @@ def main():
     if comp:
         # SM time of one step's pieces run alone vs the pipeline's SM time per step
         sms = torch.cuda.get_device_properties(dev_id).multi_processor_count
-        step_sum = 2 * dG * comp["ntt_digit"] + 2 * comp["intt"] + comp["mac"]
+        # the last digit's NTT comes from the accumulator when Q < BG^digitG
+        derive = (P.Q >> (P.BG_bits * dG)) == 0
+        step_sum = 2 * (dG - (1 if derive else 0)) * comp["ntt_digit"] + 2 * comp["intt"] + comp["mac"]
         step_pipe = br_s * 1e9 * sms / total_steps
         roofline["components"] = {
             "unit": "SM ns per unit, each piece run alone at the kernel's occupancy (fheacc_measure_components)",
