@@ -192,7 +192,7 @@ struct Br64Args {
 };
 
 // 3 CTAs per SM (80 registers): the extra resident warps hide the latency of
-// the key stream better than the spill-free 2-CTA budget (862 vs 1028 ms for
+// the key stream better than the spill-free 2-CTA register allocation (862 vs 1028 ms for
 // 2048 gates). An XOR swizzle of the shared-memory passes removed their bank
 // conflicts but cost more in index arithmetic than it saved.
 __global__ void __launch_bounds__(kT64, 3) br64_kernel(const __grid_constant__ Br64Args A,

@@ -1,7 +1,7 @@
 /*
  * fhe_oracle.c -- CPU restatement of the reference's gate-bootstrapping path.
  *
- * TEST INFRASTRUCTURE (the checker): only tests/, __graft_entry__.smoke() and
+ * TEST INFRASTRUCTURE: only tests/, __graft_entry__.smoke() and
  * bench.py's CPU baseline / reference arm load this file's library. Nothing in
  * the shipped library links it.
  *

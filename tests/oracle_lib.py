@@ -1,4 +1,4 @@
-"""ctypes access to the checker libraries: oracle/liboracle.so (the C
+"""ctypes access to the test libraries: oracle/liboracle.so (the C
 restatement of the reference path) and, where it was built, oracle/_ref/libref.so
 (the reference's own runtime). Test infrastructure only."""
 import ctypes

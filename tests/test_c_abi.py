@@ -1,6 +1,6 @@
 """The boundary from C and C++: a C99 program linked against libfheacc.so
-(tests/c_abi/abi_client.c), and the reference-side binding shown in
-INTEGRATION.md compiled against the reference runtime's own headers."""
+(tests/c_abi/abi_client.c), and the reference-side binding shown in the
+integration notes compiled against the reference runtime's own headers."""
 import os
 import re
 import subprocess
@@ -31,8 +31,9 @@ def test_c_client_links_and_runs(F, tmp_path):
 
 @pytest.mark.skipif(not os.path.isdir(REF_INC), reason="reference headers not mounted")
 def test_integration_shim_compiles_against_reference_headers(tmp_path):
-    """The GPU:: binding a maintainer adds to FHE_ACC_runtime (INTEGRATION.md)
-    compiles against the runtime's headers and include/fheacc.h."""
+    """The GPU:: binding a maintainer adds to FHE_ACC_runtime (the C++ block
+    of the integration notes) compiles against the runtime's headers and
+    include/fheacc.h."""
     text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
     code = re.search(r"```cpp\n(// FHE_ACC_runtime/src/gpu_backend.cpp.*?)```", text, re.S).group(1)
     src = tmp_path / "gpu_backend.cpp"
