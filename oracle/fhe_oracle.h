@@ -1,6 +1,6 @@
 /*
  * fhe_oracle.h -- CPU restatement of the FHEW/AP gate-bootstrapping path of
- * zhehongw/3rd_Gen_FHE_ACC (FHE_ACC_runtime), used ONLY as a test checker.
+ * zhehongw/3rd_Gen_FHE_ACC (FHE_ACC_runtime), used ONLY as test infrastructure.
  *
  * TEST INFRASTRUCTURE. Only tests/, __graft_entry__.smoke() and the
  * cpu_baseline / reference arm of bench.py may load this library. The product
