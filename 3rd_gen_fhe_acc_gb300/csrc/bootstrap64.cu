@@ -333,6 +333,7 @@ struct Ks64Args {
     uint64_t *out;
     int n, N, digitKS;
     uint32_t Bks, ks_row, q, modswitch;
+    int fold;   // rows between mod-Q folds of the 64-bit sums, a multiple of 8
     uint64_t Q;
 };
 
@@ -344,15 +345,21 @@ __device__ __forceinline__ uint64_t scale_round64(uint64_t x, uint64_t new_mod, 
 
 // LWE_keyswitch (LWE.cpp:233-253) + optional LWE_modswitch, one CTA per
 // ciphertext; 64-bit sums are folded mod Q every 256 rows (256 Q < 2^64).
-__global__ void __launch_bounds__(kT64) lwe_ks64_kernel(const __grid_constant__ Ks64Args A)
+// One CTA per ciphertext, one thread per two words of a key row (ks_row / 2
+// threads, one 128-bit load per row), eight rows in flight per iteration;
+// the 64-bit sums are folded mod Q every A.fold rows (fold * Q < 2^64).
+constexpr int kKs64Unroll = 8;
+
+__global__ void __launch_bounds__(512) lwe_ks64_kernel(const __grid_constant__ Ks64Args A)
 {
     extern __shared__ uint8_t digits[];   // [N][digitKS]
-    const int n = A.n, N = A.N, D = A.digitKS;
+    const int n = A.n, N = A.N, D = A.digitKS, t = threadIdx.x;
     const uint64_t Q = A.Q;
-    constexpr int PT = 4;   // coefficients per thread, n + 1 <= 1024
+    const size_t rs2 = A.ks_row / 2;
+    const ulonglong2 *key2 = reinterpret_cast<const ulonglong2 *>(A.kskey);
     for (size_t ci = blockIdx.x; ci < A.count; ci += gridDim.x) {
         const uint64_t *ext = A.ext + ci * kExtract64;
-        for (int i = threadIdx.x; i < N; i += kT64) {
+        for (int i = t; i < N; i += blockDim.x) {
             uint64_t a = ext[i];
             for (int j = 0; j < D; j++) {
                 digits[i * D + j] = (uint8_t)(a % A.Bks);
@@ -360,32 +367,44 @@ __global__ void __launch_bounds__(kT64) lwe_ks64_kernel(const __grid_constant__ 
             }
         }
         __syncthreads();
-        uint64_t acc[PT] = {0, 0, 0, 0};
-        int rows = 0;
-        for (int i = 0; i < N; i++) {
-            for (int j = 0; j < D; j++) {
-                const uint32_t d = digits[i * D + j];
-                const uint64_t *row = A.kskey + ((size_t)(d * D + j) * N + i) * A.ks_row;
+        uint64_t s0 = 0, s1 = 0;
+        const int total = N * D;
+        int i = 0, j = 0, rows = 0;
+        for (int r0 = 0; r0 < total; r0 += kKs64Unroll) {
+            ulonglong2 v[kKs64Unroll];
 #pragma unroll
-                for (int cc = 0; cc < PT; cc++) {
-                    const int k = threadIdx.x + cc * kT64;
-                    if (k <= n) acc[cc] += __ldg(row + k);
+            for (int u = 0; u < kKs64Unroll; u++) {
+                v[u] = make_ulonglong2(0, 0);
+                if (r0 + u < total) {
+                    const uint32_t d = digits[r0 + u];
+                    v[u] = __ldg(key2 + ((size_t)(d * D + j) * N + i) * rs2 + t);
                 }
-                if (++rows == 256) {
-                    rows = 0;
+                if (++j == D) {
+                    j = 0;
+                    ++i;
+                }
+            }
 #pragma unroll
-                    for (int cc = 0; cc < PT; cc++) acc[cc] %= Q;
-                }
+            for (int u = 0; u < kKs64Unroll; u++) {
+                s0 += v[u].x;
+                s1 += v[u].y;
+            }
+            rows += kKs64Unroll;
+            if (rows >= A.fold) {
+                rows = 0;
+                s0 %= Q;
+                s1 %= Q;
             }
         }
         const uint64_t b0 = ext[N];
         const uint64_t Q8 = Q / 8 + 1;
         uint64_t *out = A.out + ci * (size_t)(n + 1);
+        const uint64_t sums[2] = {s0, s1};
 #pragma unroll
-        for (int cc = 0; cc < PT; cc++) {
-            const int k = threadIdx.x + cc * kT64;
+        for (int c2 = 0; c2 < 2; c2++) {
+            const int k = 2 * t + c2;
             if (k <= n) {
-                const uint64_t sred = acc[cc] % Q;
+                const uint64_t sred = sums[c2] % Q;
                 uint64_t v;
                 if (k < n) v = sred ? Q - sred : 0;
                 else v = ((b0 + Q8) % Q + Q - sred) % Q;
@@ -513,14 +532,18 @@ int launch_lwe_keyswitch64(Context &c, const uint64_t *d_extract, size_t count, 
 {
     if (!count) return FHEACC_OK;
     if (!c.d_kskey64) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
-    if (c.p.n + 1 > 4 * dev::kT64) return c.fail(FHEACC_EINVAL, "n too large for key switch");
+    if (c.dp.ks_row > 1024) return c.fail(FHEACC_EINVAL, "n too large for key switch");
     dev::Ks64Args A{};
     A.ext = d_extract; A.count = count; A.kskey = c.d_kskey64; A.out = d_out;
     A.n = c.p.n; A.N = c.p.N; A.digitKS = (int)c.p.digitKS; A.Bks = c.p.Bks; A.ks_row = c.dp.ks_row;
     A.q = c.p.q; A.modswitch = modswitch ? 1u : 0u; A.Q = c.p.Q;
+    // key words are < Q: (fold + 1) Q must stay below 2^64
+    const uint64_t fold = std::min<uint64_t>(256, UINT64_MAX / c.p.Q - 1);
+    A.fold = (int)std::max<uint64_t>(8, fold & ~(uint64_t)7);
     const size_t smem = (size_t)c.p.N * c.p.digitKS;
-    size_t blocks = std::min<size_t>(count, (size_t)sms_of(c) * 8);
-    dev::lwe_ks64_kernel<<<(unsigned)blocks, dev::kT64, smem, st>>>(A);
+    const unsigned threads = c.dp.ks_row / 2;   // ks_row: a multiple of 32 words, > n
+    size_t blocks = std::min<size_t>(count, (size_t)sms_of(c) * 6);
+    dev::lwe_ks64_kernel<<<(unsigned)blocks, threads, smem, st>>>(A);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "lwe_ks64 launch");
 }
