@@ -99,3 +99,23 @@ def test_reference_fixture(F, ctx0, keys0):
     assert digest(c1, c2) == fx["inputs_sha256"].item().decode()
     out = ctx0.eval_bootstrap_batch(c1, c2, g)
     assert np.array_equal(out, fx["out"].astype(np.uint64))
+
+
+@pytest.mark.parametrize("count,group", [(12007, 0), (1021, 3), (2, 0)])
+def test_large_and_ragged_batches(F, ctx0, keys0, count, group):
+    """Batches that take several chunks per CTA (12007 gates: more than the
+    grid holds in one group), uneven groups under a small cap (1021 gates,
+    at most 3 per CTA) and a batch smaller than one group per CTA: every
+    gate decrypts, and a sample (first, last and spread) equals the oracle."""
+    x, y, g, c1, c2 = random_gate_batch(keys0, count, seed=200 + count)
+    ctx0.set_option(F.OPT_BR_GROUP, group)
+    try:
+        out = ctx0.eval_bootstrap_batch(c1, c2, g)
+    finally:
+        ctx0.set_option(F.OPT_BR_GROUP, 0)
+    truth = np.array([F.gate_truth(int(a), b, c) for a, b, c in zip(g, x, y)], dtype=np.uint8)
+    assert np.array_equal(keys0.decrypt(out), truth)
+    idx = np.unique(np.concatenate([[0, count - 1], np.linspace(0, count - 1, 14).astype(int)]))
+    want, failed = keys0.oracle.eval_bootstrap_batch(c1[idx], c2[idx], g[idx], keys0.btkey, keys0.kskey)
+    assert failed == 0
+    assert np.array_equal(out[idx], want)
