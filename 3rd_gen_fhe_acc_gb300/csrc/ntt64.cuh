@@ -57,71 +57,119 @@ __device__ __forceinline__ void group_sync(int bar_id, int threads)
     asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "r"(threads) : "memory");
 }
 
+// One radix-8 forward pass: stages t, t/2, t/4 (m = N / 2t) on the octets
+// e0 + k t/4 (k < 8) of every 2t-block, by `G` threads.
+template <int G>
+__device__ __forceinline__ void fwd_pass8(uint64_t *a, const ulonglong2 *__restrict__ tw, const Ntt64Consts &c,
+                                          int tid, int t, int m)
+{
+    const int h = t >> 2;
+    for (int oc = tid; oc < 256; oc += G) {
+        const int grp = oc / h, j = oc - grp * h;
+        const int e0 = grp * 2 * t + j;
+        uint64_t x[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) x[k] = a[e0 + k * h];
+        const ulonglong2 w1 = __ldg(tw + m + grp);
+        ct64(x[0], x[4], w1, c.Q, c.twoQ);
+        ct64(x[1], x[5], w1, c.Q, c.twoQ);
+        ct64(x[2], x[6], w1, c.Q, c.twoQ);
+        ct64(x[3], x[7], w1, c.Q, c.twoQ);
+        const ulonglong2 w2a = __ldg(tw + 2 * m + 2 * grp), w2b = __ldg(tw + 2 * m + 2 * grp + 1);
+        ct64(x[0], x[2], w2a, c.Q, c.twoQ);
+        ct64(x[1], x[3], w2a, c.Q, c.twoQ);
+        ct64(x[4], x[6], w2b, c.Q, c.twoQ);
+        ct64(x[5], x[7], w2b, c.Q, c.twoQ);
+#pragma unroll
+        for (int k = 0; k < 4; k++) ct64(x[2 * k], x[2 * k + 1], __ldg(tw + 4 * m + 4 * grp + k), c.Q, c.twoQ);
+#pragma unroll
+        for (int k = 0; k < 8; k++) a[e0 + k * h] = x[k];
+    }
+}
+
 // Forward NTT of a[2048] in shared memory by `G` threads (tid < G) that share
 // the named barrier `bar`. tw[k] = (psi^bitrev(k), companion). Input < Q,
-// output < 23Q, bit-reversed order as the reference's.
+// output < 23Q, bit-reversed order as the reference's. Three radix-8 passes
+// (stages t = 1024..256, 128..32, 16..4) and one radix-4 pass (t = 2, 1).
 template <int G>
 __device__ __forceinline__ void ntt64_fwd_2048(uint64_t *a, const ulonglong2 *__restrict__ tw, const Ntt64Consts &c,
                                                int tid, int bar)
 {
-    constexpr int N = 2048;
-    int m = 1;
-#pragma unroll 1
-    for (int t = N / 2; t >= 2; t >>= 2, m <<= 2) {   // stages (t, t/2)
-        const int h = t >> 1;
-        for (int qd = tid; qd < N / 4; qd += G) {
-            const int grp = qd / h, j = qd - grp * h;
-            const int e0 = grp * 2 * t + j;
-            uint64_t x0 = a[e0], x1 = a[e0 + h], x2 = a[e0 + t], x3 = a[e0 + t + h];
-            const ulonglong2 w = __ldg(tw + m + grp);
-            ct64(x0, x2, w, c.Q, c.twoQ);
-            ct64(x1, x3, w, c.Q, c.twoQ);
-            ct64(x0, x1, __ldg(tw + 2 * m + 2 * grp), c.Q, c.twoQ);
-            ct64(x2, x3, __ldg(tw + 2 * m + 2 * grp + 1), c.Q, c.twoQ);
-            a[e0] = x0; a[e0 + h] = x1; a[e0 + t] = x2; a[e0 + t + h] = x3;
-        }
-        group_sync(bar, G);
-    }
-    // last stage, t = 1, m = 1024
-    for (int b = tid; b < N / 2; b += G) {
-        uint64_t x = a[2 * b], y = a[2 * b + 1];
-        ct64(x, y, __ldg(tw + 1024 + b), c.Q, c.twoQ);
-        a[2 * b] = x;
-        a[2 * b + 1] = y;
+    fwd_pass8<G>(a, tw, c, tid, 1024, 1);
+    group_sync(bar, G);
+    fwd_pass8<G>(a, tw, c, tid, 128, 8);
+    group_sync(bar, G);
+    fwd_pass8<G>(a, tw, c, tid, 16, 64);
+    group_sync(bar, G);
+    // stages t = 2, 1 (m = 512, 1024): quads 4b + {0, 1, 2, 3}
+    for (int b = tid; b < 512; b += G) {
+        uint64_t x0 = a[4 * b], x1 = a[4 * b + 1], x2 = a[4 * b + 2], x3 = a[4 * b + 3];
+        const ulonglong2 w = __ldg(tw + 512 + b);
+        ct64(x0, x2, w, c.Q, c.twoQ);
+        ct64(x1, x3, w, c.Q, c.twoQ);
+        ct64(x0, x1, __ldg(tw + 1024 + 2 * b), c.Q, c.twoQ);
+        ct64(x2, x3, __ldg(tw + 1024 + 2 * b + 1), c.Q, c.twoQ);
+        a[4 * b] = x0; a[4 * b + 1] = x1; a[4 * b + 2] = x2; a[4 * b + 3] = x3;
     }
     group_sync(bar, G);
 }
 
+// One radix-8 inverse pass: stages t, 2t, 4t (m = N / 2t) on the octets
+// e0 + k t (k < 8) of every 8t-block.
+template <int G>
+__device__ __forceinline__ void inv_pass8(uint64_t *a, const ulonglong2 *__restrict__ itw, const Ntt64Consts &c,
+                                          int tid, int t, int m)
+{
+    for (int oc = tid; oc < 256; oc += G) {
+        const int grp = oc / t, j = oc - grp * t;
+        const int e0 = grp * 8 * t + j;
+        uint64_t x[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) x[k] = a[e0 + k * t];
+#pragma unroll
+        for (int k = 0; k < 4; k++) gs64(x[2 * k], x[2 * k + 1], __ldg(itw + m + 4 * grp + k), c.Q, c.twoQ);
+        const ulonglong2 w2a = __ldg(itw + (m >> 1) + 2 * grp), w2b = __ldg(itw + (m >> 1) + 2 * grp + 1);
+        gs64(x[0], x[2], w2a, c.Q, c.twoQ);
+        gs64(x[1], x[3], w2a, c.Q, c.twoQ);
+        gs64(x[4], x[6], w2b, c.Q, c.twoQ);
+        gs64(x[5], x[7], w2b, c.Q, c.twoQ);
+        const ulonglong2 w4 = __ldg(itw + (m >> 2) + grp);
+        gs64(x[0], x[4], w4, c.Q, c.twoQ);
+        gs64(x[1], x[5], w4, c.Q, c.twoQ);
+        gs64(x[2], x[6], w4, c.Q, c.twoQ);
+        gs64(x[3], x[7], w4, c.Q, c.twoQ);
+#pragma unroll
+        for (int k = 0; k < 8; k++) a[e0 + k * t] = x[k];
+    }
+}
+
 // Inverse NTT of a[2048] (values < 2Q, bit-reversed order) in shared memory
 // -> canonical coefficients times N^-1. itw[k] = (psi^-bitrev(k), companion).
+// Three radix-8 passes (stages t = 1..4, 8..32, 64..256) and one radix-4 pass
+// (t = 512 and the last stage, t = 1024, with N^-1 folded into both outputs).
 template <int G>
 __device__ __forceinline__ void ntt64_inv_2048(uint64_t *a, const ulonglong2 *__restrict__ itw, const Ntt64Consts &c,
                                                int tid, int bar)
 {
-    constexpr int N = 2048;
-    int m = N / 2;
-#pragma unroll 1
-    for (int t = 1; t <= N / 8; t <<= 2, m >>= 2) {   // stages (t, 2t)
-        for (int qd = tid; qd < N / 4; qd += G) {
-            const int grp = qd / t, j = qd - grp * t;
-            const int e0 = grp * 4 * t + j;
-            uint64_t x0 = a[e0], x1 = a[e0 + t], x2 = a[e0 + 2 * t], x3 = a[e0 + 3 * t];
-            gs64(x0, x1, __ldg(itw + m + 2 * grp), c.Q, c.twoQ);
-            gs64(x2, x3, __ldg(itw + m + 2 * grp + 1), c.Q, c.twoQ);
-            const ulonglong2 w = __ldg(itw + (m >> 1) + grp);
-            gs64(x0, x2, w, c.Q, c.twoQ);
-            gs64(x1, x3, w, c.Q, c.twoQ);
-            a[e0] = x0; a[e0 + t] = x1; a[e0 + 2 * t] = x2; a[e0 + 3 * t] = x3;
-        }
-        group_sync(bar, G);
-    }
-    // last stage, t = 1024, m = 1, with N^-1 folded into both outputs
-    for (int b = tid; b < N / 2; b += G) {
-        const uint64_t x = a[b], y = a[b + 1024];
-        uint64_t u = shoup64(x + y, c.iN, c.iNs, c.Q);
-        uint64_t v = shoup64(x - y + c.twoQ, c.iw1N, c.iw1Ns, c.Q);
+    inv_pass8<G>(a, itw, c, tid, 1, 1024);
+    group_sync(bar, G);
+    inv_pass8<G>(a, itw, c, tid, 8, 128);
+    group_sync(bar, G);
+    inv_pass8<G>(a, itw, c, tid, 64, 16);
+    group_sync(bar, G);
+    for (int b = tid; b < 512; b += G) {
+        uint64_t x0 = a[b], x1 = a[b + 512], x2 = a[b + 1024], x3 = a[b + 1536];
+        gs64(x0, x1, __ldg(itw + 2), c.Q, c.twoQ);   // t = 512, m = 2, block 0
+        gs64(x2, x3, __ldg(itw + 3), c.Q, c.twoQ);   // block 1
+        // t = 1024, m = 1, with N^-1 folded into both outputs
+        uint64_t u = shoup64(x0 + x2, c.iN, c.iNs, c.Q);
+        uint64_t v = shoup64(x0 - x2 + c.twoQ, c.iw1N, c.iw1Ns, c.Q);
         a[b] = u >= c.Q ? u - c.Q : u;
         a[b + 1024] = v >= c.Q ? v - c.Q : v;
+        u = shoup64(x1 + x3, c.iN, c.iNs, c.Q);
+        v = shoup64(x1 - x3 + c.twoQ, c.iw1N, c.iw1Ns, c.Q);
+        a[b + 512] = u >= c.Q ? u - c.Q : u;
+        a[b + 1536] = v >= c.Q ? v - c.Q : v;
     }
     group_sync(bar, G);
 }
