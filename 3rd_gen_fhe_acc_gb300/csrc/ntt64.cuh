@@ -57,60 +57,47 @@ __device__ __forceinline__ void group_sync(int bar_id, int threads)
     asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "r"(threads) : "memory");
 }
 
-// One radix-8 forward pass: stages t, t/2, t/4 (m = N / 2t) on the octets
-// e0 + k t/4 (k < 8) of every 2t-block, by `G` threads.
-template <int G>
-__device__ __forceinline__ void fwd_pass8(uint64_t *a, const ulonglong2 *__restrict__ tw, const Ntt64Consts &c,
+// One radix-2^R forward pass: stages t, t/2, ..., t/2^(R-1) (m = N / 2t) on
+// the tuples e0 + k t/2^(R-1) (k < 2^R) of every 2t-block.
+template <int G, int R>
+__device__ __forceinline__ void fwd_passR(uint64_t *a, const ulonglong2 *__restrict__ tw, const Ntt64Consts &c,
                                           int tid, int t, int m)
 {
-    const int h = t >> 2;
-    for (int oc = tid; oc < 256; oc += G) {
+    constexpr int K = 1 << R;
+    const int h = t >> (R - 1);
+    for (int oc = tid; oc < 2048 / K; oc += G) {
         const int grp = oc / h, j = oc - grp * h;
         const int e0 = grp * 2 * t + j;
-        uint64_t x[8];
+        uint64_t x[K];
 #pragma unroll
-        for (int k = 0; k < 8; k++) x[k] = a[e0 + k * h];
-        const ulonglong2 w1 = __ldg(tw + m + grp);
-        ct64(x[0], x[4], w1, c.Q, c.twoQ);
-        ct64(x[1], x[5], w1, c.Q, c.twoQ);
-        ct64(x[2], x[6], w1, c.Q, c.twoQ);
-        ct64(x[3], x[7], w1, c.Q, c.twoQ);
-        const ulonglong2 w2a = __ldg(tw + 2 * m + 2 * grp), w2b = __ldg(tw + 2 * m + 2 * grp + 1);
-        ct64(x[0], x[2], w2a, c.Q, c.twoQ);
-        ct64(x[1], x[3], w2a, c.Q, c.twoQ);
-        ct64(x[4], x[6], w2b, c.Q, c.twoQ);
-        ct64(x[5], x[7], w2b, c.Q, c.twoQ);
+        for (int k = 0; k < K; k++) x[k] = a[e0 + k * h];
 #pragma unroll
-        for (int k = 0; k < 4; k++) ct64(x[2 * k], x[2 * k + 1], __ldg(tw + 4 * m + 4 * grp + k), c.Q, c.twoQ);
+        for (int st = 0; st < R; st++) {
+            const int d = K >> (st + 1);
 #pragma unroll
-        for (int k = 0; k < 8; k++) a[e0 + k * h] = x[k];
+            for (int k = 0; k < K; k++) {
+                if (k & d) continue;
+                ct64(x[k], x[k + d], __ldg(tw + (m << st) + (grp << st) + (k >> (R - st))), c.Q, c.twoQ);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++) a[e0 + k * h] = x[k];
     }
 }
 
 // Forward NTT of a[2048] in shared memory by `G` threads (tid < G) that share
 // the named barrier `bar`. tw[k] = (psi^bitrev(k), companion). Input < Q,
-// output < 23Q, bit-reversed order as the reference's. Three radix-8 passes
-// (stages t = 1024..256, 128..32, 16..4) and one radix-4 pass (t = 2, 1).
+// output < 23Q, bit-reversed order as the reference's. Two radix-16 passes
+// (stages t = 1024..128, 64..8) and one radix-8 pass (t = 4, 2, 1).
 template <int G>
 __device__ __forceinline__ void ntt64_fwd_2048(uint64_t *a, const ulonglong2 *__restrict__ tw, const Ntt64Consts &c,
                                                int tid, int bar)
 {
-    fwd_pass8<G>(a, tw, c, tid, 1024, 1);
+    fwd_passR<G, 4>(a, tw, c, tid, 1024, 1);   // t = 1024 .. 128
     group_sync(bar, G);
-    fwd_pass8<G>(a, tw, c, tid, 128, 8);
+    fwd_passR<G, 4>(a, tw, c, tid, 64, 16);    // t = 64 .. 8
     group_sync(bar, G);
-    fwd_pass8<G>(a, tw, c, tid, 16, 64);
-    group_sync(bar, G);
-    // stages t = 2, 1 (m = 512, 1024): quads 4b + {0, 1, 2, 3}
-    for (int b = tid; b < 512; b += G) {
-        uint64_t x0 = a[4 * b], x1 = a[4 * b + 1], x2 = a[4 * b + 2], x3 = a[4 * b + 3];
-        const ulonglong2 w = __ldg(tw + 512 + b);
-        ct64(x0, x2, w, c.Q, c.twoQ);
-        ct64(x1, x3, w, c.Q, c.twoQ);
-        ct64(x0, x1, __ldg(tw + 1024 + 2 * b), c.Q, c.twoQ);
-        ct64(x2, x3, __ldg(tw + 1024 + 2 * b + 1), c.Q, c.twoQ);
-        a[4 * b] = x0; a[4 * b + 1] = x1; a[4 * b + 2] = x2; a[4 * b + 3] = x3;
-    }
+    fwd_passR<G, 3>(a, tw, c, tid, 4, 256);    // t = 4, 2, 1
     group_sync(bar, G);
 }
 
