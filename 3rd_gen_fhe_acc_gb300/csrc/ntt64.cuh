@@ -7,8 +7,9 @@
 // A 64-bit Shoup multiplication (w' = floor(w 2^64 / Q)) costs about five
 // times a 32-bit one, so shared-memory traffic matters less here than in the
 // 32-bit path: the polynomial stays in shared memory and each thread runs
-// radix-4 passes (two butterfly stages per load/store of four words), with one
-// group barrier per pass. Forward butterflies leave the upper input unreduced
+// radix-8 / radix-16 passes (three or four butterfly stages per load/store of
+// 8 or 16 words, 4 passes per transform), with one group barrier per pass.
+// Forward butterflies leave the upper input unreduced
 // (bound grows by 2Q a stage: inputs < Q end below 23Q < 2^59 for Q < 2^54);
 // the inverse keeps Harvey's [0, 2Q) invariant and ends canonical.
 #pragma once
