@@ -24,16 +24,17 @@
 // __syncthreads:
 //   inverse-NTT warps (2): load acc of item k+1, inverse NTT of a and b,
 //                          canonical time-domain coefficients -> tslot[k+1 & 1]
-//   digit warps (2*digitG): item k: digit h of poly p from tslot[k & 1],
-//                          forward NTT (first two stages by table lookup,
-//                          ntt_fwd_1024_digit) -> dbuf; named barrier;
-//                          multiply-accumulate with the item's RGSW key
-//                          (64-bit sums, one Montgomery reduction per output)
-//                          -> acc (global)
+//   digit warps (2*(digitG-1)): item k: digit h < digitG-1 of poly p from
+//                          tslot[k & 1], forward NTT (first two stages by
+//                          table lookup when BG <= kMaxTableBG,
+//                          ntt_fwd_1024_digit) -> dbuf
+//   all warps, after __syncthreads: multiply-accumulate item k with its RGSW
+//                          key (64-bit sums, one Montgomery reduction per
+//                          output) -> acc (global)
 // An item whose ciphertext is still in the digit stage waits one period.
 //
-// Last digit. When Q < BG^digitG the digits recompose each canonical
-// coefficient exactly, so sum_h BG^h NTT(digit_h) equals the NTT-domain
+// Last digit. Parameter validation requires Q < BG^digitG, so the digits
+// recompose each canonical coefficient exactly, so sum_h BG^h NTT(digit_h) equals the NTT-domain
 // accumulator. The keys are uploaded with that identity folded in
 // (DevParams::last_digit_from_acc), the warps of the last digit skip their
 // transform, and the MAC multiplies the accumulator (read from global memory
@@ -60,6 +61,7 @@ namespace fheacc {
 namespace dev {
 
 constexpr int kMaxGroup = 24;   // ciphertexts per CTA and chunk (residue table in shared memory)
+constexpr int kMaxTableBG = 512;   // largest gadget base with digit tables (20 BG bytes of shared memory)
 
 struct PipeArgs {
     const uint64_t *c1, *c2;
@@ -78,6 +80,7 @@ struct PipeArgs {
     uint32_t nmul, nmuls;      // N mod Q and its Shoup companion (canonical accumulators out)
     uint32_t w21, w31;         // rou[2] rou[1], rou[3] rou[1] mod Q (digit tables)
     uint32_t derive_last;      // last digit's NTT from the accumulator (DevParams::last_digit_from_acc)
+    uint32_t digit_tables;     // first two digit-NTT stages by table lookup (BG <= kMaxTableBG)
     uint64_t gate_constant[8];
 };
 
@@ -127,11 +130,6 @@ __device__ __forceinline__ void store_btile(uint32_t *dst, const uint32_t (&x)[3
                                                                        x[4 * qq + 3]));
 }
 
-__device__ __forceinline__ void named_barrier(int id, int threads)
-{
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
-}
-
 // Plans the next pipeline period (run by one thread). ctl: [0, 1] cursor
 // (step, ciphertext) of the last item taken by the inverse-NTT warps; [2, 3]
 // item of the digit warps; [4] slot; [5] cursor exhausted; [6] this period's
@@ -175,17 +173,16 @@ __device__ __noinline__ void pipe_schedule(int *ctl, const uint8_t *res, int m, 
     ctl[4] ^= 1;
 }
 
-// DV = 1: the last digit's NTT comes from the accumulator (2 (digitG - 1)
-// digit warps, and all warps share the MAC); DV = 0: 2 digitG digit warps.
-template <int DG, int MINB, int DV>
-__global__ void __launch_bounds__(32 * (2 * (DG - DV) + 2), MINB)
+// 2 (digitG - 1) digit warps (the last digit's NTT comes from the
+// accumulator) and 2 inverse-NTT warps; all warps share the MAC.
+template <int DG, int MINB>
+__global__ void __launch_bounds__(32 * (2 * (DG - 1) + 2), MINB)
     br32_pipe_kernel(const __grid_constant__ PipeArgs A, const __grid_constant__ Ntt32Consts c,
                      const uint2 *__restrict__ fwd_tw, const uint2 *__restrict__ inv_tw, uint32_t mu32)
 {
-    constexpr int DT = DG - DV;  // digit NTTs per poly
+    constexpr int DT = DG - 1;   // digit NTTs per poly
     constexpr int GW = 2 * DT;   // digit warps
     constexpr int NW = GW + 2;   // plus the two inverse-NTT warps
-    constexpr int GT = 32 * GW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PipeSmem<GW> &s = *reinterpret_cast<PipeSmem<GW> *>(smem_raw);
     uint8_t *res = smem_raw + sizeof(PipeSmem<GW>);   // [group][n * digitR] residues
@@ -198,7 +195,7 @@ __global__ void __launch_bounds__(32 * (2 * (DG - DV) + 2), MINB)
     const size_t G = gridDim.x;
 
     // digit tables (ntt_fwd_1024_digit): t1 [BG], t23 [BG], t123 [BG]
-    const int BG = 1 << A.bg_bits;
+    const int BG = A.digit_tables ? 1 << A.bg_bits : 0;
     uint32_t *t1 = reinterpret_cast<uint32_t *>(smem_raw + pipe_tables_offset<GW>(A.group, S));
     uint2 *t23 = reinterpret_cast<uint2 *>(t1 + BG), *t123 = t23 + BG;
     for (int y = threadIdx.x; y < BG; y += blockDim.x) {
@@ -291,32 +288,20 @@ __global__ void __launch_bounds__(32 * (2 * (DG - DV) + 2), MINB)
                 load_row(x, s.tslot[sh ^ 1][p], lane);
 #pragma unroll
                 for (int r = 0; r < 32; r++) x[r] = (x[r] >> shift) & mask;
-                ntt_fwd_1024_digit(x, c, fwd_tw, s.dbuf[warp], dt, lane);
+                if (A.digit_tables) ntt_fwd_1024_digit(x, c, fwd_tw, s.dbuf[warp], dt, lane);
+                else ntt_fwd_1024(x, c, fwd_tw, s.dbuf[warp], lane);
                 store_row(s.dbuf[warp], lane, x);
-                if (!DV) {
-                    // the digit warps alone multiply-accumulate, after their named barrier
-                    const int gk = ctl[3], gs = ctl[2];
-                    const uint32_t rr = res[gk * S + gs];
-                    const uint4 *key =
-                        reinterpret_cast<const uint4 *>(A.btkey + ((size_t)gs * A.Br + rr) * rgsw_words);
-                    uint4 *acc = reinterpret_cast<uint4 *>(A.accs + (first + (size_t)gk * G) * 2048);
-                    named_barrier(1, GT);
-                    for (int u = threadIdx.x; u < 256; u += GT) mac_chunk<DG>(u, key, s.dbuf, acc, c.Q, A.qinv_neg);
-                }
             }
-            if (DV) {
-                // all warps multiply-accumulate the digit warps' item once its
-                // digit NTTs are in shared memory
-                __syncthreads();
-                if (ctl[3] >= 0) {
-                    const int gk = ctl[3], gs = ctl[2];
-                    const uint32_t rr = res[gk * S + gs];
-                    const uint4 *key =
-                        reinterpret_cast<const uint4 *>(A.btkey + ((size_t)gs * A.Br + rr) * rgsw_words);
-                    uint4 *acc = reinterpret_cast<uint4 *>(A.accs + (first + (size_t)gk * G) * 2048);
-                    for (int u = threadIdx.x; u < 256; u += 32 * NW)
-                        mac_chunk<DG, true>(u, key, s.dbuf, acc, c.Q, A.qinv_neg, acc);
-                }
+            // all warps multiply-accumulate the digit warps' item once its digit
+            // NTTs are in shared memory
+            __syncthreads();
+            if (ctl[3] >= 0) {
+                const int gk = ctl[3], gs = ctl[2];
+                const uint32_t rr = res[gk * S + gs];
+                const uint4 *key = reinterpret_cast<const uint4 *>(A.btkey + ((size_t)gs * A.Br + rr) * rgsw_words);
+                uint4 *acc = reinterpret_cast<uint4 *>(A.accs + (first + (size_t)gk * G) * 2048);
+                for (int u = threadIdx.x; u < 256; u += 32 * NW)
+                    mac_chunk<DG, true>(u, key, s.dbuf, acc, c.Q, A.qinv_neg, acc);
             }
             __syncthreads();
             if (threadIdx.x == 0) pipe_schedule(ctl, res, m, S, compat);
@@ -364,13 +349,13 @@ static int sm_count(Context &c)
     return v > 0 ? v : 1;
 }
 
-template <int DG, int MINB, int DV>
+template <int DG, int MINB>
 static int launch_pipe_dg(Context &c, dev::PipeArgs A, int max_ctas, cudaStream_t st)
 {
-    constexpr int GW = 2 * (DG - DV);
+    constexpr int GW = 2 * (DG - 1);
     constexpr int threads = 32 * (GW + 2);
-    auto kern = dev::br32_pipe_kernel<DG, MINB, DV>;
-    const size_t steps = (size_t)c.p.n * c.p.digitR, tables = 20 * ((size_t)1 << c.p.BG_bits);
+    auto kern = dev::br32_pipe_kernel<DG, MINB>;
+    const size_t steps = (size_t)c.p.n * c.p.digitR, tables = A.digit_tables ? 20 * ((size_t)1 << c.p.BG_bits) : 0;
     const int cap = c.tune.br_group > 0 ? std::min(c.tune.br_group, dev::kMaxGroup) : dev::kMaxGroup;
     // residency with the largest group allowed; the group is then fitted to the batch
     size_t smem = dev::pipe_tables_offset<GW>(cap, steps) + tables;
@@ -408,24 +393,20 @@ static void fill_pipe_params(Context &c, dev::PipeArgs &A, uint32_t flags)
     A.w21 = (uint32_t)((uint64_t)c.nc.fw[2] * c.nc.fw[1] % Q);
     A.w31 = (uint32_t)((uint64_t)c.nc.fw[3] * c.nc.fw[1] % Q);
     A.derive_last = c.dp.last_digit_from_acc;
+    A.digit_tables = (1u << c.p.BG_bits) <= (uint32_t)dev::kMaxTableBG;
     for (int i = 0; i < 8; i++) A.gate_constant[i] = c.dp.gate_constant[i];
 }
 
 static int launch_pipe(Context &c, const dev::PipeArgs &A, int max_ctas, cudaStream_t st)
 {
-    const bool three = c.tune.br_regs_for_3 < 0 ? A.derive_last != 0 : c.tune.br_regs_for_3 != 0;
-    if (A.derive_last) {
-        switch (c.p.digitG) {
-        case 2: return three ? launch_pipe_dg<2, 3, 1>(c, A, max_ctas, st) : launch_pipe_dg<2, 2, 1>(c, A, max_ctas, st);
-        case 3: return three ? launch_pipe_dg<3, 3, 1>(c, A, max_ctas, st) : launch_pipe_dg<3, 2, 1>(c, A, max_ctas, st);
-        case 4: return three ? launch_pipe_dg<4, 3, 1>(c, A, max_ctas, st) : launch_pipe_dg<4, 2, 1>(c, A, max_ctas, st);
-        default: break;
-        }
-    }
+    // parameter validation makes the gadget cover Q, which the last-digit
+    // identity of the kernel needs
+    if (!A.derive_last) return c.fail(FHEACC_EINVAL, "gadget base^digitG must exceed Q");
+    const bool three = c.tune.br_regs_for_3 != 0;   // -1 (default) or 1: 3 CTAs per SM
     switch (c.p.digitG) {
-    case 2: return three ? launch_pipe_dg<2, 3, 0>(c, A, max_ctas, st) : launch_pipe_dg<2, 2, 0>(c, A, max_ctas, st);
-    case 3: return three ? launch_pipe_dg<3, 3, 0>(c, A, max_ctas, st) : launch_pipe_dg<3, 2, 0>(c, A, max_ctas, st);
-    case 4: return three ? launch_pipe_dg<4, 3, 0>(c, A, max_ctas, st) : launch_pipe_dg<4, 2, 0>(c, A, max_ctas, st);
+    case 2: return three ? launch_pipe_dg<2, 3>(c, A, max_ctas, st) : launch_pipe_dg<2, 2>(c, A, max_ctas, st);
+    case 3: return three ? launch_pipe_dg<3, 3>(c, A, max_ctas, st) : launch_pipe_dg<3, 2>(c, A, max_ctas, st);
+    case 4: return three ? launch_pipe_dg<4, 3>(c, A, max_ctas, st) : launch_pipe_dg<4, 2>(c, A, max_ctas, st);
     default: return c.fail(FHEACC_EINVAL, "digitG must be 2..4 for the 32-bit path");
     }
 }

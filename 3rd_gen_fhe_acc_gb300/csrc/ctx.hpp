@@ -35,8 +35,7 @@ struct DevParams {
 // Launch-shape choices of the blind-rotation kernel (set by fheacc_set_option
 // or picked by fheacc_autotune).
 struct Tuning {
-    int br_regs_for_3 = -1;   // register budget for 3 CTAs/SM (1) or 2 (0); -1: 3 when the
-                              // last-digit identity applies (8-warp CTAs), else 2
+    int br_regs_for_3 = -1;   // register budget for 3 CTAs/SM (1 or -1, the default) or 2 (0)
     int br_ctas_per_sm = 0;   // cap on resident CTAs per SM (0: occupancy limit)
     int br_group = 0;         // cap on ciphertexts per CTA and chunk (0: kernel maximum)
 };

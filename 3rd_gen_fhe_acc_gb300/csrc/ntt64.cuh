@@ -8,7 +8,8 @@
 // times a 32-bit one, so shared-memory traffic matters less here than in the
 // 32-bit path: the polynomial stays in shared memory and each thread runs
 // radix-8 / radix-16 passes (three or four butterfly stages per load/store of
-// 8 or 16 words, 4 passes per transform), with one group barrier per pass.
+// 8 or 16 words: 3 passes per forward transform, 4 per inverse), with one
+// group barrier per pass.
 // Forward butterflies leave the upper input unreduced
 // (bound grows by 2Q a stage: inputs < Q end below 23Q < 2^59 for Q < 2^54);
 // the inverse keeps Harvey's [0, 2Q) invariant and ends canonical.

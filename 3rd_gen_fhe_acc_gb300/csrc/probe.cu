@@ -177,16 +177,23 @@ int measure_components(Context &c, double ns[4])
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
     if (sms < 1) sms = 1;
     const int blocks = 2 * sms, iters = 200;
-    const size_t smem = 10 * dev::kN32 * sizeof(uint32_t) + 20 * ((size_t)1 << c.p.BG_bits);
+    // the digit transform uses tables only for gadget bases up to 2^9 (as the
+    // blind rotation does); above that it is the plain forward NTT
+    const bool tables = c.p.BG_bits <= 9;
+    const int bg = tables ? (int)c.p.BG_bits : 1;
+    const size_t smem = 10 * dev::kN32 * sizeof(uint32_t) + 20 * ((size_t)1 << bg);
     float ms[4] = {0, 0, 0, 0};
     int rc = FHEACC_OK;
     auto k0 = dev::ntt_rate_kernel<0>, k1 = dev::ntt_rate_kernel<1>, k2 = dev::ntt_rate_kernel<2>;
     for (auto k : {k0, k1, k2})
         if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return c.cuda_fail(cudaGetLastError(), "component probe smem attribute");
-    const int bg = (int)c.p.BG_bits;
     rc = time_best(c, [&] { k0<<<blocks, 320, smem, c.stream>>>(nullptr, iters, c.nc, c.d_fwd_tw, c.d_inv_tw, bg); }, &ms[0]);
-    if (!rc) rc = time_best(c, [&] { k1<<<blocks, 320, smem, c.stream>>>(nullptr, iters, c.nc, c.d_fwd_tw, c.d_inv_tw, bg); }, &ms[1]);
+    if (!rc && tables)
+        rc = time_best(c, [&] { k1<<<blocks, 320, smem, c.stream>>>(nullptr, iters, c.nc, c.d_fwd_tw, c.d_inv_tw, bg); },
+                       &ms[1]);
+    else
+        ms[1] = ms[0];
     if (!rc) rc = time_best(c, [&] { k2<<<blocks, 320, smem, c.stream>>>(nullptr, iters, c.nc, c.d_fwd_tw, c.d_inv_tw, bg); }, &ms[2]);
     if (rc) return rc;
     uint32_t *accs = nullptr;

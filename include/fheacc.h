@@ -207,9 +207,8 @@ int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t cou
                                uint64_t *d_out, void *stream);
 
 /* Launch-shape options of the blind-rotation kernel.
- *  FHEACC_OPT_BR_REGS_FOR_3 : 1 = the register budget of 3 resident CTAs
- *                             per SM, 0 = of 2 CTAs per SM, -1 (default) =
- *                             3 for 8-warp CTAs (Q < BG^digitG), else 2
+ *  FHEACC_OPT_BR_REGS_FOR_3 : 1 or -1 (default) = the register budget of 3
+ *                             resident CTAs per SM, 0 = of 2 CTAs per SM
  *  FHEACC_OPT_BR_CTAS_PER_SM: cap on resident CTAs per SM, 0 = occupancy limit
  *  FHEACC_OPT_BR_GROUP      : cap on the ciphertexts a CTA carries through the
  *                             bootstrap key together (its step-outer group;

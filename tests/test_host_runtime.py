@@ -59,6 +59,11 @@ def test_invalid_params_rejected(F):
     p.q = 500              # not a power of two
     with pytest.raises(F.FheaccError):
         F.derive(p)
+    for preset in (0, 1):
+        p = F.params_preset(preset)
+        p.BG_bits, p.digitG = 6, 4  # BG^digitG = 2^24 does not cover Q
+        with pytest.raises(F.FheaccError):
+            F.derive(p)
 
 
 def test_context_without_gpu_fails_cleanly(F):
