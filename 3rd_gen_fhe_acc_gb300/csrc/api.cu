@@ -36,6 +36,24 @@ int ensure_scratch(Context &c, Scratch &s, size_t bytes)
     return FHEACC_OK;
 }
 
+int prepare_window(Context &c, int steps, cudaStream_t st, dev::StepWindow &w)
+{
+    w = dev::StepWindow{};
+    const int K = c.tune.br_window < 0 ? kWindowWide : c.tune.br_window;
+    if (K <= 0 || !c.d_window || steps <= 0) return FHEACC_OK;
+    const int buckets = (steps + K - 1) / K;
+    if (buckets > kWindowCapacity) return FHEACC_OK;
+    cudaError_t e = cudaMemsetAsync(c.d_window, 0, (buckets + 1) * sizeof(unsigned), st);
+    if (e != cudaSuccess) return c.cuda_fail(e, "step-window reset");
+    w.count = c.d_window;
+    w.steps = K;
+    w.buckets = buckets;
+    // a bucket of the slowest CTAs takes well under a millisecond (32-bit) or a
+    // few milliseconds (64-bit); CTAs stop waiting after about 10 / 40 ms
+    w.spin_limit = c.wide ? 160000u : 40000u;
+    return FHEACC_OK;
+}
+
 
 int bootstrap_device_with(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
                           size_t count, uint64_t *d_out, uint32_t flags, void *accs, void *extract,
@@ -284,6 +302,12 @@ int fheacc_create(const fheacc_params *p, int device, fheacc_ctx **out)
         fheacc_destroy(reinterpret_cast<fheacc_ctx *>(c));
         return FHEACC_EIO;
     }
+    e = cudaMalloc(&c->d_window, (kWindowCapacity + 1) * sizeof(unsigned));
+    if (e != cudaSuccess) {
+        g_create_error = std::string("step-window counters: ") + cudaGetErrorString(e);
+        fheacc_destroy(reinterpret_cast<fheacc_ctx *>(c));
+        return FHEACC_ENOMEM;
+    }
     int rc = build_tables(*c);
     if (rc == FHEACC_OK) rc = build_rotations(*c);
     if (rc != FHEACC_OK) {
@@ -316,6 +340,8 @@ int fheacc_destroy(fheacc_ctx *ctx)
     cudaFree(c->accs.ptr);
     cudaFree(c->extract.ptr);
     cudaFree(c->io.ptr);
+    cudaFree(c->psi.ptr);
+    cudaFree(c->d_window);
     if (c->done) cudaEventDestroy(c->done);
     for (auto &ev : c->prof)
         if (ev) cudaEventDestroy(ev);
@@ -695,6 +721,11 @@ int fheacc_set_option(fheacc_ctx *ctx, int option, int value)
         if (value < 0 || value > 64) return c.fail(FHEACC_EINVAL, "group size out of range");
         c.tune.br_group = value;
         return FHEACC_OK;
+    case FHEACC_OPT_BR_WINDOW:
+        if (value < -1 || value > 1024) return c.fail(FHEACC_EINVAL, "step window out of range");
+        c.tune.br_window = value;
+        return FHEACC_OK;
+
     default:
         return c.fail(FHEACC_EINVAL, "unknown option");
     }

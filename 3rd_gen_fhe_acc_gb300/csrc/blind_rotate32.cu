@@ -10,14 +10,14 @@
 // instruction issue (myfpga.cpp:1446-1492) feeding iNTT_module.sv,
 // NTT_leading_stage.sv, poly_mult_RLWE.sv and accumulator.sv.
 //
-// Schedule. The grid is persistent; CTA b owns the group of ciphertexts
-// b, b + grid, b + 2 grid, ... (the launcher fits the group size to the
-// batch: the fewest chunks of at most kMaxGroup, or the tuned cap). Steps are the
-// OUTER loop: a CTA applies step s to every ciphertext of its group before
-// step s + 1, so all CTAs walk through the bootstrapping key together and the
-// 23 RGSW keys of a step (1.5 MB) are fetched from HBM about once and then
-// served from L2 to every CTA. Accumulators live in global memory (8 KB per
-// ciphertext, L2-resident for batches of thousands).
+// Schedule. The grid is persistent; each CTA claims a group of consecutive
+// ciphertexts from a counter (the launcher fits the group size to the batch:
+// the fewest rounds of at most kMaxGroup, or the tuned cap) and claims again
+// until the batch is done. Steps are the OUTER loop: a CTA applies step s to every ciphertext of
+// its group before step s + 1, so the CTAs walk through the bootstrapping key
+// together and the 23 RGSW keys of a step (1.5 MB) are mostly served from L2.
+// Accumulators live in global memory (8 KB per ciphertext, L2-resident for
+// batches of thousands).
 //
 // Inside a CTA the (step, ciphertext) items flow through a two-stage warp-
 // specialised pipeline, one item per period, periods separated by
@@ -82,6 +82,7 @@ struct PipeArgs {
     uint32_t derive_last;      // last digit's NTT from the accumulator (DevParams::last_digit_from_acc)
     uint32_t digit_tables;     // first two digit-NTT stages by table lookup (BG <= kMaxTableBG)
     uint64_t gate_constant[8];
+    unsigned long long *claim_next;   // next unclaimed ciphertext (zeroed before the launch)
 };
 
 // Shared memory of one CTA. tslot holds lane-major copies of the inverse-NTT
@@ -187,12 +188,13 @@ __global__ void __launch_bounds__(32 * (2 * (DG - 1) + 2), MINB)
     PipeSmem<GW> &s = *reinterpret_cast<PipeSmem<GW> *>(smem_raw);
     uint8_t *res = smem_raw + sizeof(PipeSmem<GW>);   // [group][n * digitR] residues
     __shared__ int ctl[8];
+    __shared__ unsigned long long claim_first;
+    __shared__ int claim_m;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = A.n, S = n * (int)A.digitR;
     const uint32_t q = A.q, qmask = q - 1;
     const size_t rgsw_words = (size_t)DG * 4 * 1024;
     const bool compat = (A.flags & FHEACC_FLAG_FPGA_COMPAT) != 0;
-    const size_t G = gridDim.x;
 
     // digit tables (ntt_fwd_1024_digit): t1 [BG], t23 [BG], t123 [BG]
     const int BG = A.digit_tables ? 1 << A.bg_bits : 0;
@@ -207,14 +209,21 @@ __global__ void __launch_bounds__(32 * (2 * (DG - 1) + 2), MINB)
     const DigitTables dt{t1, t23, t123};
     __syncthreads();
 
-    for (size_t base = 0; base < A.count; base += G * (size_t)A.group) {
-        const size_t first = base + blockIdx.x;
-        int m = 0;
-        while (m < A.group && first + (size_t)m * G < A.count) m++;
+    // each CTA claims A.group consecutive ciphertexts at a time until none are left
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned long long f = atomicAdd(A.claim_next, (unsigned long long)A.group);
+            claim_first = f;
+            claim_m = f < A.count ? (int)min((unsigned long long)A.group, (unsigned long long)A.count - f) : 0;
+        }
+        __syncthreads();
+        const size_t first = claim_first;
+        const int m = claim_m;
+        if (m == 0) break;
 
         // ---- prologue: LWE_evaluate, residues, acc_initialization (one warp per ciphertext)
         for (int k = warp; k < m; k += NW) {
-            const size_t gid = first + (size_t)k * G;
+            const size_t gid = first + (size_t)k;
             const int g = A.gates[gid];
             const bool x2 = (g == 4 || g == 5);
             const uint64_t *c1 = A.c1 + (A.idx1 ? (size_t)A.idx1[gid] : gid) * (size_t)(n + 1);
@@ -276,7 +285,7 @@ __global__ void __launch_bounds__(32 * (2 * (DG - 1) + 2), MINB)
                 if (ctl[6]) {
                     const int hp = warp - GW;
                     uint32_t x[32];
-                    load_btile(x, A.accs + (first + (size_t)ctl[1] * G) * 2048 + hp * 1024, lane);
+                    load_btile(x, A.accs + (first + (size_t)ctl[1]) * 2048 + hp * 1024, lane);
                     uint32_t *ts = s.tslot[sh][hp];
                     ntt_inv_1024_noscale(x, c, inv_tw, ts, lane);
                     store_row(ts, lane, x);
@@ -299,7 +308,7 @@ __global__ void __launch_bounds__(32 * (2 * (DG - 1) + 2), MINB)
                 const int gk = ctl[3], gs = ctl[2];
                 const uint32_t rr = res[gk * S + gs];
                 const uint4 *key = reinterpret_cast<const uint4 *>(A.btkey + ((size_t)gs * A.Br + rr) * rgsw_words);
-                uint4 *acc = reinterpret_cast<uint4 *>(A.accs + (first + (size_t)gk * G) * 2048);
+                uint4 *acc = reinterpret_cast<uint4 *>(A.accs + (first + (size_t)gk) * 2048);
                 for (int u = threadIdx.x; u < 256; u += 32 * NW)
                     mac_chunk<DG, true>(u, key, s.dbuf, acc, c.Q, A.qinv_neg, acc);
             }
@@ -311,7 +320,7 @@ __global__ void __launch_bounds__(32 * (2 * (DG - 1) + 2), MINB)
         // ---- epilogue: NTT accumulators out, or extraction for the key switch
         for (int t = warp; t < 2 * m; t += NW) {
             const int k = t >> 1, P = t & 1;
-            const size_t gid = first + (size_t)k * G;
+            const size_t gid = first + (size_t)k;
             const uint32_t *acc = A.accs + gid * 2048 + P * 1024;
             uint32_t x[32];
             if (A.extract) {
@@ -369,10 +378,14 @@ static int launch_pipe_dg(Context &c, dev::PipeArgs A, int max_ctas, cudaStream_
     size_t blocks = std::min<size_t>((size_t)sm_count(c) * per_sm, (A.count + 1) / 2);
     if (max_ctas > 0) blocks = std::min<size_t>(blocks, (size_t)max_ctas);
     blocks = std::max<size_t>(blocks, 1);
-    // equal groups: the fewest chunks of at most `cap` ciphertexts per CTA
-    const size_t chunks = (A.count + blocks * cap - 1) / (blocks * cap);
-    A.group = (int)((A.count + blocks * chunks - 1) / (blocks * chunks));
+    // equal claims: the fewest rounds of at most `cap` ciphertexts per CTA
+    const size_t rounds = (A.count + blocks * cap - 1) / (blocks * cap);
+    A.group = (int)((A.count + blocks * rounds - 1) / (blocks * rounds));
     smem = dev::pipe_tables_offset<GW>(A.group, steps) + tables;
+    // claim counter after the accumulators
+    A.claim_next = reinterpret_cast<unsigned long long *>(A.accs + A.count * 2048);
+    e = cudaMemsetAsync(A.claim_next, 0, kClaimWords * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return c.cuda_fail(e, "blind rotation claim reset");
     kern<<<(unsigned)blocks, threads, smem, st>>>(A, c.nc, c.d_fwd_tw, c.d_inv_tw, (uint32_t)((1ULL << 32) / c.p.Q));
     e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "blind rotation launch");
@@ -417,7 +430,7 @@ int launch_blind_rotate32(Context &c, const uint64_t *d_c1, const uint64_t *d_c2
 {
     if (!count) return FHEACC_OK;
     if (!c.d_btkey) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
-    int rc = ensure_scratch(c, c.accs, count * 2048 * sizeof(uint32_t));
+    int rc = ensure_scratch(c, c.accs, bootstrap_accs_bytes(c, count));
     if (rc) return rc;
     dev::PipeArgs A{};
     A.c1 = d_c1; A.c2 = d_c2; A.gates = d_gates; A.count = count;
@@ -431,7 +444,7 @@ int launch_blind_rotate32(Context &c, const uint64_t *d_c1, const uint64_t *d_c2
 namespace fheacc {
 
 // Same launch as launch_blind_rotate32, with the accumulator scratch supplied
-// by the caller (`accs`: count * 2048 u32 words, 16-byte aligned); allocates
+// by the caller (`accs`: bootstrap_accs_bytes, 16-byte aligned); allocates
 // nothing.
 int launch_blind_rotate32_with(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
                                size_t count, uint32_t flags, uint32_t *accs, uint32_t *d_extract, cudaStream_t st)

@@ -189,6 +189,7 @@ struct Br64Args {
     int n, DG;
     uint32_t q, embed, Br, digitR, bg_bits, flags;
     uint64_t gate_constant[8];
+    StepWindow win;            // keeps the CTAs within a few steps of each other (window.cuh)
 };
 
 // 3 CTAs per SM (80 registers): the extra resident warps hide the latency of
@@ -261,8 +262,14 @@ __global__ void __launch_bounds__(kT64, 3) br64_kernel(const __grid_constant__ B
             }
             __syncthreads();
         }
-        // blind rotation, steps outer
-        for (int st = 0; st < S; st++) {
+        // blind rotation, steps outer; thread 0 keeps the step window
+        const unsigned target = (unsigned)(base / (G * (size_t)A.group) + 1) * (unsigned)G;
+        int wcur = 0, won = 1;
+        for (int st = 0; st < S && m > 0; st++) {
+            if (A.win.count && st % A.win.steps == 0) {
+                if (tid == 0) window_enter(A.win, wcur, won, st / A.win.steps, target);
+                __syncthreads();
+            }
             for (int k = 0; k < m; k++) {
                 const uint32_t r = res[k * S + st];
                 if (r == 0 && !compat) continue;
@@ -275,6 +282,7 @@ __global__ void __launch_bounds__(kT64, 3) br64_kernel(const __grid_constant__ B
                 __syncthreads();
             }
         }
+        if (tid == 0) window_enter(A.win, wcur, won, A.win.buckets, target);
         // output
         for (int k = 0; k < m; k++) {
             const size_t gid = first + (size_t)k * G;
@@ -513,6 +521,8 @@ int launch_blind_rotate64_with(Context &c, const uint64_t *d_c1, const uint64_t 
     const size_t chunks = (count + blocks * cap - 1) / (blocks * cap);
     A.group = (int)((count + blocks * chunks - 1) / (blocks * chunks));
     smem = sizeof(dev::Step64Smem) + (size_t)A.group * steps;
+    int rc = prepare_window(c, (int)steps, st, A.win);
+    if (rc) return rc;
     dev::br64_kernel<<<(unsigned)blocks, dev::kT64, smem, st>>>(A, c.d_tw64, c.d_itw64, c.nc64);
     e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "br64 launch");

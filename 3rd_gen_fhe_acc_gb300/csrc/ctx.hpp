@@ -7,6 +7,7 @@
 #include "fheacc.h"
 #include "ntt32.cuh"
 #include "ntt64.cuh"
+#include "window.cuh"
 
 namespace fheacc {
 
@@ -38,7 +39,15 @@ struct Tuning {
     int br_regs_for_3 = -1;   // register budget for 3 CTAs/SM (1 or -1, the default) or 2 (0)
     int br_ctas_per_sm = 0;   // cap on resident CTAs per SM (0: occupancy limit)
     int br_group = 0;         // cap on ciphertexts per CTA and chunk (0: kernel maximum)
+    int br_window = -1;       // 64-bit path: steps per bucket of the step window (0: off; -1: default)
 };
+
+constexpr size_t kClaimWords = 64;   // u32 words of claim counters after the 32-bit accumulators
+
+// Step-window default of the 64-bit path (steps per bucket; a step's key tile,
+// values and Shoup companions, is 18 MB).
+constexpr int kWindowWide = 1;
+constexpr int kWindowCapacity = 4096;   // buckets of the context's counter buffer
 
 // Makes `dev` current for a scope and restores the caller's device.
 struct DeviceGuard {
@@ -98,6 +107,7 @@ struct Context {
     Scratch extract;               // extracted RLWEs between blind rotation and key switch
     Scratch io;                    // device staging for the host-buffer entry points
     Scratch psi;                   // CMUX / blind-rotation / homo_expand intermediates (psi.cu)
+    unsigned *d_window = nullptr;  // step-window counters, kWindowCapacity + 1 (window.cuh)
 
     size_t device_bytes() const
     {
@@ -119,6 +129,10 @@ struct Context {
 // Grows `s` to at least `bytes` (device memory).
 int ensure_scratch(Context &c, Scratch &s, size_t bytes);
 
+// Step window of a blind-rotation launch over `steps` refresh steps: zeroes
+// the context's counters on `st` and fills `w` (w.count null: no window).
+int prepare_window(Context &c, int steps, cudaStream_t st, dev::StepWindow &w);
+
 // launchers (bootstrap32.cu)
 int launch_ntt32(Context &c, uint64_t *d_polys, size_t count, bool inverse, cudaStream_t st);
 // RLWE_mult_RGSW of count accumulators (canonical NTT RLWEs, u64); RGSW i at
@@ -132,7 +146,7 @@ int launch_blind_rotate32(Context &c, const uint64_t *d_c1, const uint64_t *d_c2
                           size_t count, uint32_t flags, uint64_t *d_acc_out, uint32_t *d_extract,
                           int max_ctas, cudaStream_t st);
 // The same blind rotation writing extracted RLWEs, with caller-supplied
-// accumulator scratch (count * 2048 u32 words); performs no allocation.
+// accumulator scratch (bootstrap_accs_bytes); performs no allocation.
 int launch_blind_rotate32_with(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
                                size_t count, uint32_t flags, uint32_t *accs, uint32_t *d_extract, cudaStream_t st);
 // Blind rotation whose gate g reads c1 + idx1[g] * (n+1) and c2 + idx2[g] *
@@ -185,7 +199,7 @@ constexpr size_t kExtract64 = 2048 + 8;        // u64 words per extracted RLWE (
 // accumulators and extracted RLWEs (bytes of each).
 inline size_t bootstrap_accs_bytes(const Context &c, size_t count)
 {
-    return c.wide ? count * 4096 * sizeof(uint64_t) : count * 2048 * sizeof(uint32_t);
+    return c.wide ? count * 4096 * sizeof(uint64_t) : (count * 2048 + kClaimWords) * sizeof(uint32_t);
 }
 inline size_t bootstrap_extract_bytes(const Context &c, size_t count)
 {

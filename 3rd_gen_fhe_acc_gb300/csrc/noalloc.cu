@@ -18,7 +18,7 @@ namespace fheacc {
 // gates: blind-rotation accumulators (2048 words per gate) followed by the
 // extracted RLWEs (kExtractStride words per gate). 776 KiB, held on every GPU
 // that loads the library until the process exits.
-constexpr size_t kNoAllocAccWords = (size_t)FHEACC_NOALLOC_MAX_GATES * 2048;
+constexpr size_t kNoAllocAccWords = (size_t)FHEACC_NOALLOC_MAX_GATES * 2048 + kClaimWords;
 constexpr size_t kNoAllocWords = kNoAllocAccWords + (size_t)FHEACC_NOALLOC_MAX_GATES * kExtractStride;
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWords];
 

@@ -310,7 +310,7 @@ int fheacc_server_create(fheacc_ctx *ctx, size_t max_batch, size_t pool_cipherte
     cudaError_t e = cudaMalloc(&s->d_pool, (size_t)s->slots * s->W * sizeof(uint64_t));
     if (e == cudaSuccess) e = cudaMalloc(&s->d_idx, 4 * max_batch * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMallocHost(&s->h_idx, 4 * max_batch * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&s->d_accs, max_batch * 2048 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_accs, (max_batch * 2048 + kClaimWords) * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMalloc(&s->d_ext, max_batch * kExtractStride * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev, cudaEventDisableTiming);

@@ -214,10 +214,16 @@ int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t cou
  *                             bootstrap key together (its step-outer group;
  *                             0 = the kernel's maximum, 24 for 32-bit words,
  *                             8 for 64-bit); the launch fits equal groups to
- *                             the batch under the cap */
+ *                             the batch under the cap
+ *  FHEACC_OPT_BR_WINDOW     : 64-bit words: steps per bucket of the step
+ *                             window that keeps the CTAs of a launch within
+ *                             two buckets of each other, so that the key tiles
+ *                             they read stay in L2; 0 = off, -1 (default) = 1
+ * Results never depend on the options. */
 #define FHEACC_OPT_BR_REGS_FOR_3  1
 #define FHEACC_OPT_BR_CTAS_PER_SM 2
 #define FHEACC_OPT_BR_GROUP       3
+#define FHEACC_OPT_BR_WINDOW      4
 int fheacc_set_option(fheacc_ctx *ctx, int option, int value);
 
 /* Per-kernel device times (ms) of the most recent call made with
@@ -235,7 +241,7 @@ int fheacc_measure_imad_rate(fheacc_ctx *ctx, double *imad_per_s);
  * parameter sets with the bootstrap key uploaded. */
 int fheacc_measure_components(fheacc_ctx *ctx, double ns[4]);
 
-/* Picks the blind rotation's launch options (the three FHEACC_OPT_BR_* above)
+/* Picks the blind rotation's launch options (the FHEACC_OPT_BR_* above)
  * for batches of `count` gates: times every candidate on a synthetic batch of
  * that size (uniform LWE inputs mod q, the six gates in turn) with this
  * context's keys, and leaves the fastest set on the context. `trials` (may be
@@ -247,6 +253,7 @@ typedef struct fheacc_tune_trial {
     int regs_for_3;    /* FHEACC_OPT_BR_REGS_FOR_3 value */
     int ctas_per_sm;   /* FHEACC_OPT_BR_CTAS_PER_SM value */
     int group;         /* FHEACC_OPT_BR_GROUP value */
+    int window;        /* FHEACC_OPT_BR_WINDOW value */
     float ms;          /* one bootstrap of the synthetic batch, best of two */
 } fheacc_tune_trial;
 int fheacc_autotune(fheacc_ctx *ctx, size_t count, fheacc_tune_trial *trials, int max_trials, int *n_trials);
