@@ -31,6 +31,7 @@ OPT_BR_REGS_FOR_3 = 1
 OPT_BR_CTAS_PER_SM = 2
 OPT_BR_GROUP = 3
 OPT_BR_WINDOW = 4
+OPT_BR_PIPES = 5
 GRAPH_CONCURRENT = 1
 KIND_LWE_SK, KIND_RLWE_SK, KIND_BOOTSTRAP_KEY, KIND_LWE_KS_KEY, KIND_SUBS_KEY, KIND_LWE_CT, KIND_RLWE_CT, \
     KIND_RGSW_CT = range(1, 9)
@@ -74,7 +75,7 @@ class ServerStats(ctypes.Structure):
 
 class TuneTrial(ctypes.Structure):
     _fields_ = [("regs_for_3", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("group", ctypes.c_int32),
-                ("window", ctypes.c_int32), ("ms", ctypes.c_float)]
+                ("window", ctypes.c_int32), ("pipes", ctypes.c_int32), ("ms", ctypes.c_float)]
 
 
 class FheaccError(RuntimeError):

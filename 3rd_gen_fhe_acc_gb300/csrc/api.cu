@@ -721,6 +721,10 @@ int fheacc_set_option(fheacc_ctx *ctx, int option, int value)
         if (value < 0 || value > 64) return c.fail(FHEACC_EINVAL, "group size out of range");
         c.tune.br_group = value;
         return FHEACC_OK;
+    case FHEACC_OPT_BR_PIPES:
+        if (value < 0 || value > 3) return c.fail(FHEACC_EINVAL, "pipelines per CTA must be 0..3");
+        c.tune.br_pipes = value;
+        return FHEACC_OK;
     case FHEACC_OPT_BR_WINDOW:
         if (value < -1 || value > 1024) return c.fail(FHEACC_EINVAL, "step window out of range");
         c.tune.br_window = value;

@@ -92,14 +92,15 @@ template <int NB>
 struct PipeSmem {
     uint32_t tslot[2][2][kN32];   // time-domain accumulators, one slot per pipeline stage
     uint32_t dbuf[NB][kN32];      // digit NTT outputs / transposes of the digit warps
+    int ctl[16];                  // the pipeline's plan for the next period (pipe_schedule)
 };
 
-// Bytes of dynamic shared memory before the digit tables: PipeSmem, then the
-// residue table [group][n * digitR], rounded up to 16.
-template <int NB>
+// Bytes of dynamic shared memory before the digit tables: one PipeSmem per
+// pipeline, then the residue table [group][n * digitR], rounded up to 16.
+template <int NB, int NP>
 __host__ __device__ constexpr size_t pipe_tables_offset(int group, size_t steps)
 {
-    return sizeof(PipeSmem<NB>) + ((size_t)group * steps + 15) / 16 * 16;
+    return NP * sizeof(PipeSmem<NB>) + ((size_t)group * steps + 15) / 16 * 16;
 }
 
 __device__ __forceinline__ void load_btile(uint32_t (&x)[32], const uint32_t *src, int lane)
@@ -131,14 +132,25 @@ __device__ __forceinline__ void store_btile(uint32_t *dst, const uint32_t (&x)[3
                                                                        x[4 * qq + 3]));
 }
 
-// Plans the next pipeline period (run by one thread). ctl: [0, 1] cursor
-// (step, ciphertext) of the last item taken by the inverse-NTT warps; [2, 3]
-// item of the digit warps; [4] slot; [5] cursor exhausted; [6] this period's
-// inverse-NTT item valid; [7] stop. On the first call ctl[6] is 0 and the
-// digit warps have no item. An item whose ciphertext is still held by the
-// digit warps waits one period.
-__device__ __noinline__ void pipe_schedule(int *ctl, const uint8_t *res, int m, int S, bool compat)
+// Plans the next period of one pipeline (run by one thread of it). The
+// pipelines of a CTA share the group's items: a cursor walks the (step,
+// ciphertext) items step-major, and an item is issued only once the previous
+// item of its ciphertext (its last earlier step with a non-zero residue) has
+// finished, which keeps every ciphertext's steps in the reference's order.
+// ctl: [0, 1] item of the inverse-NTT warps; [2, 3] item of the digit warps
+// (ciphertext < 0: none); [4] slot; [5] cursor exhausted; [6] this period's
+// inverse-NTT item valid; [7] stop; [8, 9, 10] claimed item waiting to be
+// issued (step < 0: none) and the step its ciphertext must have finished.
+// done[k]: last finished step of ciphertext k.
+__device__ __noinline__ void pipe_schedule(int *ctl, volatile int *done, int *cursor, const uint8_t *res, int m,
+                                           int S, bool compat)
 {
+    // the digit warps' item of the period just run is finished: its MAC
+    // completed before the pipeline's barrier
+    if (ctl[3] >= 0) {
+        __threadfence_block();
+        done[ctl[3]] = ctl[2];
+    }
     // the inverse-NTT item of the period just run moves to the digit warps
     if (ctl[6]) {
         ctl[2] = ctl[0];
@@ -147,50 +159,66 @@ __device__ __noinline__ void pipe_schedule(int *ctl, const uint8_t *res, int m, 
         ctl[2] = -1;
         ctl[3] = -1;
     }
-    int ns = ctl[0], nk = ctl[1];
-    bool found = false;
-    if (!ctl[5]) {
+    if (ctl[8] < 0 && !ctl[5]) {
         for (;;) {
-            if (++nk == m) {
-                nk = 0;
-                ++ns;
+            const int idx = atomicAdd(cursor, 1);
+            if (idx >= S * m) {
+                ctl[5] = 1;
+                break;
             }
-            if (ns >= S) break;
-            if (compat || res[nk * S + ns]) {
-                found = true;
+            const int st = idx / m, k = idx - st * m;
+            if (compat || res[k * S + st]) {
+                int prev = st - 1;
+                if (!compat)
+                    while (prev >= 0 && !res[k * S + prev]) prev--;
+                ctl[8] = st;
+                ctl[9] = k;
+                ctl[10] = prev;
                 break;
             }
         }
-        if (!found) ctl[5] = 1;
     }
-    const bool hv = found && !(ctl[3] >= 0 && ctl[3] == nk);
+    const bool hv = ctl[8] >= 0 && done[ctl[9]] == ctl[10];
     if (hv) {
-        ctl[0] = ns;
-        ctl[1] = nk;
+        __threadfence_block();
+        ctl[0] = ctl[8];
+        ctl[1] = ctl[9];
+        ctl[8] = -1;
     }
     ctl[6] = hv;
-    ctl[7] = !hv && ctl[3] < 0 && ctl[5];
+    ctl[7] = !hv && ctl[8] < 0 && ctl[3] < 0 && ctl[5];
     // slot: the inverse-NTT warps alternate slots every period
     ctl[4] ^= 1;
 }
 
-// 2 (digitG - 1) digit warps (the last digit's NTT comes from the
-// accumulator) and 2 inverse-NTT warps; all warps share the MAC.
-template <int DG, int MINB>
-__global__ void __launch_bounds__(32 * (2 * (DG - 1) + 2), MINB)
+__device__ __forceinline__ void pipe_barrier(int id, int threads)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
+// NP pipelines per CTA, each of 2 (digitG - 1) digit warps (the last digit's
+// NTT comes from the accumulator) and 2 inverse-NTT warps, all of whose warps
+// share the MAC; pipeline p synchronises on named barrier 1 + p.
+template <int DG, int NP, int MINB>
+__global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
     br32_pipe_kernel(const __grid_constant__ PipeArgs A, const __grid_constant__ Ntt32Consts c,
                      const uint2 *__restrict__ fwd_tw, const uint2 *__restrict__ inv_tw, uint32_t mu32)
 {
     constexpr int DT = DG - 1;   // digit NTTs per poly
     constexpr int GW = 2 * DT;   // digit warps
     constexpr int NW = GW + 2;   // plus the two inverse-NTT warps
+    constexpr int PT = 32 * NW;  // threads of a pipeline
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    PipeSmem<GW> &s = *reinterpret_cast<PipeSmem<GW> *>(smem_raw);
-    uint8_t *res = smem_raw + sizeof(PipeSmem<GW>);   // [group][n * digitR] residues
-    __shared__ int ctl[8];
+    PipeSmem<GW> *pipes = reinterpret_cast<PipeSmem<GW> *>(smem_raw);
+    uint8_t *res = smem_raw + NP * sizeof(PipeSmem<GW>);   // [group][n * digitR] residues
+    __shared__ int done[kMaxGroup * NP];
+    __shared__ int cursor;
     __shared__ unsigned long long claim_first;
     __shared__ int claim_m;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int pl = warp / NW, pw = warp - pl * NW;
+    PipeSmem<GW> &s = pipes[pl];
+    int *ctl = s.ctl;
     const int n = A.n, S = n * (int)A.digitR;
     const uint32_t q = A.q, qmask = q - 1;
     const size_t rgsw_words = (size_t)DG * 4 * 1024;
@@ -198,7 +226,7 @@ __global__ void __launch_bounds__(32 * (2 * (DG - 1) + 2), MINB)
 
     // digit tables (ntt_fwd_1024_digit): t1 [BG], t23 [BG], t123 [BG]
     const int BG = A.digit_tables ? 1 << A.bg_bits : 0;
-    uint32_t *t1 = reinterpret_cast<uint32_t *>(smem_raw + pipe_tables_offset<GW>(A.group, S));
+    uint32_t *t1 = reinterpret_cast<uint32_t *>(smem_raw + pipe_tables_offset<GW, NP>(A.group, S));
     uint2 *t23 = reinterpret_cast<uint2 *>(t1 + BG), *t123 = t23 + BG;
     for (int y = threadIdx.x; y < BG; y += blockDim.x) {
         const uint64_t Q = c.Q;
@@ -222,7 +250,7 @@ __global__ void __launch_bounds__(32 * (2 * (DG - 1) + 2), MINB)
         if (m == 0) break;
 
         // ---- prologue: LWE_evaluate, residues, acc_initialization (one warp per ciphertext)
-        for (int k = warp; k < m; k += NW) {
+        for (int k = warp; k < m; k += NP * NW) {
             const size_t gid = first + (size_t)k;
             const int g = A.gates[gid];
             const bool x2 = (g == 4 || g == 5);
@@ -253,8 +281,7 @@ __global__ void __launch_bounds__(32 * (2 * (DG - 1) + 2), MINB)
                 }
                 x[r] = v;
             }
-            uint32_t *buf = warp < GW ? s.dbuf[warp] : s.tslot[0][warp - GW];
-            ntt_fwd_1024(x, c, fwd_tw, buf, lane);
+            ntt_fwd_1024(x, c, fwd_tw, pw < GW ? s.dbuf[pw] : s.tslot[0][pw - GW], lane);
 #pragma unroll
             for (int r = 0; r < 32; r++) x[r] = reduce32(x[r], mu32, c.Q);
             uint32_t *acc = A.accs + gid * 2048;
@@ -264,26 +291,29 @@ __global__ void __launch_bounds__(32 * (2 * (DG - 1) + 2), MINB)
             for (int qq = 0; qq < 8; qq++) __stcg(a4 + qq * 32 + lane, make_uint4(0, 0, 0, 0));
             __syncwarp();
         }
-        __syncthreads();
-
-        // ---- pipeline over the (step, ciphertext) items of the group. Thread 0
-        // schedules: it picks the next item of the inverse-NTT warps after each
-        // period and publishes the period's plan in shared memory.
-        if (threadIdx.x == 0) {
-            ctl[0] = 0; ctl[1] = -1;      // cursor (step, ciphertext) of the last item taken
+        if (threadIdx.x == 0) cursor = 0;
+        for (int k = threadIdx.x; k < m; k += blockDim.x) done[k] = -1;
+        if (pw == 0 && lane == 0) {
+            ctl[0] = 0; ctl[1] = -1;      // item of the inverse-NTT warps
             ctl[2] = -1; ctl[3] = -1;     // item of the digit warps (ciphertext < 0: none)
             ctl[4] = 0;                   // slot written by the inverse-NTT warps
-            ctl[5] = m == 0;              // no more items for the inverse-NTT warps
+            ctl[5] = 0;                   // cursor exhausted
             ctl[6] = 0; ctl[7] = 0;       // this period: inverse-NTT item valid, stop
-            pipe_schedule(ctl, res, m, S, compat);
+            ctl[8] = -1;                  // no claimed item waiting
         }
         __syncthreads();
+
+        // ---- NP pipelines over the (step, ciphertext) items of the group. One
+        // thread of each plans the pipeline's next period after each period
+        // and publishes the plan in shared memory.
+        if (pw == 0 && lane == 0) pipe_schedule(ctl, done, &cursor, res, m, S, compat);
+        pipe_barrier(1 + pl, PT);
         for (;;) {
             if (ctl[7]) break;
             const int sh = ctl[4];
-            if (warp >= GW) {
+            if (pw >= GW) {
                 if (ctl[6]) {
-                    const int hp = warp - GW;
+                    const int hp = pw - GW;
                     uint32_t x[32];
                     load_btile(x, A.accs + (first + (size_t)ctl[1]) * 2048 + hp * 1024, lane);
                     uint32_t *ts = s.tslot[sh][hp];
@@ -291,34 +321,35 @@ __global__ void __launch_bounds__(32 * (2 * (DG - 1) + 2), MINB)
                     store_row(ts, lane, x);
                 }
             } else if (ctl[3] >= 0) {
-                const int p = warp / DT, h = warp % DT;
+                const int p = pw / DT, h = pw % DT;
                 const uint32_t shift = A.bg_bits * h, mask = (1u << A.bg_bits) - 1;
                 uint32_t x[32];
                 load_row(x, s.tslot[sh ^ 1][p], lane);
 #pragma unroll
                 for (int r = 0; r < 32; r++) x[r] = (x[r] >> shift) & mask;
-                if (A.digit_tables) ntt_fwd_1024_digit(x, c, fwd_tw, s.dbuf[warp], dt, lane);
-                else ntt_fwd_1024(x, c, fwd_tw, s.dbuf[warp], lane);
-                store_row(s.dbuf[warp], lane, x);
+                if (A.digit_tables) ntt_fwd_1024_digit(x, c, fwd_tw, s.dbuf[pw], dt, lane);
+                else ntt_fwd_1024(x, c, fwd_tw, s.dbuf[pw], lane);
+                store_row(s.dbuf[pw], lane, x);
             }
-            // all warps multiply-accumulate the digit warps' item once its digit
-            // NTTs are in shared memory
-            __syncthreads();
+            // all warps of the pipeline multiply-accumulate the digit warps'
+            // item once its digit NTTs are in shared memory
+            pipe_barrier(1 + pl, PT);
             if (ctl[3] >= 0) {
                 const int gk = ctl[3], gs = ctl[2];
                 const uint32_t rr = res[gk * S + gs];
                 const uint4 *key = reinterpret_cast<const uint4 *>(A.btkey + ((size_t)gs * A.Br + rr) * rgsw_words);
                 uint4 *acc = reinterpret_cast<uint4 *>(A.accs + (first + (size_t)gk) * 2048);
-                for (int u = threadIdx.x; u < 256; u += 32 * NW)
+                for (int u = pw * 32 + lane; u < 256; u += PT)
                     mac_chunk<DG, true>(u, key, s.dbuf, acc, c.Q, A.qinv_neg, acc);
             }
-            __syncthreads();
-            if (threadIdx.x == 0) pipe_schedule(ctl, res, m, S, compat);
-            __syncthreads();
+            pipe_barrier(1 + pl, PT);
+            if (pw == 0 && lane == 0) pipe_schedule(ctl, done, &cursor, res, m, S, compat);
+            pipe_barrier(1 + pl, PT);
         }
+        __syncthreads();
 
         // ---- epilogue: NTT accumulators out, or extraction for the key switch
-        for (int t = warp; t < 2 * m; t += NW) {
+        for (int t = warp; t < 2 * m; t += NP * NW) {
             const int k = t >> 1, P = t & 1;
             const size_t gid = first + (size_t)k;
             const uint32_t *acc = A.accs + gid * 2048 + P * 1024;
@@ -326,8 +357,7 @@ __global__ void __launch_bounds__(32 * (2 * (DG - 1) + 2), MINB)
             if (A.extract) {
                 if (P == 0) load_btile_reversed(x, acc, lane);
                 else load_btile(x, acc, lane);
-                uint32_t *buf = warp < GW ? s.dbuf[warp] : s.tslot[0][warp - GW];
-                ntt_inv_1024_noscale(x, c, inv_tw, buf, lane);
+                ntt_inv_1024_noscale(x, c, inv_tw, pw < GW ? s.dbuf[pw] : s.tslot[0][pw - GW], lane);
                 uint32_t *ext = A.extract + gid * kExtractStride;
                 if (P == 0) {
 #pragma unroll
@@ -358,30 +388,35 @@ static int sm_count(Context &c)
     return v > 0 ? v : 1;
 }
 
-template <int DG, int MINB>
+template <int DG, int NP, int MINB>
 static int launch_pipe_dg(Context &c, dev::PipeArgs A, int max_ctas, cudaStream_t st)
 {
     constexpr int GW = 2 * (DG - 1);
-    constexpr int threads = 32 * (GW + 2);
-    auto kern = dev::br32_pipe_kernel<DG, MINB>;
+    constexpr int threads = NP * 32 * (GW + 2);
+    auto kern = dev::br32_pipe_kernel<DG, NP, MINB>;
     const size_t steps = (size_t)c.p.n * c.p.digitR, tables = A.digit_tables ? 20 * ((size_t)1 << c.p.BG_bits) : 0;
-    const int cap = c.tune.br_group > 0 ? std::min(c.tune.br_group, dev::kMaxGroup) : dev::kMaxGroup;
+    // group cap: kMaxGroup (or the tuned cap) per pipeline, within the shared memory of one CTA
+    int cap = NP * (c.tune.br_group > 0 ? std::min(c.tune.br_group, dev::kMaxGroup) : dev::kMaxGroup);
+    const size_t fixed = dev::pipe_tables_offset<GW, NP>(0, steps) + tables + 16;
+    if (fixed + (size_t)cap * steps > kPipeSmemBudget)
+        cap = fixed < kPipeSmemBudget ? (int)((kPipeSmemBudget - fixed) / steps) : 0;
+    if (cap < 1) return c.fail(FHEACC_EINVAL, "n * digitR too large for the blind rotation's residue table");
     // residency with the largest group allowed; the group is then fitted to the batch
-    size_t smem = dev::pipe_tables_offset<GW>(cap, steps) + tables;
+    size_t smem = dev::pipe_tables_offset<GW, NP>(cap, steps) + tables;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return c.cuda_fail(e, "blind rotation smem attribute");
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
     if (per_sm < 1) per_sm = 1;
     if (c.tune.br_ctas_per_sm > 0) per_sm = std::min(per_sm, c.tune.br_ctas_per_sm);
-    // at least two ciphertexts per CTA keep both pipeline stages busy
-    size_t blocks = std::min<size_t>((size_t)sm_count(c) * per_sm, (A.count + 1) / 2);
+    // at least two ciphertexts per pipeline keep both of its stages busy
+    size_t blocks = std::min<size_t>((size_t)sm_count(c) * per_sm, (A.count + 2 * NP - 1) / (2 * NP));
     if (max_ctas > 0) blocks = std::min<size_t>(blocks, (size_t)max_ctas);
     blocks = std::max<size_t>(blocks, 1);
     // equal claims: the fewest rounds of at most `cap` ciphertexts per CTA
     const size_t rounds = (A.count + blocks * cap - 1) / (blocks * cap);
     A.group = (int)((A.count + blocks * rounds - 1) / (blocks * rounds));
-    smem = dev::pipe_tables_offset<GW>(A.group, steps) + tables;
+    smem = dev::pipe_tables_offset<GW, NP>(A.group, steps) + tables;
     // claim counter after the accumulators
     A.claim_next = reinterpret_cast<unsigned long long *>(A.accs + A.count * 2048);
     e = cudaMemsetAsync(A.claim_next, 0, kClaimWords * sizeof(uint32_t), st);
@@ -389,6 +424,21 @@ static int launch_pipe_dg(Context &c, dev::PipeArgs A, int max_ctas, cudaStream_
     kern<<<(unsigned)blocks, threads, smem, st>>>(A, c.nc, c.d_fwd_tw, c.d_inv_tw, (uint32_t)((1ULL << 32) / c.p.Q));
     e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "blind rotation launch");
+}
+
+// Pipelines per CTA. By default from the gates per SM (one GB300, 4096-gate
+// key set): up to 2 a single pipeline per SM is fastest (its items do not
+// wait on other pipelines), up to 5 two pipelines, beyond that three.
+template <int DG>
+static int launch_pipe_shape(Context &c, const dev::PipeArgs &A, int max_ctas, cudaStream_t st)
+{
+    const size_t sms = (size_t)sm_count(c);
+    const int np = c.tune.br_pipes > 0 ? c.tune.br_pipes : A.count <= 2 * sms ? 1 : A.count <= 5 * sms ? 2 : 3;
+    if (np == 3) return launch_pipe_dg<DG, 3, 1>(c, A, max_ctas, st);
+    if (np == 2) return launch_pipe_dg<DG, 2, 1>(c, A, max_ctas, st);
+    // one pipeline per CTA: the register budget of 3 (default) or 2 CTAs per SM
+    return c.tune.br_regs_for_3 != 0 ? launch_pipe_dg<DG, 1, 3>(c, A, max_ctas, st)
+                                     : launch_pipe_dg<DG, 1, 2>(c, A, max_ctas, st);
 }
 
 // Parameter-set fields of PipeArgs.
@@ -415,11 +465,10 @@ static int launch_pipe(Context &c, const dev::PipeArgs &A, int max_ctas, cudaStr
     // parameter validation makes the gadget cover Q, which the last-digit
     // identity of the kernel needs
     if (!A.derive_last) return c.fail(FHEACC_EINVAL, "gadget base^digitG must exceed Q");
-    const bool three = c.tune.br_regs_for_3 != 0;   // -1 (default) or 1: 3 CTAs per SM
     switch (c.p.digitG) {
-    case 2: return three ? launch_pipe_dg<2, 3>(c, A, max_ctas, st) : launch_pipe_dg<2, 2>(c, A, max_ctas, st);
-    case 3: return three ? launch_pipe_dg<3, 3>(c, A, max_ctas, st) : launch_pipe_dg<3, 2>(c, A, max_ctas, st);
-    case 4: return three ? launch_pipe_dg<4, 3>(c, A, max_ctas, st) : launch_pipe_dg<4, 2>(c, A, max_ctas, st);
+    case 2: return launch_pipe_shape<2>(c, A, max_ctas, st);
+    case 3: return launch_pipe_shape<3>(c, A, max_ctas, st);
+    case 4: return launch_pipe_shape<4>(c, A, max_ctas, st);
     default: return c.fail(FHEACC_EINVAL, "digitG must be 2..4 for the 32-bit path");
     }
 }

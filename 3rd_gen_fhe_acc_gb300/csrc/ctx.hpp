@@ -40,7 +40,10 @@ struct Tuning {
     int br_ctas_per_sm = 0;   // cap on resident CTAs per SM (0: occupancy limit)
     int br_group = 0;         // cap on ciphertexts per CTA and chunk (0: kernel maximum)
     int br_window = -1;       // 64-bit path: steps per bucket of the step window (0: off; -1: default)
+    int br_pipes = 0;         // 32-bit path: pipelines per CTA, 1..3 (0: by gates per SM)
 };
+
+constexpr size_t kPipeSmemBudget = 220 * 1024;   // dynamic shared memory of one blind-rotation CTA
 
 constexpr size_t kClaimWords = 64;   // u32 words of claim counters after the 32-bit accumulators
 

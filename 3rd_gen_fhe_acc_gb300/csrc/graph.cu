@@ -248,19 +248,20 @@ int fheacc_autotune(fheacc_ctx *ctx, size_t count, fheacc_tune_trial *trials, in
     const int32_t *dgates = (const int32_t *)(d + off_g);
     uint64_t *dout = (uint64_t *)(d + off_o);
     // candidates: (register budget for 3 CTAs/SM, CTAs per SM cap, group cap,
-    // steps per bucket of the step window)
+    // steps per bucket of the step window, pipelines per CTA)
     struct Cand {
-        int regs3, ctas, group, window;
+        int regs3, ctas, group, window, pipes;
     };
     std::vector<Cand> cands;
     if (c.wide) {
         for (int ctas : {0, 1})
-            for (int group : {0, 2, 4}) cands.push_back({0, ctas, group, -1});
-        for (int window : {0, 2, 4}) cands.push_back({0, 0, 0, window});
+            for (int group : {0, 2, 4}) cands.push_back({0, ctas, group, -1, 0});
+        for (int window : {0, 2, 4}) cands.push_back({0, 0, 0, window, 0});
     } else {
+        for (int group : {0, 6, 12}) cands.push_back({-1, 0, group, -1, 3});
+        cands.push_back({-1, 0, 0, -1, 2});
         for (int regs3 : {0, 1})
-            for (int ctas : {0, 1})
-                for (int group : {0, 6, 12}) cands.push_back({regs3, ctas, group, -1});
+            for (int group : {0, 12}) cands.push_back({regs3, 0, group, -1, 1});
     }
     const Tuning saved = c.tune;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -276,6 +277,7 @@ int fheacc_autotune(fheacc_ctx *ctx, size_t count, fheacc_tune_trial *trials, in
         c.tune.br_ctas_per_sm = k.ctas;
         c.tune.br_group = k.group;
         c.tune.br_window = k.window;
+        c.tune.br_pipes = k.pipes;
         float t = 1e30f;
         for (int rep = 0; rep < 3 && !rc; rep++) {
             cudaEventRecord(e0, c.stream);
@@ -289,7 +291,7 @@ int fheacc_autotune(fheacc_ctx *ctx, size_t count, fheacc_tune_trial *trials, in
             if (!rc && rep > 0 && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) t = std::min(t, ms);
         }
         if (rc) break;
-        if (trials && nt < max_trials) trials[nt] = {k.regs3, k.ctas, k.group, k.window, t};
+        if (trials && nt < max_trials) trials[nt] = {k.regs3, k.ctas, k.group, k.window, k.pipes, t};
         nt++;
         if (t < best) {
             best = t;

@@ -370,7 +370,7 @@ def run_mixed(args):
         S["tuned_ms"] = alone(S)
         S["tuned_same"] = np.array_equal(S["dout"].cpu().numpy().view(np.uint64), S["ref_out"])
         best = min(S["trials"], key=lambda t: t["ms"])
-        S["best"] = {k: best[k] for k in ("regs_for_3", "ctas_per_sm", "group", "window")}
+        S["best"] = {k: best[k] for k in ("regs_for_3", "ctas_per_sm", "group", "window", "pipes")}
 
     graph = F.Graph()
     for S in sets:

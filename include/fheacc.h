@@ -219,11 +219,18 @@ int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t cou
  *                             window that keeps the CTAs of a launch within
  *                             two buckets of each other, so that the key tiles
  *                             they read stay in L2; 0 = off, -1 (default) = 1
+ *  FHEACC_OPT_BR_PIPES      : 32-bit words: pipelines per CTA (1..3; 0 =
+ *                             default: 1 up to 2 gates per SM, 2 up to 5,
+ *                             else 3). The pipelines of a CTA share its group
+ *                             of ciphertexts item by item, so they finish
+ *                             together; with one pipeline per CTA, up to 3
+ *                             CTAs share an SM and finish at different times.
  * Results never depend on the options. */
 #define FHEACC_OPT_BR_REGS_FOR_3  1
 #define FHEACC_OPT_BR_CTAS_PER_SM 2
 #define FHEACC_OPT_BR_GROUP       3
 #define FHEACC_OPT_BR_WINDOW      4
+#define FHEACC_OPT_BR_PIPES       5
 int fheacc_set_option(fheacc_ctx *ctx, int option, int value);
 
 /* Per-kernel device times (ms) of the most recent call made with
@@ -254,6 +261,7 @@ typedef struct fheacc_tune_trial {
     int ctas_per_sm;   /* FHEACC_OPT_BR_CTAS_PER_SM value */
     int group;         /* FHEACC_OPT_BR_GROUP value */
     int window;        /* FHEACC_OPT_BR_WINDOW value */
+    int pipes;         /* FHEACC_OPT_BR_PIPES value */
     float ms;          /* one bootstrap of the synthetic batch, best of two */
 } fheacc_tune_trial;
 int fheacc_autotune(fheacc_ctx *ctx, size_t count, fheacc_tune_trial *trials, int max_trials, int *n_trials);

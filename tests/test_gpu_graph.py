@@ -116,15 +116,17 @@ def test_autotune_keeps_results(F, small, cuda_ok):
     assert len(trials) >= 4 and all(t["ms"] > 0 for t in trials)
     after = direct(torch, ctx, d, 300)
     assert np.array_equal(before, after) and np.array_equal(ks.decrypt(after), truth)
-    assert {t["window"] for t in trials} >= {-1, 0}
+    assert {t["pipes"] for t in trials} >= {1, 3}
     # every tried shape gives the same words
     for t in trials:
         ctx.set_option(F.OPT_BR_REGS_FOR_3, t["regs_for_3"])
         ctx.set_option(F.OPT_BR_CTAS_PER_SM, t["ctas_per_sm"])
         ctx.set_option(F.OPT_BR_GROUP, t["group"])
         ctx.set_option(F.OPT_BR_WINDOW, t["window"])
+        ctx.set_option(F.OPT_BR_PIPES, t["pipes"])
         assert np.array_equal(direct(torch, ctx, d, 300), before)
     ctx.set_option(F.OPT_BR_REGS_FOR_3, -1)   # back to the defaults
     ctx.set_option(F.OPT_BR_WINDOW, -1)
+    ctx.set_option(F.OPT_BR_PIPES, 0)
     for o in (F.OPT_BR_CTAS_PER_SM, F.OPT_BR_GROUP):
         ctx.set_option(o, 0)

@@ -1,7 +1,7 @@
 """Every instantiation of the 32-bit blind-rotation kernel on the GPU, against
 the oracle: digitG = 2, 3 and 4 (the last digit taken from the accumulator),
-each with both register budgets, and a gadget base above the digit-table
-limit. Parameter validation rejects gadgets with BG^digitG <= Q, so those need
+each with 1 (both register budgets), 2 and 3 pipelines per CTA, and a gadget
+base above the digit-table limit. Parameter validation rejects gadgets with BG^digitG <= Q, so those need
 no kernel. Small n keeps key generation and the oracle quick."""
 import numpy as np
 import pytest
@@ -43,7 +43,10 @@ def test_kernel_instantiations(F, cuda_ok, bg_bits, digit_g, decrypts):
         ctx.upload_bootstrap_key(ks.btkey)
         ctx.upload_keyswitch_key(ks.kskey)
         outs = []
-        for regs3 in (0, 1):   # both register budgets (2 and 3 CTAs per SM)
+        # every launch shape: 1 pipeline per CTA with the register budget of 2
+        # or 3 CTAs per SM, 2 and 3 pipelines per CTA
+        for pipes, regs3 in ((1, 0), (1, 1), (2, -1), (3, -1)):
+            ctx.set_option(F.OPT_BR_PIPES, pipes)
             ctx.set_option(F.OPT_BR_REGS_FOR_3, regs3)
             outs.append(ctx.eval_bootstrap_batch(c1, c2, g))
     finally:
