@@ -204,9 +204,9 @@ def run_reference(args):
 
 def profile_case(preset=0):
     """The case the committed ncu section captures use: the bench parameter
-    set with n = 64 (same per-step work), 608 random gates (one wave of the
-    persistent grid; 912 for the 64-bit set), two batched launches, outputs
-    checked by decryption."""
+    set with n = 64 (same per-step work), 912 random gates (6 per SM: the
+    3-pipeline shape of the 32-bit kernel, one wave of the 64-bit grid), two
+    batched launches, outputs checked by decryption."""
     import torch
     import __graft_entry__
     __graft_entry__.build_product()
@@ -220,7 +220,7 @@ def profile_case(preset=0):
     ctx = F.Context(P, 0)
     ctx.upload_bootstrap_key(F.bootstrap_key(P, 3, lsk, rsk))
     ctx.upload_keyswitch_key(F.keyswitch_key(P, 4, rsk, lsk))
-    B = 608 if P.N == 1024 else 912
+    B = 912
     rng = np.random.default_rng(0)
     bits = rng.integers(0, 2, 2 * B).astype(np.uint8)
     c = F.LWE_encrypt(P, 9, lsk, bits)
