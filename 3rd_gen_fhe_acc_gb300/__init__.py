@@ -151,6 +151,7 @@ def lib():
             "fheacc_lwe_keyswitch_async": (ctypes.c_int, [vp, vp, sz, vp, vp]),
             "fheacc_lwe_modswitch_async": (ctypes.c_int, [vp, vp, sz, vp, vp]),
             "fheacc_sync": (ctypes.c_int, [vp, ctypes.c_uint32]),
+            "fheacc_device_status": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_uint32)]),
             "fheacc_kernel_times": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_float)]),
             "fheacc_set_option": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
             "fheacc_measure_imad_rate": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
@@ -484,6 +485,13 @@ class Context:
 
     def sync(self, timeout_ms=0):
         self.check(lib().fheacc_sync(self._h, timeout_ms))
+
+    def device_status(self):
+        """Status bits of the context's finished device work (read and cleared);
+        raises FheaccError when a kernel flagged its results invalid."""
+        bits = ctypes.c_uint32()
+        self.check(lib().fheacc_device_status(self._h, ctypes.byref(bits)))
+        return bits.value
 
     def set_option(self, option, value):
         self.check(lib().fheacc_set_option(self._h, option, value))

@@ -36,6 +36,20 @@ int ensure_scratch(Context &c, Scratch &s, size_t bytes)
     return FHEACC_OK;
 }
 
+// Reads and clears the device status word after the context's work finished;
+// a set bit means a kernel abandoned a bounded wait and its results are invalid.
+static int take_device_status(Context &c, uint32_t *bits)
+{
+    uint32_t v = 0;
+    cudaError_t e = cudaMemcpy(&v, c.d_status, sizeof(v), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && v) e = cudaMemset(c.d_status, 0, sizeof(v));
+    if (e != cudaSuccess) return c.cuda_fail(e, "device status");
+    if (bits) *bits = v;
+    if (v & kStatusWaitLimit)
+        return c.fail(FHEACC_EIO, "a blind-rotation worker gave up a bounded wait on another worker; results invalid");
+    return FHEACC_OK;
+}
+
 int prepare_window(Context &c, int steps, cudaStream_t st, dev::StepWindow &w)
 {
     w = dev::StepWindow{};
@@ -302,7 +316,11 @@ int fheacc_create(const fheacc_params *p, int device, fheacc_ctx **out)
         fheacc_destroy(reinterpret_cast<fheacc_ctx *>(c));
         return FHEACC_EIO;
     }
-    e = cudaMalloc(&c->d_window, (kWindowCapacity + 1) * sizeof(unsigned));
+    e = cudaMalloc(&c->d_window, (kWindowCapacity + 2) * sizeof(unsigned));
+    if (e == cudaSuccess) {
+        c->d_status = c->d_window + kWindowCapacity + 1;
+        e = cudaMemset(c->d_status, 0, sizeof(unsigned));
+    }
     if (e != cudaSuccess) {
         g_create_error = std::string("step-window counters: ") + cudaGetErrorString(e);
         fheacc_destroy(reinterpret_cast<fheacc_ctx *>(c));
@@ -631,7 +649,8 @@ int fheacc_bootstrap(fheacc_ctx *ctx, const uint64_t *c1, const uint64_t *c2, co
     if (rc) return rc;
     e = cudaMemcpyAsync(out, d_out, lwe_bytes, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "bootstrap");
+    if (e != cudaSuccess) return c.cuda_fail(e, "bootstrap");
+    return take_device_status(c, nullptr);
 }
 
 int fheacc_ntt_forward(fheacc_ctx *ctx, uint64_t *d_polys, size_t count, void *stream)
@@ -845,6 +864,14 @@ int fheacc_expand_rlwe(fheacc_ctx *ctx, const uint64_t *d_in, uint64_t *d_out, v
     return mark_done(c, st, expand_device(c, d_in, d_out, st));
 }
 
+int fheacc_device_status(fheacc_ctx *ctx, uint32_t *bits)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    DeviceGuard g(c.device);
+    return take_device_status(c, bits);
+}
+
 int fheacc_sync(fheacc_ctx *ctx, uint32_t timeout_ms)
 {
     if (!ctx) return FHEACC_EINVAL;
@@ -854,7 +881,7 @@ int fheacc_sync(fheacc_ctx *ctx, uint32_t timeout_ms)
     for (;;) {
         cudaError_t e = cudaStreamQuery(c.stream);
         if (e == cudaSuccess) e = cudaEventQuery(c.done);
-        if (e == cudaSuccess) return FHEACC_OK;
+        if (e == cudaSuccess) return take_device_status(c, nullptr);
         if (e != cudaErrorNotReady) return c.cuda_fail(e, "sync");
         if (timeout_ms) {
             auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();

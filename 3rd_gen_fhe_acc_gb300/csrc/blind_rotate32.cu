@@ -83,7 +83,12 @@ struct PipeArgs {
     uint32_t digit_tables;     // first two digit-NTT stages by table lookup (BG <= kMaxTableBG)
     uint64_t gate_constant[8];
     unsigned long long *claim_next;   // next unclaimed ciphertext (zeroed before the launch)
+    unsigned *status;                 // set to kStatusWaitLimit if a pipeline gave up waiting
 };
+
+// Periods a pipeline idles with a claimed item whose ciphertext's previous step
+// another pipeline still holds, before it gives up and flags the launch.
+constexpr int kIdleLimit = 1 << 22;
 
 // Shared memory of one CTA. tslot holds lane-major copies of the inverse-NTT
 // warps' registers (layout A), dbuf the digit NTT outputs as swizzled rows
@@ -140,10 +145,11 @@ __device__ __forceinline__ void store_btile(uint32_t *dst, const uint32_t (&x)[3
 // ctl: [0, 1] item of the inverse-NTT warps; [2, 3] item of the digit warps
 // (ciphertext < 0: none); [4] slot; [5] cursor exhausted; [6] this period's
 // inverse-NTT item valid; [7] stop; [8, 9, 10] claimed item waiting to be
-// issued (step < 0: none) and the step its ciphertext must have finished.
-// done[k]: last finished step of ciphertext k.
+// issued (step < 0: none) and the step its ciphertext must have finished;
+// [11] periods idled in a row waiting for it. done[k]: last finished step of
+// ciphertext k.
 __device__ __noinline__ void pipe_schedule(int *ctl, volatile int *done, int *cursor, const uint8_t *res, int m,
-                                           int S, bool compat)
+                                           int S, bool compat, unsigned *status)
 {
     // the digit warps' item of the period just run is finished: its MAC
     // completed before the pipeline's barrier
@@ -184,6 +190,14 @@ __device__ __noinline__ void pipe_schedule(int *ctl, volatile int *done, int *cu
         ctl[0] = ctl[8];
         ctl[1] = ctl[9];
         ctl[8] = -1;
+    }
+    // a wait on another pipeline ends within a few periods; one that does not
+    // is abandoned (bounded wait) and flagged
+    ctl[11] = (!hv && ctl[3] < 0 && ctl[8] >= 0) ? ctl[11] + 1 : 0;
+    if (ctl[11] > kIdleLimit) {
+        atomicOr(status, kStatusWaitLimit);
+        ctl[8] = -1;
+        ctl[5] = 1;
     }
     ctl[6] = hv;
     ctl[7] = !hv && ctl[8] < 0 && ctl[3] < 0 && ctl[5];
@@ -300,13 +314,14 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
             ctl[5] = 0;                   // cursor exhausted
             ctl[6] = 0; ctl[7] = 0;       // this period: inverse-NTT item valid, stop
             ctl[8] = -1;                  // no claimed item waiting
+            ctl[11] = 0;                  // idle periods in a row
         }
         __syncthreads();
 
         // ---- NP pipelines over the (step, ciphertext) items of the group. One
         // thread of each plans the pipeline's next period after each period
         // and publishes the plan in shared memory.
-        if (pw == 0 && lane == 0) pipe_schedule(ctl, done, &cursor, res, m, S, compat);
+        if (pw == 0 && lane == 0) pipe_schedule(ctl, done, &cursor, res, m, S, compat, A.status);
         pipe_barrier(1 + pl, PT);
         for (;;) {
             if (ctl[7]) break;
@@ -343,7 +358,7 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
                     mac_chunk<DG, true>(u, key, s.dbuf, acc, c.Q, A.qinv_neg, acc);
             }
             pipe_barrier(1 + pl, PT);
-            if (pw == 0 && lane == 0) pipe_schedule(ctl, done, &cursor, res, m, S, compat);
+            if (pw == 0 && lane == 0) pipe_schedule(ctl, done, &cursor, res, m, S, compat, A.status);
             pipe_barrier(1 + pl, PT);
         }
         __syncthreads();
@@ -456,6 +471,7 @@ static void fill_pipe_params(Context &c, dev::PipeArgs &A, uint32_t flags)
     A.w21 = (uint32_t)((uint64_t)c.nc.fw[2] * c.nc.fw[1] % Q);
     A.w31 = (uint32_t)((uint64_t)c.nc.fw[3] * c.nc.fw[1] % Q);
     A.derive_last = c.dp.last_digit_from_acc;
+    A.status = c.d_status;
     A.digit_tables = (1u << c.p.BG_bits) <= (uint32_t)dev::kMaxTableBG;
     for (int i = 0; i < 8; i++) A.gate_constant[i] = c.dp.gate_constant[i];
 }

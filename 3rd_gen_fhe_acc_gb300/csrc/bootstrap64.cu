@@ -33,18 +33,20 @@ struct Step64Smem {
 };
 
 // One RLWE x RGSW step on s.acc (NTT domain, values < 2Q) with the key
-// `key` (Shoup pairs, [digitG][2][2][2048]).
+// `key` (Shoup pairs, [digitG][2][2][2048]), run by the 256 threads tid of a
+// worker that synchronises on named barrier `bar` (its two 128-thread groups
+// on bar + 1 and bar + 2).
 // With acc_nd (the step's NTT-domain accumulator in global memory, read before
 // it is overwritten) the last digit's NTT is replaced by the accumulator: the
 // keys were uploaded with K'_h = K_h - BG^(h-DG+1) K_last, K'_last =
 // BG^-(DG-1) K_last (Q < BG^DG, so sum_h BG^h NTT(digit_h) = acc).
 __device__ __forceinline__ void step64(Step64Smem &s, const ulonglong2 *__restrict__ key, int DG, uint32_t bg_bits,
                                        const ulonglong2 *__restrict__ tw, const ulonglong2 *__restrict__ itw,
-                                       const Ntt64Consts &c, const uint64_t *acc_nd = nullptr)
+                                       const Ntt64Consts &c, const uint64_t *acc_nd, int tid, int bar)
 {
-    const int tid = threadIdx.x, grp = tid >> 7, gtid = tid & 127;
-    ntt64_inv_2048<128>(s.acc[grp], itw, c, gtid, 1 + grp);
-    __syncthreads();
+    const int grp = tid >> 7, gtid = tid & 127;
+    ntt64_inv_2048<128>(s.acc[grp], itw, c, gtid, bar + 1 + grp);
+    group_sync(bar, kT64);
     uint64_t sa[8], sb[8];
 #pragma unroll
     for (int i = 0; i < 8; i++) sa[i] = sb[i] = 0;
@@ -53,9 +55,9 @@ __device__ __forceinline__ void step64(Step64Smem &s, const ulonglong2 *__restri
     for (int h = 0; h < DH; h++) {
         const uint32_t sh = bg_bits * h;
         for (int e = gtid; e < 2048; e += 128) s.buf[grp][e] = (s.acc[grp][e] >> sh) & mask;
-        group_sync(1 + grp, 128);
-        ntt64_fwd_2048<128>(s.buf[grp], tw, c, gtid, 1 + grp);
-        __syncthreads();
+        group_sync(bar + 1 + grp, 128);
+        ntt64_fwd_2048<128>(s.buf[grp], tw, c, gtid, bar + 1 + grp);
+        group_sync(bar, kT64);
         const ulonglong2 *k0 = key + (size_t)(h * 2 + 0) * 2 * 2048;   // row c_text[h][0]: times digit of a
         const ulonglong2 *k1 = key + (size_t)(h * 2 + 1) * 2 * 2048;   // row c_text[h][1]: times digit of b
 #pragma unroll
@@ -67,7 +69,7 @@ __device__ __forceinline__ void step64(Step64Smem &s, const ulonglong2 *__restri
             sa[i] += shoup64(da, a0.x, a0.y, c.Q) + shoup64(db, a1.x, a1.y, c.Q);
             sb[i] += shoup64(da, b0.x, b0.y, c.Q) + shoup64(db, b1.x, b1.y, c.Q);
         }
-        __syncthreads();
+        group_sync(bar, kT64);
     }
     if (acc_nd) {
         const ulonglong2 *k0 = key + (size_t)((DG - 1) * 2 + 0) * 2 * 2048;
@@ -88,7 +90,7 @@ __device__ __forceinline__ void step64(Step64Smem &s, const ulonglong2 *__restri
         s.acc[0][k] = barrett64_2q(sa[i], c.mu64, c.Q);
         s.acc[1][k] = barrett64_2q(sb[i], c.mu64, c.Q);
     }
-    __syncthreads();
+    group_sync(bar, kT64);
 }
 
 // Forward / inverse NTT of count polys (u64, canonical in and out), one
@@ -167,7 +169,7 @@ __global__ void __launch_bounds__(kT64) rlwe_mult_rgsw64_kernel(const uint64_t *
     for (size_t ci = blockIdx.x; ci < count; ci += gridDim.x) {
         for (int e = threadIdx.x; e < 4096; e += kT64) s.acc[e >> 11][e & 2047] = acc_in[ci * 4096 + e];
         __syncthreads();
-        step64(s, rgsw + ci * rgsw_stride, DG, bg_bits, tw, itw, c);
+        step64(s, rgsw + ci * rgsw_stride, DG, bg_bits, tw, itw, c, nullptr, threadIdx.x, 1);
         for (int e = threadIdx.x; e < 4096; e += kT64) {
             const uint64_t v = s.acc[e >> 11][e & 2047];
             acc_out[ci * 4096 + e] = v >= c.Q ? v - c.Q : v;
@@ -184,43 +186,73 @@ struct Br64Args {
     uint64_t *accs;            // scratch [count][2][2048], NTT domain, values < 2Q
     uint64_t *acc_out;         // optional canonical NTT accumulators [count][4096]
     uint64_t *extract;         // optional [count][kExtract64]
-    int group;                 // ciphertexts per CTA and chunk (<= kMaxGroup64)
+    int group;                 // ciphertexts per claim (<= kMaxGroup64 per worker)
     int derive_last;           // last digit's NTT from the accumulator (DevParams::last_digit_from_acc)
     int n, DG;
     uint32_t q, embed, Br, digitR, bg_bits, flags;
     uint64_t gate_constant[8];
     StepWindow win;            // keeps the CTAs within a few steps of each other (window.cuh)
+    unsigned long long *claim_next;   // next unclaimed ciphertext (zeroed before the launch)
+    unsigned *status;          // set to kStatusWaitLimit if a worker gave up waiting
 };
 
-// 3 CTAs per SM (80 registers): the extra resident warps hide the latency of
-// the key stream better than the spill-free 2-CTA register allocation (862 vs 1028 ms for
-// 2048 gates). An XOR swizzle of the shared-memory passes removed their bank
+// Polls of a worker waiting for another worker's step of the same ciphertext
+// (about 60 ns each) before it gives up and flags the launch.
+constexpr unsigned kWorkerWaitLimit = 1u << 26;
+
+// W workers of 256 threads per CTA (W = 1: 3 CTAs per SM, 80 registers; the
+// extra resident warps hide the latency of the key stream better than the
+// spill-free 2-CTA register allocation, 862 vs 1028 ms for 2048 gates). Each
+// CTA claims groups of consecutive ciphertexts; its workers share the group's
+// (step, ciphertext) items through a cursor that walks them step-major, and a
+// worker issues an item once the previous item of its ciphertext (its last
+// earlier step with a non-zero residue) has finished, so every ciphertext's
+// steps keep the reference's order and the workers finish together. Worker w
+// synchronises on named barrier 1 + 3w (its two 128-thread groups on 2 + 3w and
+// 3 + 3w). An XOR swizzle of the shared-memory passes removed their bank
 // conflicts but cost more in index arithmetic than it saved.
-__global__ void __launch_bounds__(kT64, 3) br64_kernel(const __grid_constant__ Br64Args A,
-                                                   const ulonglong2 *__restrict__ tw, const ulonglong2 *__restrict__ itw,
-                                                   const __grid_constant__ Ntt64Consts c)
+template <int W, int MINB>
+__global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_constant__ Br64Args A,
+                                                          const ulonglong2 *__restrict__ tw,
+                                                          const ulonglong2 *__restrict__ itw,
+                                                          const __grid_constant__ Ntt64Consts c)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    Step64Smem &s = *reinterpret_cast<Step64Smem *>(smem_raw);
-    uint8_t *res = smem_raw + sizeof(Step64Smem);   // [group][n * digitR]
-    __shared__ uint32_t bvals[kMaxGroup64], b1s[kMaxGroup64], b2s[kMaxGroup64];
-    const int tid = threadIdx.x;
+    uint8_t *res = smem_raw + W * sizeof(Step64Smem);   // [group][n * digitR]
+    __shared__ uint32_t bvals[kMaxGroup64 * W], b1s[kMaxGroup64 * W], b2s[kMaxGroup64 * W];
+    __shared__ int done[kMaxGroup64 * W];
+    __shared__ int plan[W][2];
+    __shared__ int cursor, wcur, won;
+    __shared__ unsigned long long claim_first;
+    __shared__ int claim_m;
+    const int wk = threadIdx.x / kT64, tid = threadIdx.x - wk * kT64, bar = 1 + 3 * wk;
+    Step64Smem &s = reinterpret_cast<Step64Smem *>(smem_raw)[wk];
     const int n = A.n, S = n * (int)A.digitR;
     const uint32_t q = A.q, qmask = q - 1;
     const size_t rgsw_pairs = (size_t)A.DG * 4 * 2048;
     const bool compat = (A.flags & FHEACC_FLAG_FPGA_COMPAT) != 0;
-    const size_t G = gridDim.x;
-    for (size_t base = 0; base < A.count; base += G * (size_t)A.group) {
-        const size_t first = base + blockIdx.x;
-        int m = 0;
-        while (m < A.group && first + (size_t)m * G < A.count) m++;
+    const unsigned target = gridDim.x;   // the window is used with one round of claims
+    if (threadIdx.x == 0) {
+        wcur = 0;
+        won = 1;
+    }
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned long long f = atomicAdd(A.claim_next, (unsigned long long)A.group);
+            claim_first = f;
+            claim_m = f < A.count ? (int)min((unsigned long long)A.group, (unsigned long long)A.count - f) : 0;
+        }
+        __syncthreads();
+        const size_t first = claim_first;
+        const int m = claim_m;
+        if (m == 0) break;
         // LWE_evaluate and residues
         for (int k = 0; k < m; k++) {
-            const size_t gid = first + (size_t)k * G;
+            const size_t gid = first + (size_t)k;
             const int g = A.gates[gid];
             const bool x2 = (g == 4 || g == 5);
             const uint64_t *c1 = A.c1 + gid * (size_t)(n + 1), *c2 = A.c2 + gid * (size_t)(n + 1);
-            for (int i = tid; i <= n; i += kT64) {
+            for (int i = threadIdx.x; i <= n; i += blockDim.x) {
                 const uint64_t v = x2 ? 2 * (c1[i] - c2[i]) : c1[i] + c2[i];
                 if (i < n) {
                     uint32_t nega = (q - (uint32_t)(v & qmask)) & qmask;
@@ -236,10 +268,13 @@ __global__ void __launch_bounds__(kT64, 3) br64_kernel(const __grid_constant__ B
                 }
             }
         }
+        for (int k = threadIdx.x; k < m; k += blockDim.x) done[k] = -1;
+        if (threadIdx.x == 0) cursor = 0;
         __syncthreads();
-        // acc_initialization: a = 0, b = test vector, forward NTT (group 1 transforms b)
-        for (int k = 0; k < m; k++) {
-            const size_t gid = first + (size_t)k * G;
+        // acc_initialization, one ciphertext per worker: a = 0, b = test vector,
+        // forward NTT (the worker's group 1 transforms b)
+        for (int k = wk; k < m; k += W) {
+            const size_t gid = first + (size_t)k;
             const uint64_t Q8 = c.Q / 8 + 1, negQ8 = c.Q - Q8;
             const uint32_t b1 = b1s[k], b2 = b2s[k], val = bvals[k];
             for (int e = tid; e < 2048; e += kT64) {
@@ -251,41 +286,83 @@ __global__ void __launch_bounds__(kT64, 3) br64_kernel(const __grid_constant__ B
                 }
                 s.buf[1][e] = v;
             }
-            __syncthreads();
-            if (tid >= 128) ntt64_fwd_2048<128>(s.buf[1], tw, c, tid - 128, 2);
-            __syncthreads();
+            group_sync(bar, kT64);
+            if (tid >= 128) ntt64_fwd_2048<128>(s.buf[1], tw, c, tid - 128, bar + 2);
+            group_sync(bar, kT64);
             uint64_t *acc = A.accs + gid * 4096;
             for (int e = tid; e < 2048; e += kT64) {
                 acc[e] = 0;
                 uint64_t v = barrett64_2q(s.buf[1][e], c.mu64, c.Q);
                 acc[2048 + e] = v >= c.Q ? v - c.Q : v;
             }
-            __syncthreads();
+            group_sync(bar, kT64);
         }
-        // blind rotation, steps outer; thread 0 keeps the step window
-        const unsigned target = (unsigned)(base / (G * (size_t)A.group) + 1) * (unsigned)G;
-        int wcur = 0, won = 1;
-        for (int st = 0; st < S && m > 0; st++) {
-            if (A.win.count && st % A.win.steps == 0) {
-                if (tid == 0) window_enter(A.win, wcur, won, st / A.win.steps, target);
-                __syncthreads();
+        __syncthreads();
+        // blind rotation: the workers take the group's items from the cursor
+        for (;;) {
+            if (tid == 0) {
+                int st = -1, k = -1, prev = -1;
+                for (;;) {
+                    const int idx = atomicAdd(&cursor, 1);
+                    if (idx >= S * m) break;
+                    const int s_ = idx / m, k_ = idx - s_ * m;
+                    if (compat || res[k_ * S + s_]) {
+                        st = s_;
+                        k = k_;
+                        prev = st - 1;
+                        if (!compat)
+                            while (prev >= 0 && !res[k * S + prev]) prev--;
+                        break;
+                    }
+                }
+                if (st >= 0 && A.win.count) {
+                    // step window: count this CTA into the buckets it has left, then
+                    // wait for the slowest CTA
+                    const int b = st / A.win.steps;
+                    const int old = atomicMax(&wcur, b);
+                    for (int x = old; x < b; x++) atomicAdd(A.win.count + x, 1u);
+                    int on = won;
+                    int cur = b;
+                    window_enter(A.win, cur, on, b, target);
+                    if (!on) won = 0;
+                }
+                if (st >= 0) {
+                    // the previous item of the ciphertext must have finished
+                    const volatile int *dk = done + k;
+                    unsigned polls = 0;
+                    while (*dk != prev) {
+                        if (++polls > kWorkerWaitLimit) {
+                            atomicOr(A.status, kStatusWaitLimit);
+                            st = -1;
+                            break;
+                        }
+                        __nanosleep(32);
+                    }
+                    __threadfence_block();
+                }
+                plan[wk][0] = st;
+                plan[wk][1] = k;
             }
-            for (int k = 0; k < m; k++) {
-                const uint32_t r = res[k * S + st];
-                if (r == 0 && !compat) continue;
-                uint64_t *acc = A.accs + (first + (size_t)k * G) * 4096;
-                for (int e = tid; e < 4096; e += kT64) s.acc[e >> 11][e & 2047] = __ldcg(acc + e);
-                __syncthreads();
-                step64(s, A.btkey + ((size_t)st * A.Br + r) * rgsw_pairs, A.DG, A.bg_bits, tw, itw, c,
-                       A.derive_last ? acc : nullptr);
-                for (int e = tid; e < 4096; e += kT64) __stcg(acc + e, s.acc[e >> 11][e & 2047]);
-                __syncthreads();
+            group_sync(bar, kT64);
+            const int st = plan[wk][0], k = plan[wk][1];
+            if (st < 0) break;
+            const uint32_t r = res[k * S + st];
+            uint64_t *acc = A.accs + (first + (size_t)k) * 4096;
+            for (int e = tid; e < 4096; e += kT64) s.acc[e >> 11][e & 2047] = __ldcg(acc + e);
+            group_sync(bar, kT64);
+            step64(s, A.btkey + ((size_t)st * A.Br + r) * rgsw_pairs, A.DG, A.bg_bits, tw, itw, c,
+                   A.derive_last ? acc : nullptr, tid, bar);
+            for (int e = tid; e < 4096; e += kT64) __stcg(acc + e, s.acc[e >> 11][e & 2047]);
+            group_sync(bar, kT64);
+            if (tid == 0) {
+                __threadfence_block();
+                done[k] = st;
             }
         }
-        if (tid == 0) window_enter(A.win, wcur, won, A.win.buckets, target);
-        // output
-        for (int k = 0; k < m; k++) {
-            const size_t gid = first + (size_t)k * G;
+        __syncthreads();
+        // output, one ciphertext per worker
+        for (int k = wk; k < m; k += W) {
+            const size_t gid = first + (size_t)k;
             const uint64_t *acc = A.accs + gid * 4096;
             if (A.extract) {
                 // NTT_a_transpose on poly a, then inverse NTT of both polys
@@ -293,9 +370,9 @@ __global__ void __launch_bounds__(kT64, 3) br64_kernel(const __grid_constant__ B
                     s.acc[0][e] = __ldcg(acc + 2047 - e);
                     s.acc[1][e] = __ldcg(acc + 2048 + e);
                 }
-                __syncthreads();
-                ntt64_inv_2048<128>(s.acc[tid >> 7], itw, c, tid & 127, 1 + (tid >> 7));
-                __syncthreads();
+                group_sync(bar, kT64);
+                ntt64_inv_2048<128>(s.acc[tid >> 7], itw, c, tid & 127, bar + 1 + (tid >> 7));
+                group_sync(bar, kT64);
                 uint64_t *ext = A.extract + gid * kExtract64;
                 for (int e = tid; e < 2048; e += kT64) ext[e] = s.acc[0][e];
                 if (tid == 0) ext[2048] = s.acc[1][0];
@@ -305,8 +382,14 @@ __global__ void __launch_bounds__(kT64, 3) br64_kernel(const __grid_constant__ B
                     A.acc_out[gid * 4096 + e] = v >= c.Q ? v - c.Q : v;
                 }
             }
-            __syncthreads();
+            group_sync(bar, kT64);
         }
+        __syncthreads();
+    }
+    // a CTA counts into every bucket it has not counted into yet
+    if (threadIdx.x == 0 && A.win.count) {
+        const int old = atomicMax(&wcur, A.win.buckets);
+        for (int x = old; x < A.win.buckets; x++) atomicAdd(A.win.count + x, 1u);
     }
 }
 
@@ -487,10 +570,47 @@ int launch_blind_rotate64(Context &c, const uint64_t *d_c1, const uint64_t *d_c2
 {
     if (!count) return FHEACC_OK;
     if (!c.d_btkey64) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
-    int rc = ensure_scratch(c, c.accs, count * 4096 * sizeof(uint64_t));
+    int rc = ensure_scratch(c, c.accs, bootstrap_accs_bytes(c, count));
     if (rc) return rc;
     return launch_blind_rotate64_with(c, d_c1, d_c2, d_gates, count, flags, (uint64_t *)c.accs.ptr, d_acc_out,
                                       d_extract, max_ctas, st);
+}
+
+template <int W, int MINB>
+static int launch_br64_shape(Context &c, dev::Br64Args A, int max_ctas, cudaStream_t st)
+{
+    auto kern = dev::br64_kernel<W, MINB>;
+    const size_t steps = (size_t)c.p.n * c.p.digitR;
+    // group cap: kMaxGroup64 (or the tuned cap) per worker, within the shared memory of one CTA
+    int cap = W * (c.tune.br_group > 0 ? std::min(c.tune.br_group, dev::kMaxGroup64) : dev::kMaxGroup64);
+    const size_t fixed = W * sizeof(dev::Step64Smem) + 16;
+    if (fixed + (size_t)cap * steps > kPipeSmemBudget)
+        cap = fixed < kPipeSmemBudget ? (int)((kPipeSmemBudget - fixed) / steps) : 0;
+    if (cap < 1) return c.fail(FHEACC_EINVAL, "n * digitR too large for the blind rotation's residue table");
+    size_t smem = W * sizeof(dev::Step64Smem) + (size_t)cap * steps;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return c.cuda_fail(e, "br64 smem attribute");
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, W * dev::kT64, smem);
+    if (per_sm < 1) per_sm = 1;
+    if (c.tune.br_ctas_per_sm > 0) per_sm = std::min(per_sm, c.tune.br_ctas_per_sm);
+    size_t blocks = std::min<size_t>((size_t)sms_of(c) * per_sm, (A.count + W - 1) / W);
+    if (max_ctas > 0) blocks = std::min<size_t>(blocks, (size_t)max_ctas);
+    blocks = std::max<size_t>(blocks, 1);
+    // equal claims: the fewest rounds of at most `cap` ciphertexts per CTA
+    const size_t rounds = (A.count + blocks * cap - 1) / (blocks * cap);
+    A.group = (int)((A.count + blocks * rounds - 1) / (blocks * rounds));
+    smem = W * sizeof(dev::Step64Smem) + (size_t)A.group * steps;
+    // claim counter after the accumulators
+    A.claim_next = reinterpret_cast<unsigned long long *>(A.accs + A.count * 4096);
+    e = cudaMemsetAsync(A.claim_next, 0, kClaimWords * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return c.cuda_fail(e, "br64 claim reset");
+    // the window's per-bucket targets assume one round of claims
+    int rc = rounds == 1 ? prepare_window(c, (int)steps, st, A.win) : FHEACC_OK;
+    if (rc) return rc;
+    kern<<<(unsigned)blocks, W * dev::kT64, smem, st>>>(A, c.d_tw64, c.d_itw64, c.nc64);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "br64 launch");
 }
 
 int launch_blind_rotate64_with(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
@@ -504,28 +624,16 @@ int launch_blind_rotate64_with(Context &c, const uint64_t *d_c1, const uint64_t 
     A.btkey = c.d_btkey64; A.accs = accs; A.acc_out = d_acc_out; A.extract = d_extract;
     A.n = c.p.n; A.DG = (int)c.p.digitG; A.q = c.p.q; A.embed = c.dp.embed; A.Br = c.p.Br; A.digitR = c.p.digitR;
     A.bg_bits = c.p.BG_bits; A.flags = flags; A.derive_last = (int)c.dp.last_digit_from_acc;
+    A.status = c.d_status;
     for (int i = 0; i < 8; i++) A.gate_constant[i] = c.dp.gate_constant[i];
-    const int cap = c.tune.br_group > 0 ? std::min(c.tune.br_group, dev::kMaxGroup64) : dev::kMaxGroup64;
-    const size_t steps = (size_t)c.p.n * c.p.digitR;
-    size_t smem = sizeof(dev::Step64Smem) + (size_t)cap * steps;
-    cudaError_t e = cudaFuncSetAttribute(dev::br64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return c.cuda_fail(e, "br64 smem attribute");
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dev::br64_kernel, dev::kT64, smem);
-    if (per_sm < 1) per_sm = 1;
-    if (c.tune.br_ctas_per_sm > 0) per_sm = std::min(per_sm, c.tune.br_ctas_per_sm);
-    size_t blocks = std::min<size_t>((size_t)sms_of(c) * per_sm, count);
-    if (max_ctas > 0) blocks = std::min<size_t>(blocks, (size_t)max_ctas);
-    blocks = std::max<size_t>(blocks, 1);
-    // equal groups: the fewest chunks of at most `cap` ciphertexts per CTA
-    const size_t chunks = (count + blocks * cap - 1) / (blocks * cap);
-    A.group = (int)((count + blocks * chunks - 1) / (blocks * chunks));
-    smem = sizeof(dev::Step64Smem) + (size_t)A.group * steps;
-    int rc = prepare_window(c, (int)steps, st, A.win);
-    if (rc) return rc;
-    dev::br64_kernel<<<(unsigned)blocks, dev::kT64, smem, st>>>(A, c.d_tw64, c.d_itw64, c.nc64);
-    e = cudaGetLastError();
-    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "br64 launch");
+    // workers per CTA, by default from the gates per SM (one GB300, 2048-gate
+    // batches and smaller): up to 1 one worker per CTA (3 CTAs per SM), up to 3
+    // two workers, beyond that three (700 gates: 305 / 247 / 235 ms)
+    const size_t sms = (size_t)sms_of(c);
+    const int w = c.tune.br_pipes > 0 ? c.tune.br_pipes : count <= sms ? 1 : count <= 3 * sms ? 2 : 3;
+    if (w == 3) return launch_br64_shape<3, 1>(c, A, max_ctas, st);
+    if (w == 2) return launch_br64_shape<2, 1>(c, A, max_ctas, st);
+    return launch_br64_shape<1, 3>(c, A, max_ctas, st);
 }
 
 int launch_extract64(Context &c, const uint64_t *d_rlwe, size_t count, uint64_t *d_extract, cudaStream_t st)

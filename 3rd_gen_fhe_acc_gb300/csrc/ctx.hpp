@@ -45,7 +45,10 @@ struct Tuning {
 
 constexpr size_t kPipeSmemBudget = 220 * 1024;   // dynamic shared memory of one blind-rotation CTA
 
-constexpr size_t kClaimWords = 64;   // u32 words of claim counters after the 32-bit accumulators
+constexpr size_t kClaimWords = 64;   // u32 words of claim counters after the blind-rotation accumulators
+// Device status bits (Context::d_status): a kernel that gave up a bounded wait
+// on another worker of its CTA sets kStatusWaitLimit; its results are not valid.
+constexpr unsigned kStatusWaitLimit = FHEACC_STATUS_WAIT_LIMIT;
 
 // Step-window default of the 64-bit path (steps per bucket; a step's key tile,
 // values and Shoup companions, is 18 MB).
@@ -111,6 +114,7 @@ struct Context {
     Scratch io;                    // device staging for the host-buffer entry points
     Scratch psi;                   // CMUX / blind-rotation / homo_expand intermediates (psi.cu)
     unsigned *d_window = nullptr;  // step-window counters, kWindowCapacity + 1 (window.cuh)
+    unsigned *d_status = nullptr;  // device status word (kStatus*), after the window counters
 
     size_t device_bytes() const
     {
@@ -202,7 +206,8 @@ constexpr size_t kExtract64 = 2048 + 8;        // u64 words per extracted RLWE (
 // accumulators and extracted RLWEs (bytes of each).
 inline size_t bootstrap_accs_bytes(const Context &c, size_t count)
 {
-    return c.wide ? count * 4096 * sizeof(uint64_t) : (count * 2048 + kClaimWords) * sizeof(uint32_t);
+    return c.wide ? count * 4096 * sizeof(uint64_t) + kClaimWords * sizeof(uint32_t)
+                  : (count * 2048 + kClaimWords) * sizeof(uint32_t);
 }
 inline size_t bootstrap_extract_bytes(const Context &c, size_t count)
 {

@@ -219,11 +219,12 @@ int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t cou
  *                             window that keeps the CTAs of a launch within
  *                             two buckets of each other, so that the key tiles
  *                             they read stay in L2; 0 = off, -1 (default) = 1
- *  FHEACC_OPT_BR_PIPES      : 32-bit words: pipelines per CTA (1..3; 0 =
- *                             default: 1 up to 2 gates per SM, 2 up to 5,
- *                             else 3). The pipelines of a CTA share its group
- *                             of ciphertexts item by item, so they finish
- *                             together; with one pipeline per CTA, up to 3
+ *  FHEACC_OPT_BR_PIPES      : pipelines (32-bit words) or workers (64-bit)
+ *                             per CTA, 1..3; 0 = default: 32-bit 1 up to 2
+ *                             gates per SM, 2 up to 5, else 3; 64-bit 1 up to
+ *                             1 gate per SM, 2 up to 3, else 3. The pipelines of a CTA
+ *                             share its group of ciphertexts item by item, so
+ *                             they finish together; with one per CTA, up to 3
  *                             CTAs share an SM and finish at different times.
  * Results never depend on the options. */
 #define FHEACC_OPT_BR_REGS_FOR_3  1
@@ -388,8 +389,19 @@ int fheacc_subs_keyswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t co
 int fheacc_expand_rlwe(fheacc_ctx *ctx, const uint64_t *d_in, uint64_t *d_out, void *stream);
 
 /* Wait until the most recent asynchronous call of the context (and every
- * blocking call) has finished, at most timeout_ms (0 = no limit). */
+ * blocking call) has finished, at most timeout_ms (0 = no limit). Returns
+ * FHEACC_EIO if a kernel of the context flagged its results invalid (see
+ * fheacc_device_status). */
 int fheacc_sync(fheacc_ctx *ctx, uint32_t timeout_ms);
+
+/* Device status of the context, read and cleared (call after the work has
+ * finished). Bit FHEACC_STATUS_WAIT_LIMIT: a blind-rotation worker gave up a
+ * bounded wait on another worker of its CTA (every such wait ends within a few
+ * steps by construction; the bound keeps a fault from hanging the GPU), and
+ * the launch's results are invalid; the call then returns FHEACC_EIO.
+ * fheacc_bootstrap and fheacc_sync check it themselves. */
+#define FHEACC_STATUS_WAIT_LIMIT 1u
+int fheacc_device_status(fheacc_ctx *ctx, uint32_t *bits);
 
 #ifdef __cplusplus
 }

@@ -79,3 +79,27 @@ def test_wide_blind_rotate(F, ctx1, keys1, cuda_ok):
         want, steps = keys1.oracle.blind_rotate(c1[i], c2[i], int(g[i]), keys1.btkey)
         assert steps > 1150
         assert np.array_equal(got[i], want)
+
+
+_want12 = {}
+
+
+@pytest.mark.parametrize("pipes,window", [(1, -1), (1, 0), (2, -1), (3, -1), (3, 0), (3, 4)])
+def test_wide_worker_shapes(F, ctx1, keys1, pipes, window):
+    """Every launch shape of the 64-bit blind rotation (1, 2 or 3 workers per
+    CTA sharing a group item by item; step window on and off) gives the
+    oracle's words."""
+    x, y, g, c1, c2 = random_gate_batch(keys1, 12, seed=9)
+    if "w" not in _want12:
+        want, failed = keys1.oracle.eval_bootstrap_batch(c1, c2, g, keys1.btkey, keys1.kskey)
+        assert failed == 0
+        _want12["w"] = want
+    ctx1.set_option(F.OPT_BR_PIPES, pipes)
+    ctx1.set_option(F.OPT_BR_WINDOW, window)
+    try:
+        out = ctx1.eval_bootstrap_batch(c1, c2, g)
+        assert ctx1.device_status() == 0
+    finally:
+        ctx1.set_option(F.OPT_BR_PIPES, 0)
+        ctx1.set_option(F.OPT_BR_WINDOW, -1)
+    assert np.array_equal(out, _want12["w"])
