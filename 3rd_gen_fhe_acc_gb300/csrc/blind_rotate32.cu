@@ -97,7 +97,7 @@ template <int NB>
 struct PipeSmem {
     uint32_t tslot[2][2][kN32];   // time-domain accumulators, one slot per pipeline stage
     uint32_t dbuf[NB][kN32];      // digit NTT outputs / transposes of the digit warps
-    int ctl[16];                  // the pipeline's plan for the next period (pipe_schedule)
+    int ctl[2][16];               // the pipeline's plans, one per period parity (pipe_plan)
 };
 
 // Bytes of dynamic shared memory before the digit tables: one PipeSmem per
@@ -137,39 +137,36 @@ __device__ __forceinline__ void store_btile(uint32_t *dst, const uint32_t (&x)[3
                                                                        x[4 * qq + 3]));
 }
 
-// Plans the next period of one pipeline (run by one thread of it). The
-// pipelines of a CTA share the group's items: a cursor walks the (step,
-// ciphertext) items step-major, and an item is issued only once the previous
-// item of its ciphertext (its last earlier step with a non-zero residue) has
-// finished, which keeps every ciphertext's steps in the reference's order.
-// ctl: [0, 1] item of the inverse-NTT warps; [2, 3] item of the digit warps
-// (ciphertext < 0: none); [4] slot; [5] cursor exhausted; [6] this period's
-// inverse-NTT item valid; [7] stop; [8, 9, 10] claimed item waiting to be
-// issued (step < 0: none) and the step its ciphertext must have finished;
-// [11] periods idled in a row waiting for it. done[k]: last finished step of
-// ciphertext k.
-__device__ __noinline__ void pipe_schedule(int *ctl, volatile int *done, int *cursor, const uint8_t *res, int m,
-                                           int S, bool compat, unsigned *status)
+// Plans period t + 1 of one pipeline (run by one thread of it while the other
+// threads multiply-accumulate period t's digit item). C is period t's plan, Nx
+// receives the next. The pipelines of a CTA share the group's items: a cursor
+// walks the (step, ciphertext) items step-major, and an item is issued only
+// once the previous item of its ciphertext (its last earlier step with a
+// non-zero residue) has finished, which keeps every ciphertext's steps in the
+// reference's order. The digit item of period t finishes before period t + 1
+// starts, so an item that follows it may be issued for period t + 1; the
+// planning thread marks it finished (done[]) for the other pipelines after
+// the MAC barrier.
+// Plan: [0, 1] item of the inverse-NTT warps; [2, 3] item of the digit warps
+// (ciphertext < 0: none); [4] slot; [5] cursor exhausted; [6] inverse-NTT
+// item valid; [7] stop; [8, 9, 10] claimed item waiting to be issued (step < 0:
+// none) and the step its ciphertext must have finished; [11] periods idled in
+// a row waiting for it. done[k]: last finished step of ciphertext k.
+__device__ __noinline__ void pipe_plan(const int *C, int *Nx, volatile int *done, int *cursor, const uint8_t *res,
+                                       int m, int S, bool compat, unsigned *status)
 {
-    // the digit warps' item of the period just run is finished: its MAC
-    // completed before the pipeline's barrier
-    if (ctl[3] >= 0) {
-        __threadfence_block();
-        done[ctl[3]] = ctl[2];
-    }
-    // the inverse-NTT item of the period just run moves to the digit warps
-    if (ctl[6]) {
-        ctl[2] = ctl[0];
-        ctl[3] = ctl[1];
-    } else {
-        ctl[2] = -1;
-        ctl[3] = -1;
-    }
-    if (ctl[8] < 0 && !ctl[5]) {
+    // period t's inverse-NTT item moves to the digit warps
+    Nx[2] = C[6] ? C[0] : -1;
+    Nx[3] = C[6] ? C[1] : -1;
+    Nx[5] = C[5];
+    Nx[8] = C[8];
+    Nx[9] = C[9];
+    Nx[10] = C[10];
+    if (Nx[8] < 0 && !Nx[5]) {
         for (;;) {
             const int idx = atomicAdd(cursor, 1);
             if (idx >= S * m) {
-                ctl[5] = 1;
+                Nx[5] = 1;
                 break;
             }
             const int st = idx / m, k = idx - st * m;
@@ -177,32 +174,35 @@ __device__ __noinline__ void pipe_schedule(int *ctl, volatile int *done, int *cu
                 int prev = st - 1;
                 if (!compat)
                     while (prev >= 0 && !res[k * S + prev]) prev--;
-                ctl[8] = st;
-                ctl[9] = k;
-                ctl[10] = prev;
+                Nx[8] = st;
+                Nx[9] = k;
+                Nx[10] = prev;
                 break;
             }
         }
     }
-    const bool hv = ctl[8] >= 0 && done[ctl[9]] == ctl[10];
+    const bool hv = Nx[8] >= 0 && (done[Nx[9]] == Nx[10] || (Nx[9] == C[3] && Nx[10] == C[2]));
     if (hv) {
         __threadfence_block();
-        ctl[0] = ctl[8];
-        ctl[1] = ctl[9];
-        ctl[8] = -1;
+        Nx[0] = Nx[8];
+        Nx[1] = Nx[9];
+        Nx[8] = -1;
+    } else {
+        Nx[0] = 0;
+        Nx[1] = -1;
     }
     // a wait on another pipeline ends within a few periods; one that does not
     // is abandoned (bounded wait) and flagged
-    ctl[11] = (!hv && ctl[3] < 0 && ctl[8] >= 0) ? ctl[11] + 1 : 0;
-    if (ctl[11] > kIdleLimit) {
+    Nx[11] = (!hv && Nx[3] < 0 && Nx[8] >= 0) ? C[11] + 1 : 0;
+    if (Nx[11] > kIdleLimit) {
         atomicOr(status, kStatusWaitLimit);
-        ctl[8] = -1;
-        ctl[5] = 1;
+        Nx[8] = -1;
+        Nx[5] = 1;
     }
-    ctl[6] = hv;
-    ctl[7] = !hv && ctl[8] < 0 && ctl[3] < 0 && ctl[5];
+    Nx[6] = hv;
+    Nx[7] = !hv && Nx[8] < 0 && Nx[3] < 0 && Nx[5];
     // slot: the inverse-NTT warps alternate slots every period
-    ctl[4] ^= 1;
+    Nx[4] = C[4] ^ 1;
 }
 
 __device__ __forceinline__ void pipe_barrier(int id, int threads)
@@ -232,7 +232,6 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int pl = warp / NW, pw = warp - pl * NW;
     PipeSmem<GW> &s = pipes[pl];
-    int *ctl = s.ctl;
     const int n = A.n, S = n * (int)A.digitR;
     const uint32_t q = A.q, qmask = q - 1;
     const size_t rgsw_words = (size_t)DG * 4 * 1024;
@@ -308,22 +307,24 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
         if (threadIdx.x == 0) cursor = 0;
         for (int k = threadIdx.x; k < m; k += blockDim.x) done[k] = -1;
         if (pw == 0 && lane == 0) {
-            ctl[0] = 0; ctl[1] = -1;      // item of the inverse-NTT warps
-            ctl[2] = -1; ctl[3] = -1;     // item of the digit warps (ciphertext < 0: none)
-            ctl[4] = 0;                   // slot written by the inverse-NTT warps
-            ctl[5] = 0;                   // cursor exhausted
-            ctl[6] = 0; ctl[7] = 0;       // this period: inverse-NTT item valid, stop
-            ctl[8] = -1;                  // no claimed item waiting
-            ctl[11] = 0;                  // idle periods in a row
+            int *c0 = s.ctl[1];           // a period before the first: nothing in flight
+            c0[0] = 0; c0[1] = -1;        // item of the inverse-NTT warps
+            c0[2] = -1; c0[3] = -1;       // item of the digit warps (ciphertext < 0: none)
+            c0[4] = 1;                    // slot written by the inverse-NTT warps
+            c0[5] = 0;                    // cursor exhausted
+            c0[6] = 0; c0[7] = 0;         // inverse-NTT item valid, stop
+            c0[8] = -1;                   // no claimed item waiting
+            c0[11] = 0;                   // idle periods in a row
         }
         __syncthreads();
 
         // ---- NP pipelines over the (step, ciphertext) items of the group. One
         // thread of each plans the pipeline's next period after each period
         // and publishes the plan in shared memory.
-        if (pw == 0 && lane == 0) pipe_schedule(ctl, done, &cursor, res, m, S, compat, A.status);
+        if (pw == 0 && lane == 0) pipe_plan(s.ctl[1], s.ctl[0], done, &cursor, res, m, S, compat, A.status);
         pipe_barrier(1 + pl, PT);
-        for (;;) {
+        for (int t = 0;; t ^= 1) {
+            const int *ctl = s.ctl[t];
             if (ctl[7]) break;
             const int sh = ctl[4];
             if (pw >= GW) {
@@ -347,8 +348,10 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
                 store_row(s.dbuf[pw], lane, x);
             }
             // all warps of the pipeline multiply-accumulate the digit warps'
-            // item once its digit NTTs are in shared memory
+            // item once its digit NTTs are in shared memory; one thread first
+            // plans the next period
             pipe_barrier(1 + pl, PT);
+            if (pw == 0 && lane == 0) pipe_plan(ctl, s.ctl[t ^ 1], done, &cursor, res, m, S, compat, A.status);
             if (ctl[3] >= 0) {
                 const int gk = ctl[3], gs = ctl[2];
                 const uint32_t rr = res[gk * S + gs];
@@ -358,8 +361,12 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
                     mac_chunk<DG, true>(u, key, s.dbuf, acc, c.Q, A.qinv_neg, acc);
             }
             pipe_barrier(1 + pl, PT);
-            if (pw == 0 && lane == 0) pipe_schedule(ctl, done, &cursor, res, m, S, compat, A.status);
-            pipe_barrier(1 + pl, PT);
+            // the digit item is finished: other pipelines may issue its
+            // ciphertext's next step
+            if (pw == 0 && lane == 0 && ctl[3] >= 0) {
+                __threadfence_block();
+                done[ctl[3]] = ctl[2];
+            }
         }
         __syncthreads();
 

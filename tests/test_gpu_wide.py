@@ -103,3 +103,25 @@ def test_wide_worker_shapes(F, ctx1, keys1, pipes, window):
         ctx1.set_option(F.OPT_BR_PIPES, 0)
         ctx1.set_option(F.OPT_BR_WINDOW, -1)
     assert np.array_equal(out, _want12["w"])
+
+
+def test_wide_several_rounds(F, ctx1, keys1):
+    """A group cap of one gate per worker makes the 3-worker CTAs claim three
+    rounds of groups (1000 gates, 152 CTAs of at most 3); every gate decrypts
+    and a spread sample equals the oracle."""
+    count = 1000
+    x, y, g, c1, c2 = random_gate_batch(keys1, count, seed=31)
+    ctx1.set_option(F.OPT_BR_GROUP, 1)
+    ctx1.set_option(F.OPT_BR_PIPES, 3)
+    try:
+        out = ctx1.eval_bootstrap_batch(c1, c2, g)
+        assert ctx1.device_status() == 0
+    finally:
+        ctx1.set_option(F.OPT_BR_GROUP, 0)
+        ctx1.set_option(F.OPT_BR_PIPES, 0)
+    truth = np.array([F.gate_truth(int(a), b, c) for a, b, c in zip(g, x, y)], dtype=np.uint8)
+    assert np.array_equal(keys1.decrypt(out), truth)
+    idx = np.array([0, 1, 455, 456, 500, 912, 999])
+    want, failed = keys1.oracle.eval_bootstrap_batch(c1[idx], c2[idx], g[idx], keys1.btkey, keys1.kskey)
+    assert failed == 0
+    assert np.array_equal(out[idx], want)
