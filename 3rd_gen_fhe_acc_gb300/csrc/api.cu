@@ -837,14 +837,19 @@ int fheacc_subs_keyswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t co
 
 namespace fheacc {
 
-int expand_device(Context &c, const uint64_t *d_in, uint64_t *d_out, cudaStream_t st)
+int expand_device(Context &c, const uint64_t *d_in, uint64_t *d_out, cudaStream_t st, size_t count)
 {
     if (!subs_key_level(c, 0)) return c.fail(FHEACC_ENOKEY, "substitute key not uploaded");
+    if (!count) return FHEACC_OK;
     const int N = c.p.N, logN = c.wide ? 11 : 10;
-    cudaError_t e = cudaMemcpyAsync(d_out, d_in, 2 * (size_t)N * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st);
+    const size_t rw = 2 * (size_t)N, stride = (size_t)N * rw;   // one RLWE; one expansion's output
+    // r[0] of every expansion = its input
+    cudaError_t e = cudaMemcpy2DAsync(d_out, stride * sizeof(uint64_t), d_in, rw * sizeof(uint64_t),
+                                      rw * sizeof(uint64_t), count, cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) return c.cuda_fail(e, "expand copy");
     for (int f = 0; f < logN; f++) {
-        int rc = launch_expand(c, 3, d_out, d_out, 0, f, subs_key_level(c, f), c.d_rot + (size_t)f * N, st);
+        int rc = launch_expand(c, 3, d_out, d_out, 0, f, subs_key_level(c, f), c.d_rot + (size_t)f * N, st, count,
+                               stride);
         if (rc) return rc;
     }
     return FHEACC_OK;

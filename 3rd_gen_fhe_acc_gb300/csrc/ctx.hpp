@@ -178,8 +178,10 @@ int launch_derive_keys64(Context &c, uint64_t *d_keys, size_t count, const ulong
 int launch_ntt64(Context &c, uint64_t *d_polys, size_t count, bool inverse, cudaStream_t st);
 int launch_rlwe_mult_rgsw64(Context &c, const uint64_t *d_acc, const uint64_t *d_rgsw, uint64_t *d_out,
                             size_t count, size_t rgsw_stride, cudaStream_t st);
-// expand_RLWE (app.cpp:26-76) of one NTT RLWE into N (d_out: [N][2N]).
-int expand_device(Context &c, const uint64_t *d_in, uint64_t *d_out, cudaStream_t st);
+// expand_RLWE (app.cpp:26-76) of `count` NTT RLWEs (d_in: [count][2N]), each
+// into N (d_out: [count][N][2N]), all expansions level by level in one launch
+// per level.
+int expand_device(Context &c, const uint64_t *d_in, uint64_t *d_out, cudaStream_t st, size_t count = 1);
 int launch_blind_rotate64(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
                           size_t count, uint32_t flags, uint64_t *d_acc_out, uint64_t *d_extract, int max_ctas,
                           cudaStream_t st);
@@ -191,9 +193,10 @@ int launch_extract64(Context &c, const uint64_t *d_rlwe, size_t count, uint64_t 
 int launch_lwe_keyswitch64(Context &c, const uint64_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
                            cudaStream_t st);
 // automorphism / key switch / expand (expand.cu); mode: 0 SUBS, 1 KS,
-// 2 SUBS_KS, 3 EXPAND (one level f, in place on d_out)
+// 2 SUBS_KS, 3 EXPAND (one level f, in place on d_out, for `batches` r
+// arrays bstride words apart)
 int launch_expand(Context &c, int mode, const uint64_t *d_in, uint64_t *d_out, size_t count, int f,
-                  const void *ksk, const uint64_t *d_rot, cudaStream_t st);
+                  const void *ksk, const uint64_t *d_rot, cudaStream_t st, size_t batches = 1, size_t bstride = 0);
 int launch_to_u32(Context &c, const uint64_t *d_in, uint32_t *d_out, size_t n, cudaStream_t st);
 // IMAD throughput probe (probe.cu)
 int measure_imad_rate(Context &c, double *imad_per_s);

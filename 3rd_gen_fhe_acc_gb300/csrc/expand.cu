@@ -29,9 +29,11 @@ namespace dev {
 enum ExpMode { kSubs = 0, kKs = 1, kSubsKs = 2, kExpand = 3 };
 
 struct ExpArgs {
-    const uint64_t *in;      // items [count][2N] (EXPAND: the r array)
-    uint64_t *out;           // [count][2N] (EXPAND: the r array, in place)
+    const uint64_t *in;      // items [count][2N] (EXPAND: the r arrays)
+    uint64_t *out;           // [count][2N] (EXPAND: the r arrays, in place)
     size_t count;
+    size_t batches;          // EXPAND: independent r arrays, bstride words apart (else 1)
+    size_t bstride;
     int mode, f, logN, L;    // L = digitKS_R
     uint32_t bits;           // Bks_R_bits
     uint32_t ipow;           // (N / 2^f + 1)^-1 mod 2N
@@ -62,9 +64,11 @@ __global__ void __launch_bounds__(256) expand32_kernel(const __grid_constant__ E
     const uint32_t Q = c.Q;
     const int L = A.L;
     const bool subs = A.mode != kKs;
-    const size_t items = A.mode == kExpand ? ((size_t)1 << A.f) : A.count;
+    const size_t per = A.mode == kExpand ? ((size_t)1 << A.f) : A.count;
+    const size_t items = per * A.batches;
     for (size_t it = blockIdx.x; it < items; it += gridDim.x) {
-        const uint64_t *in = A.in + it * 2048;
+        const size_t bo = it / per * A.bstride, jt = it % per;   // batch offset, item within the batch
+        const uint64_t *in = A.in + bo + jt * 2048;
         if (warp < 2) {
             uint32_t x[32];
 #pragma unroll
@@ -101,7 +105,7 @@ __global__ void __launch_bounds__(256) expand32_kernel(const __grid_constant__ E
             for (int r = 0; r < 32; r++) d[warp][33 * lane + r] = reduce32(x[r], mu32, Q);
         }
         __syncthreads();
-        uint64_t *out = A.out + it * 2048;
+        uint64_t *out = A.out + bo + jt * 2048;
         for (int k = threadIdx.x; k < 1024; k += blockDim.x) {
             uint64_t oa, ob;
             if (A.mode == kSubs) {
@@ -123,7 +127,7 @@ __global__ void __launch_bounds__(256) expand32_kernel(const __grid_constant__ E
             if (A.mode == kExpand) {
                 const uint64_t ta = in[k], tb = in[1024 + k];
                 const uint64_t rot = A.rot[k];
-                uint64_t *hi = A.out + (it + ((size_t)1 << A.f)) * 2048;
+                uint64_t *hi = A.out + bo + (jt + per) * 2048;
                 out[k] = (ta + oa) % Q;
                 out[1024 + k] = (tb + ob) % Q;
                 hi[k] = ((ta + Q - oa) % Q) * rot % Q;
@@ -151,9 +155,11 @@ __global__ void __launch_bounds__(256) expand64_kernel(const __grid_constant__ E
     const uint64_t Q = c.Q;
     const int L = A.L;
     const bool subs = A.mode != kKs;
-    const size_t items = A.mode == kExpand ? ((size_t)1 << A.f) : A.count;
+    const size_t per = A.mode == kExpand ? ((size_t)1 << A.f) : A.count;
+    const size_t items = per * A.batches;
     for (size_t it = blockIdx.x; it < items; it += gridDim.x) {
-        const uint64_t *in = A.in + it * 4096;
+        const size_t bo = it / per * A.bstride, jt = it % per;   // batch offset, item within the batch
+        const uint64_t *in = A.in + bo + jt * 4096;
         for (int e = gtid; e < 2048; e += 128) t[grp][e] = in[grp * 2048 + e];
         group_sync(1 + grp, 128);
         ntt64_inv_2048<128>(t[grp], itw, c, gtid, 1 + grp);
@@ -209,7 +215,7 @@ __global__ void __launch_bounds__(256) expand64_kernel(const __grid_constant__ E
             }
             __syncthreads();
         }
-        uint64_t *out = A.out + it * 4096;
+        uint64_t *out = A.out + bo + jt * 4096;
 #pragma unroll
         for (int i = 0; i < 8; i++) {
             const int k = tid + 256 * i;
@@ -228,7 +234,7 @@ __global__ void __launch_bounds__(256) expand64_kernel(const __grid_constant__ E
             if (A.mode == kExpand) {
                 const uint64_t ta = in[k], tb = in[2048 + k];
                 const uint64_t rot = A.rot[k];
-                uint64_t *hi = A.out + (it + ((size_t)1 << A.f)) * 4096;
+                uint64_t *hi = A.out + bo + (jt + per) * 4096;
                 const uint64_t s1 = ta + oa, s2 = tb + ob;
                 out[k] = s1 >= Q ? s1 - Q : s1;
                 out[2048 + k] = s2 >= Q ? s2 - Q : s2;
@@ -269,16 +275,18 @@ static uint32_t inv_power(int N, int f)
 
 // ksk: narrow, u32 [L][2][N] device words; wide, Shoup pairs.
 int launch_expand(Context &c, int mode, const uint64_t *d_in, uint64_t *d_out, size_t count, int f,
-                  const void *ksk, const uint64_t *d_rot, cudaStream_t st)
+                  const void *ksk, const uint64_t *d_rot, cudaStream_t st, size_t batches, size_t bstride)
 {
     const int logN = c.wide ? 11 : 10;
     if (f < 0 || f >= logN) return c.fail(FHEACC_EINVAL, "substitution factor out of range");
     dev::ExpArgs A{};
     A.in = d_in; A.out = d_out; A.count = count; A.mode = mode; A.f = f; A.logN = logN;
+    A.batches = mode == dev::kExpand ? batches : 1;
+    A.bstride = bstride;
     A.L = (int)c.p.digitKS_R; A.bits = c.p.Bks_R_bits; A.ipow = inv_power(c.p.N, mode == dev::kKs ? 0 : f);
     A.rot = d_rot; A.Q = c.p.Q; A.mu64 = c.dp.mu64;
     if (mode == dev::kKs) A.ipow = 1;
-    const size_t items = mode == dev::kExpand ? ((size_t)1 << f) : count;
+    const size_t items = (mode == dev::kExpand ? ((size_t)1 << f) : count) * A.batches;
     if (!items) return FHEACC_OK;
     size_t blocks = std::min<size_t>(items, (size_t)sms(c) * 4);
     cudaError_t e;

@@ -142,20 +142,21 @@ int fheacc_homo_expand(fheacc_ctx *ctx, const uint64_t *d_packed, const uint64_t
     DeviceGuard g(c.device);
     cudaStream_t st = (cudaStream_t)stream;
     const size_t N = (size_t)c.p.N, rw = 2 * N, dG = c.p.digitG, gw = dG * 4 * N;
-    // per digit: the N expanded RLWEs and their products with enc_sec
-    int rc = ensure_scratch(c, c.psi, 2 * N * rw * sizeof(uint64_t));
+    // all digits at once: the dG x N expanded RLWEs (the dG expansions level by
+    // level, one launch per level) and their products with enc_sec (one launch)
+    int rc = ensure_scratch(c, c.psi, 2 * dG * N * rw * sizeof(uint64_t));
     if (rc) return rc;
-    uint64_t *u = (uint64_t *)c.psi.ptr, *m = u + N * rw;
+    uint64_t *u = (uint64_t *)c.psi.ptr, *m = u + dG * N * rw;
+    rc = expand_device(c, d_packed, u, st, dG);
+    if (!rc) rc = mult_rgsw(c, u, d_enc_sec, 0, m, dG * N, st);
     for (size_t j = 0; j < dG && !rc; j++) {
-        rc = expand_device(c, d_packed + j * rw, u, st);
-        if (!rc) rc = mult_rgsw(c, u, d_enc_sec, 0, m, N, st);
-        if (rc) break;
-        // RGSW i, row j: c_text[j][0] = m[i], c_text[j][1] = u[i]
-        cudaError_t e = cudaMemcpy2DAsync(d_out + (j * 2 + 0) * rw, gw * sizeof(uint64_t), m, rw * sizeof(uint64_t),
-                                          rw * sizeof(uint64_t), N, cudaMemcpyDeviceToDevice, st);
+        // RGSW i, row j: c_text[j][0] = m[j][i], c_text[j][1] = u[j][i]
+        cudaError_t e = cudaMemcpy2DAsync(d_out + (j * 2 + 0) * rw, gw * sizeof(uint64_t), m + j * N * rw,
+                                          rw * sizeof(uint64_t), rw * sizeof(uint64_t), N, cudaMemcpyDeviceToDevice,
+                                          st);
         if (e == cudaSuccess)
-            e = cudaMemcpy2DAsync(d_out + (j * 2 + 1) * rw, gw * sizeof(uint64_t), u, rw * sizeof(uint64_t),
-                                  rw * sizeof(uint64_t), N, cudaMemcpyDeviceToDevice, st);
+            e = cudaMemcpy2DAsync(d_out + (j * 2 + 1) * rw, gw * sizeof(uint64_t), u + j * N * rw,
+                                  rw * sizeof(uint64_t), rw * sizeof(uint64_t), N, cudaMemcpyDeviceToDevice, st);
         if (e != cudaSuccess) rc = c.cuda_fail(e, "homo_expand rows");
     }
     return rc;

@@ -505,6 +505,193 @@ def run_mixed(args):
     return 0
 
 
+def run_psi(args):
+    """One PSI query of the reference's PSI test (test.cpp:1510-1606) per step,
+    at N = 2048 (the 64-bit set): homo_expand of digitG packed RLWEs into N
+    RGSWs (app.cpp:78-96), a CMUX tree selecting one of 2^(18 - log2 N) = 128
+    database RLWEs (RLWE.cpp:788-793), and an RLWE blind rotation of the
+    selected entry (RLWE.cpp:824-838). Plaintexts are made with the library's
+    own NTT; the query sets every odd bit, so the result decrypts to ones at
+    coefficients 1366..1451."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build_product()
+    import importlib
+    F = importlib.import_module("3rd_gen_fhe_acc_gb300")
+    torch.cuda.set_device(0)
+    P = F.params_preset(1)
+    F.derive(P)
+    N, Q, dG, logN = P.N, P.Q, P.digitG, 11
+    rw, gw = 2 * N, dG * 4 * N
+    t_setup = time.perf_counter()
+    rsk = F.RLWE_secretkey(P, 12)
+    subs = F.substitute_key(P, 15, rsk)
+    ctx = F.Context(P, 0)
+    ctx.upload_subs_key(subs)
+    stream = torch.cuda.current_stream()
+    st = stream.cuda_stream
+
+    def ntt_host(polys, inverse=False):
+        d = torch.from_numpy(np.ascontiguousarray(polys, dtype=np.uint64).view(np.int64)).cuda()
+        (ctx.ntt_inverse if inverse else ctx.ntt_forward)(d.data_ptr(), d.numel() // N, st)
+        torch.cuda.synchronize()
+        return d.cpu().numpy().view(np.uint64)
+
+    s_time = ntt_host(rsk, inverse=True)
+    enc_neg_s = F.RGSW_encrypt(P, 41, rsk, ntt_host((Q - s_time) % Q))
+    iN = pow(N, Q - 2, Q)
+    packed, pow_bg = [], 1
+    for i in range(dG):
+        m = np.zeros(N, dtype=np.uint64)
+        m[1::2] = pow_bg * iN % Q
+        packed.append(F.RLWE_encrypt(P, 100 + i, rsk, ntt_host(m)))
+        pow_bg = pow_bg * (1 << P.BG_bits) % Q
+    packed = np.concatenate(packed)
+    entries = 1 << (18 - logN)
+    db = []
+    for i in range(entries):
+        m = np.zeros(N, dtype=np.uint64)
+        m[:i + 1] = Q // 2
+        db.append(F.RLWE_encrypt(P, 1000 + i, rsk, ntt_host(m)))
+    db = np.concatenate(db)
+    setup_s = time.perf_counter() - t_setup
+    dv = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint64).view(np.int64)).cuda()
+    d_packed, d_enc, d_db = dv(packed), dv(enc_neg_s), dv(db)
+    rgsw = torch.zeros(N * gw, dtype=torch.int64, device="cuda")
+    bufs = [torch.zeros(entries // 2 * rw, dtype=torch.int64, device="cuda") for _ in range(2)]
+    out = torch.zeros(rw, dtype=torch.int64, device="cuda")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def query(ev=None):
+        if ev: ev[0].record(stream)
+        ctx.homo_expand(d_packed.data_ptr(), d_enc.data_ptr(), rgsw.data_ptr(), st)
+        if ev: ev[1].record(stream)
+        src, count, level = d_db, entries, logN
+        while count > 1:   # v[k] = CMUX(v[2k], v[2k+1], RGSW[level])
+            dst = bufs[level & 1]
+            ctx.CMUX(src.data_ptr(), src.data_ptr() + 8 * rw, rgsw.data_ptr() + 8 * gw * level, dst.data_ptr(),
+                     count // 2, in_stride=2 * rw, stream=st)
+            src, count, level = dst, count // 2, level + 1
+        if ev: ev[2].record(stream)
+        ctx.blind_rotate_RLWE(src.data_ptr(), rgsw.data_ptr(), False, out.data_ptr(), 1, stream=st)
+        if ev: ev[3].record(stream)
+
+    want = np.zeros(N, dtype=np.uint8)
+    want[1366:1452] = 1
+
+    def decodes(o):
+        phase = F.RLWE_phase(P, rsk, o)
+        return np.array_equal(((2 * phase.astype(object) + Q // 2) // Q % 2).astype(np.uint8), want)
+
+    for _ in range(args.warmup):
+        flush.fill_(1)
+        query()
+    torch.cuda.synchronize()
+    first_out = out.cpu().numpy().view(np.uint64).copy()
+    clocks = ClockSampler(0)
+    clocks.start()
+    phases = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        torch.cuda.synchronize()
+        query(ev)
+        torch.cuda.synchronize()
+        phases.append([ev[i].elapsed_time(ev[i + 1]) for i in range(3)])
+    clk = clocks.stop()
+    step_ms = [sum(ph) for ph in phases]
+    value = args.steps / (sum(step_ms) / 1e3)
+    repeat_ok = np.array_equal(out.cpu().numpy().view(np.uint64), first_out)
+
+    # e2e: the query's packed RLWEs in from pinned host memory, the result out
+    h_packed = torch.from_numpy(packed.view(np.int64)).pin_memory()
+    h_out = torch.zeros(rw, dtype=torch.int64).pin_memory()
+    e2e = []
+    for s_ in range(args.warmup + args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d_packed.copy_(h_packed, non_blocking=True)
+        query()
+        h_out.copy_(out, non_blocking=True)
+        torch.cuda.synchronize()
+        if s_ >= args.warmup:
+            e2e.append(time.perf_counter() - t0)
+    e2e_ok = decodes(h_out.numpy().view(np.uint64))
+
+    # integer roofline: 64-bit modular multiplies of the query, the reference's
+    # algorithm (an N = 2048 NTT is N/2 log2 N butterflies, an inverse NTT that
+    # plus N scalings): per expand item (one RLWE of one level) the inverse
+    # NTTs of a and b, digitKS_R + 1 forward NTTs, 2 digitKS_R N key products
+    # and 2N for the rotation; per RLWE x RGSW 210,944 as in the bootstrap
+    L = P.digitKS_R
+    ntt = N // 2 * logN
+    mult = 2 * (ntt + N) + 2 * dG * ntt + 4 * dG * N   # 210,944
+    expand_item = 2 * (ntt + N) + (L + 1) * ntt + 2 * L * N + 2 * N
+    items = dG * (N - 1)
+    n_mult = dG * N + (entries - 1) + logN
+    work = items * expand_item + n_mult * mult + logN * 2 * N
+    imad = ctx.measure_imad_rate()
+    slots = 16
+    peak = imad / slots
+    achieved = work / (statistics.mean(step_ms) / 1e3)
+    roofline = {"bound": "int", "achieved": achieved / 1e9, "peak": peak / 1e9, "unit": "G modmul/s",
+                "frac": achieved / peak, "traffic": None, "kernel": "whole query",
+                "work": "%d expand items x %d + %d RLWE x RGSW x %d + %d rotation multiplies = %.3g 64-bit modular "
+                        "multiplies per query" % (items, expand_item, n_mult, mult, logN * 2 * N, work),
+                "peak_source": "IMAD rate measured in this run (%.1f T lane-op/s) / %d IMAD issue slots per 64-bit "
+                               "Shoup modular multiply" % (imad / 1e12, slots)}
+
+    cpu = None
+    if not args.no_cpu:
+        import __graft_entry__ as ge
+        ge._build_oracle()
+        from oracle_lib import Oracle
+        ora = Oracle.from_params(P)
+        t0 = time.perf_counter()
+        r_exp = ora.expand_rlwe(packed[:rw], subs)
+        t_exp = time.perf_counter() - t0
+        sample_m = 8
+        t0 = time.perf_counter()
+        for k in range(sample_m):
+            ora.rlwe_mult_rgsw(r_exp[k], enc_neg_s)
+        t_mult = (time.perf_counter() - t0) / sample_m
+        t0 = time.perf_counter()
+        for k in range(sample_m):
+            ora.cmux(db[k * rw:(k + 1) * rw], db[(k + 1) * rw:(k + 2) * rw], enc_neg_s)
+        t_cmux = (time.perf_counter() - t0) / sample_m
+        cpu_query_s = dG * (t_exp + N * t_mult) + (entries - 1 + logN) * t_cmux
+        cpu = {"value": 1.0 / cpu_query_s, "unit": "PSI queries/s", "cores": 1, "kind": "port",
+               "sample": "oracle (C restatement of app.cpp:26-96, RLWE.cpp:642-704,788-838) on one thread: one "
+                         "expand_RLWE %.1f s, RLWE x RGSW %.1f ms and CMUX %.1f ms (means of %d); a query = %d "
+                         "expand_RLWE + %d RLWE x RGSW + %d CMUX = %.0f s" % (
+                             t_exp, 1e3 * t_mult, 1e3 * t_cmux, sample_m, dG, dG * N, entries - 1 + logN,
+                             cpu_query_s)}
+    ph = np.array(phases)
+    line = {
+        "metric": "PSI queries/sec on 1 GB300 (homo_expand + CMUX tree + RLWE blind rotation, bit-exact)",
+        "value": value, "unit": "PSI queries/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": statistics.mean(step_ms), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64", "data": "synthetic",
+        "config": {"workload": "the reference PSI test flow at N=2048 (Q=%d, BG=2^%d x%d, Bks_R=2^%d x%d): "
+                               "homo_expand of %d packed RLWEs into %d RGSWs, a %d-level CMUX tree over %d "
+                               "database RLWEs, an %d-CMUX blind rotation; seeded keys and plaintexts" % (
+                                   Q, P.BG_bits, dG, P.Bks_R_bits, L, dG, N, 18 - logN, entries, logN),
+                   "l2": "flushed between timed steps (write of a 512 MiB buffer)",
+                   "parallelism": "one query per GPU"},
+        "e2e": {"value": args.steps / sum(e2e), "unit": "PSI queries/s", "h2d_bytes_per_step": int(packed.nbytes),
+                "d2h_bytes_per_step": int(rw * 8), "ms_per_step": 1e3 * statistics.mean(e2e)},
+        "phases_ms": {"homo_expand": float(ph[:, 0].mean()), "cmux_tree": float(ph[:, 1].mean()),
+                      "blind_rotate": float(ph[:, 2].mean())},
+        "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+        "checks": {"result_decodes": bool(decodes(first_out)), "e2e_decodes": bool(e2e_ok),
+                   "steps_repeatable": bool(repeat_ok), "setup_s": setup_s},
+    }
+    print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 def fheacc_key_bytes(P):
     """Device bytes of the bootstrap + key-switch keys of a parameter set."""
     if P.N == 1024:
@@ -539,6 +726,8 @@ def main():
                     help="sweep serving rates (PSI queries through the continuous-batching server) and exit")
     ap.add_argument("--serve-rate", type=float, default=20000.0, help="offered bootstraps/s of the serving sample")
     ap.add_argument("--serve-seconds", type=float, default=8.0)
+    ap.add_argument("--psi", action="store_true",
+                    help="the reference's PSI query (homo_expand, CMUX tree, RLWE blind rotation) at N=2048 and exit")
     ap.add_argument("--mixed", action="store_true",
                     help="uneven batch of two parameter sets in one CUDA-graph launch (N=1024 + N=2048) and exit")
     ap.add_argument("--mixed-narrow", type=int, default=3000)
@@ -554,6 +743,8 @@ def main():
         return profile_case(args.preset)
     if args.mixed:
         return run_mixed(args)
+    if args.psi:
+        return run_psi(args)
 
     import torch
     import __graft_entry__
