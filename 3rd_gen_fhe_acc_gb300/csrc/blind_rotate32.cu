@@ -12,7 +12,7 @@
 //
 // Schedule. The grid is persistent; each CTA claims a group of consecutive
 // ciphertexts from a counter (the launcher fits the group size to the batch:
-// the fewest rounds of at most kMaxGroup, or the tuned cap) and claims again
+// the fewest rounds of at most kMaxGroup per pipeline, or the tuned cap) and claims again
 // until the batch is done. Steps are the OUTER loop: a CTA applies step s to every ciphertext of
 // its group before step s + 1, so the CTAs walk through the bootstrapping key
 // together and the 23 RGSW keys of a step (1.5 MB) are mostly served from L2.
@@ -60,7 +60,7 @@
 namespace fheacc {
 namespace dev {
 
-constexpr int kMaxGroup = 24;   // ciphertexts per CTA and chunk (residue table in shared memory)
+constexpr int kMaxGroup = 24;   // ciphertexts per pipeline and claim (residue table in shared memory)
 constexpr int kMaxTableBG = 512;   // largest gadget base with digit tables (20 BG bytes of shared memory)
 
 struct PipeArgs {
@@ -72,7 +72,7 @@ struct PipeArgs {
     uint32_t *accs;          // scratch [count][2][1024], B-tiled, values < 2Q
     uint64_t *acc_out;       // optional: canonical NTT accumulators [count][2048]
     uint32_t *extract;       // optional: [count][kExtractStride]
-    int group;               // ciphertexts per CTA and chunk (<= kMaxGroup)
+    int group;               // ciphertexts per claim (<= kMaxGroup per pipeline)
     int n;
     uint32_t q, embed, Br, digitR, bg_bits, flags;
     uint32_t qinv_neg;         // -Q^-1 mod 2^32 (keys carry 2^32 N^-1, see DevParams::key_factor)

@@ -24,7 +24,7 @@
 namespace fheacc {
 namespace dev {
 
-constexpr int kMaxGroup64 = 8;
+constexpr int kMaxGroup64 = 8;   // ciphertexts per worker and claim
 constexpr int kT64 = 256;   // threads per CTA
 
 struct Step64Smem {
