@@ -32,6 +32,30 @@ struct Step64Smem {
     uint64_t buf[2][2048];   // digit NTTs
 };
 
+constexpr int kMaxTableBG64 = 512;   // largest gadget base with digit tables (40 BG bytes of shared memory)
+
+__device__ __forceinline__ uint64_t mulmod64(uint64_t a, uint64_t b, uint64_t Q)
+{
+    return (uint64_t)((unsigned __int128)a * b % Q);
+}
+
+// Builds the digit tables (DigitTables64) for y < BG in `mem` (40 BG bytes,
+// 16-byte aligned) from the twiddles tw[1..3]; all threads of the CTA take part.
+__device__ __forceinline__ DigitTables64 build_digit_tables64(unsigned char *mem, int BG,
+                                                             const ulonglong2 *__restrict__ tw, uint64_t Q)
+{
+    ulonglong2 *t23 = reinterpret_cast<ulonglong2 *>(mem), *t123 = t23 + BG;
+    uint64_t *t1 = reinterpret_cast<uint64_t *>(t123 + BG);
+    const uint64_t w1 = tw[1].x, w2 = tw[2].x, w3 = tw[3].x;
+    const uint64_t w21 = mulmod64(w2, w1, Q), w31 = mulmod64(w3, w1, Q);
+    for (int y = threadIdx.x; y < BG; y += blockDim.x) {
+        t1[y] = mulmod64((uint64_t)y, w1, Q);
+        t23[y] = make_ulonglong2(mulmod64((uint64_t)y, w2, Q), mulmod64((uint64_t)y, w3, Q));
+        t123[y] = make_ulonglong2(mulmod64((uint64_t)y, w21, Q), mulmod64((uint64_t)y, w31, Q));
+    }
+    return DigitTables64{t1, t23, t123};
+}
+
 // One RLWE x RGSW step on s.acc (NTT domain, values < 2Q) with the key
 // `key` (Shoup pairs, [digitG][2][2][2048]), run by the 256 threads tid of a
 // worker that synchronises on named barrier `bar` (its two 128-thread groups
@@ -40,9 +64,11 @@ struct Step64Smem {
 // it is overwritten) the last digit's NTT is replaced by the accumulator: the
 // keys were uploaded with K'_h = K_h - BG^(h-DG+1) K_last, K'_last =
 // BG^-(DG-1) K_last (Q < BG^DG, so sum_h BG^h NTT(digit_h) = acc).
+// With dt the digit transforms start from the digit tables (BG <= kMaxTableBG64).
 __device__ __forceinline__ void step64(Step64Smem &s, const ulonglong2 *__restrict__ key, int DG, uint32_t bg_bits,
                                        const ulonglong2 *__restrict__ tw, const ulonglong2 *__restrict__ itw,
-                                       const Ntt64Consts &c, const uint64_t *acc_nd, int tid, int bar)
+                                       const Ntt64Consts &c, const uint64_t *acc_nd, int tid, int bar,
+                                       const DigitTables64 *dt = nullptr)
 {
     const int grp = tid >> 7, gtid = tid & 127;
     ntt64_inv_2048<128>(s.acc[grp], itw, c, gtid, bar + 1 + grp);
@@ -56,7 +82,8 @@ __device__ __forceinline__ void step64(Step64Smem &s, const ulonglong2 *__restri
         const uint32_t sh = bg_bits * h;
         for (int e = gtid; e < 2048; e += 128) s.buf[grp][e] = (s.acc[grp][e] >> sh) & mask;
         group_sync(bar + 1 + grp, 128);
-        ntt64_fwd_2048<128>(s.buf[grp], tw, c, gtid, bar + 1 + grp);
+        if (dt) ntt64_fwd_2048_digit<128>(s.buf[grp], tw, c, gtid, bar + 1 + grp, *dt);
+        else ntt64_fwd_2048<128>(s.buf[grp], tw, c, gtid, bar + 1 + grp);
         group_sync(bar, kT64);
         const ulonglong2 *k0 = key + (size_t)(h * 2 + 0) * 2 * 2048;   // row c_text[h][0]: times digit of a
         const ulonglong2 *k1 = key + (size_t)(h * 2 + 1) * 2 * 2048;   // row c_text[h][1]: times digit of b
@@ -194,6 +221,7 @@ struct Br64Args {
     StepWindow win;            // keeps the CTAs within a few steps of each other (window.cuh)
     unsigned long long *claim_next;   // next unclaimed ciphertext (zeroed before the launch)
     unsigned *status;          // set to kStatusWaitLimit if a worker gave up waiting
+    int digit_tables;          // digit NTTs start from tables (DigitTables64) after the residues
 };
 
 // Polls of a worker waiting for another worker's step of the same ciphertext
@@ -236,6 +264,9 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
         wcur = 0;
         won = 1;
     }
+    // digit tables after the residue table of the largest group
+    const DigitTables64 dt = build_digit_tables64(res + ((size_t)A.group * S + 15) / 16 * 16,
+                                                  A.digit_tables ? 1 << A.bg_bits : 0, tw, c.Q);
     for (;;) {
         if (threadIdx.x == 0) {
             const unsigned long long f = atomicAdd(A.claim_next, (unsigned long long)A.group);
@@ -351,7 +382,7 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
             for (int e = tid; e < 4096; e += kT64) s.acc[e >> 11][e & 2047] = __ldcg(acc + e);
             group_sync(bar, kT64);
             step64(s, A.btkey + ((size_t)st * A.Br + r) * rgsw_pairs, A.DG, A.bg_bits, tw, itw, c,
-                   A.derive_last ? acc : nullptr, tid, bar);
+                   A.derive_last ? acc : nullptr, tid, bar, A.digit_tables ? &dt : nullptr);
             for (int e = tid; e < 4096; e += kT64) __stcg(acc + e, s.acc[e >> 11][e & 2047]);
             group_sync(bar, kT64);
             if (tid == 0) {
@@ -555,6 +586,8 @@ int launch_rlwe_mult_rgsw64(Context &c, const uint64_t *d_acc, const uint64_t *d
     ulonglong2 *pairs = (ulonglong2 *)c.io.ptr;
     rc = launch_shoup_pairs64(c, d_rgsw, pairs, words, st);
     if (rc) return rc;
+    // no digit tables here: their 20 KB of shared memory cost this kernel more
+    // L1 (twiddles, the shared RGSW) than they saved (homo_expand 7.9 -> 8.4 ms)
     const size_t smem = sizeof(dev::Step64Smem);
     cudaFuncSetAttribute(dev::rlwe_mult_rgsw64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     size_t blocks = std::min<size_t>(count, (size_t)sms_of(c) * 2);
@@ -583,11 +616,19 @@ static int launch_br64_shape(Context &c, dev::Br64Args A, int max_ctas, cudaStre
     const size_t steps = (size_t)c.p.n * c.p.digitR;
     // group cap: kMaxGroup64 (or the tuned cap) per worker, within the shared memory of one CTA
     int cap = W * (c.tune.br_group > 0 ? std::min(c.tune.br_group, dev::kMaxGroup64) : dev::kMaxGroup64);
-    const size_t fixed = W * sizeof(dev::Step64Smem) + 16;
+    // digit tables when the gadget base allows and shared memory holds them
+    // beside a group of at least kMaxGroup64 per worker (else the group first)
+    const size_t tbytes = 40 * ((size_t)1 << c.p.BG_bits);
+    A.digit_tables = (1 << c.p.BG_bits) <= dev::kMaxTableBG64 &&
+                     W * sizeof(dev::Step64Smem) + 32 + tbytes + (size_t)cap * steps <= kPipeSmemBudget;
+    const size_t fixed = W * sizeof(dev::Step64Smem) + 32 + (A.digit_tables ? tbytes : 0);
     if (fixed + (size_t)cap * steps > kPipeSmemBudget)
         cap = fixed < kPipeSmemBudget ? (int)((kPipeSmemBudget - fixed) / steps) : 0;
     if (cap < 1) return c.fail(FHEACC_EINVAL, "n * digitR too large for the blind rotation's residue table");
-    size_t smem = W * sizeof(dev::Step64Smem) + (size_t)cap * steps;
+    auto smem_of = [&](int group) {
+        return W * sizeof(dev::Step64Smem) + ((size_t)group * steps + 15) / 16 * 16 + (A.digit_tables ? tbytes : 0);
+    };
+    size_t smem = smem_of(cap);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return c.cuda_fail(e, "br64 smem attribute");
     int per_sm = 0;
@@ -600,7 +641,7 @@ static int launch_br64_shape(Context &c, dev::Br64Args A, int max_ctas, cudaStre
     // equal claims: the fewest rounds of at most `cap` ciphertexts per CTA
     const size_t rounds = (A.count + blocks * cap - 1) / (blocks * cap);
     A.group = (int)((A.count + blocks * rounds - 1) / (blocks * rounds));
-    smem = W * sizeof(dev::Step64Smem) + (size_t)A.group * steps;
+    smem = smem_of(A.group);
     // claim counter after the accumulators
     A.claim_next = reinterpret_cast<unsigned long long *>(A.accs + A.count * 4096);
     e = cudaMemsetAsync(A.claim_next, 0, kClaimWords * sizeof(uint32_t), st);
@@ -626,11 +667,13 @@ int launch_blind_rotate64_with(Context &c, const uint64_t *d_c1, const uint64_t 
     A.bg_bits = c.p.BG_bits; A.flags = flags; A.derive_last = (int)c.dp.last_digit_from_acc;
     A.status = c.d_status;
     for (int i = 0; i < 8; i++) A.gate_constant[i] = c.dp.gate_constant[i];
-    // workers per CTA, by default from the gates per SM (one GB300, 2048-gate
-    // batches and smaller): up to 1 one worker per CTA (3 CTAs per SM), up to 3
-    // two workers, beyond that three (700 gates: 305 / 247 / 235 ms)
+    // workers per CTA, by default from the gates per SM (one GB300): up to 1
+    // one worker per CTA (3 CTAs per SM), beyond that two, whose shared memory
+    // leaves room for the digit tables that three workers' does not (2048
+    // gates: 658 ms with two workers and tables, 698 ms with three; 700 gates:
+    // 240 ms either way; 304 gates: 98 / 109 / 146 ms with 2 / 1 / 3)
     const size_t sms = (size_t)sms_of(c);
-    const int w = c.tune.br_pipes > 0 ? c.tune.br_pipes : count <= sms ? 1 : count <= 3 * sms ? 2 : 3;
+    const int w = c.tune.br_pipes > 0 ? c.tune.br_pipes : count <= sms ? 1 : 2;
     if (w == 3) return launch_br64_shape<3, 1>(c, A, max_ctas, st);
     if (w == 2) return launch_br64_shape<2, 1>(c, A, max_ctas, st);
     return launch_br64_shape<1, 3>(c, A, max_ctas, st);

@@ -254,10 +254,9 @@ int fheacc_autotune(fheacc_ctx *ctx, size_t count, fheacc_tune_trial *trials, in
     };
     std::vector<Cand> cands;
     if (c.wide) {
-        for (int pipes : {3, 1})
+        for (int pipes : {2, 3, 1})
             for (int window : {-1, 0}) cands.push_back({-1, 0, 0, window, pipes});
-        cands.push_back({-1, 0, 4, -1, 3});
-        cands.push_back({-1, 0, 0, -1, 2});
+        cands.push_back({-1, 0, 4, -1, 2});
         cands.push_back({-1, 1, 0, -1, 1});
     } else {
         for (int group : {0, 6, 12}) cands.push_back({-1, 0, group, -1, 3});

@@ -103,6 +103,68 @@ __device__ __forceinline__ void ntt64_fwd_2048(uint64_t *a, const ulonglong2 *__
     group_sync(bar, G);
 }
 
+// Products of a gadget digit (y < BG) with the three twiddles of the first two
+// forward stages, w1 = psi^bitrev(1) (stage t = 1024), w2 and w3 (t = 512):
+// t1[y] = y w1, t23[y] = (y w2, y w3), t123[y] = (y w2 w1, y w3 w1), mod Q.
+struct DigitTables64 {
+    const uint64_t *t1;
+    const ulonglong2 *t23, *t123;
+};
+
+// First forward pass (stages t = 1024 .. 128) of a digit polynomial (values
+// < BG): the first two stages of each radix-4 group (x0, x1, x2, x3) =
+// x[r, r+4, r+8, r+12] of a 16-tuple come from the tables,
+//   x[r]      = x0 + w1 x2 + w2 x1 + w2 w1 x3
+//   x[r + 4]  = x0 + w1 x2 - w2 x1 - w2 w1 x3
+//   x[r + 8]  = x0 - w1 x2 + w3 x1 - w3 w1 x3
+//   x[r + 12] = x0 - w1 x2 - w3 x1 + w3 w1 x3
+// (each below 3Q + BG), the other two stages are Cooley-Tukey butterflies.
+template <int G>
+__device__ __forceinline__ void fwd_pass16_digit(uint64_t *a, const ulonglong2 *__restrict__ tw, const Ntt64Consts &c,
+                                                 int tid, const DigitTables64 &T)
+{
+    for (int j = tid; j < 128; j += G) {
+        uint64_t x[16];
+#pragma unroll
+        for (int k = 0; k < 16; k++) x[k] = a[j + k * 128];
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const uint64_t x0 = x[r];
+            const uint64_t av = T.t1[x[r + 8]];
+            const ulonglong2 bd = T.t23[x[r + 4]], ce = T.t123[x[r + 12]];
+            x[r] = x0 + av + bd.x + ce.x;
+            x[r + 4] = x0 + av + (c.twoQ - bd.x - ce.x);
+            x[r + 8] = x0 + (c.twoQ - av - ce.y) + bd.y;
+            x[r + 12] = x0 + (c.twoQ - av - bd.y) + ce.y;
+        }
+#pragma unroll
+        for (int st = 2; st < 4; st++) {
+            const int d = 16 >> (st + 1);
+#pragma unroll
+            for (int k = 0; k < 16; k++) {
+                if (k & d) continue;
+                ct64(x[k], x[k + d], __ldg(tw + (1 << st) + (k >> (4 - st))), c.Q, c.twoQ);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < 16; k++) a[j + k * 128] = x[k];
+    }
+}
+
+// Forward NTT of a digit polynomial (values < BG) as ntt64_fwd_2048, the
+// first two stages from the digit tables; output < 21Q + BG.
+template <int G>
+__device__ __forceinline__ void ntt64_fwd_2048_digit(uint64_t *a, const ulonglong2 *__restrict__ tw,
+                                                     const Ntt64Consts &c, int tid, int bar, const DigitTables64 &T)
+{
+    fwd_pass16_digit<G>(a, tw, c, tid, T);      // t = 1024 .. 128
+    group_sync(bar, G);
+    fwd_passR<G, 4>(a, tw, c, tid, 64, 16);    // t = 64 .. 8
+    group_sync(bar, G);
+    fwd_passR<G, 3>(a, tw, c, tid, 4, 256);    // t = 4, 2, 1
+    group_sync(bar, G);
+}
+
 // One radix-8 inverse pass: stages t, 2t, 4t (m = N / 2t) on the octets
 // e0 + k t (k < 8) of every 8t-block.
 template <int G>

@@ -222,7 +222,7 @@ int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t cou
  *  FHEACC_OPT_BR_PIPES      : pipelines (32-bit words) or workers (64-bit)
  *                             per CTA, 1..3; 0 = default: 32-bit 1 up to 2
  *                             gates per SM, 2 up to 5, else 3; 64-bit 1 up to
- *                             1 gate per SM, 2 up to 3, else 3. The pipelines of a CTA
+ *                             1 gate per SM, else 2. The pipelines of a CTA
  *                             share its group of ciphertexts item by item, so
  *                             they finish together; with one per CTA, up to 3
  *                             CTAs share an SM and finish at different times.
