@@ -54,11 +54,17 @@ def test_plain_equals_batched(F, ctx0, keys0, cuda_ok):
     assert np.array_equal(ob.cpu().numpy().view(np.uint64), ctx0.eval_bootstrap_batch(c1, c2, g))
 
 
-def test_fpga_compat_mode(F, ctx0, keys0):
+@pytest.mark.parametrize("pipes", [0, 1, 2, 3])
+def test_fpga_compat_mode(F, ctx0, keys0, pipes):
     """The no-skip issue order of fpga_eval_bootstrap_x4..x16
-    (myfpga.cpp:1200-1210) against the oracle run the same way."""
-    x, y, g, c1, c2 = random_gate_batch(keys0, 3, seed=3)
-    out = ctx0.eval_bootstrap_batch(c1, c2, g, flags=F.FLAG_FPGA_COMPAT)
+    (myfpga.cpp:1200-1210) against the oracle run the same way, with every
+    number of pipelines per CTA (their shared cursor then issues every step)."""
+    x, y, g, c1, c2 = random_gate_batch(keys0, 7, seed=3)
+    ctx0.set_option(F.OPT_BR_PIPES, pipes)
+    try:
+        out = ctx0.eval_bootstrap_batch(c1, c2, g, flags=F.FLAG_FPGA_COMPAT)
+    finally:
+        ctx0.set_option(F.OPT_BR_PIPES, 0)
     want, failed = keys0.oracle.eval_bootstrap_batch(c1, c2, g, keys0.btkey, keys0.kskey, fpga_compat=True)
     assert np.array_equal(out, want)
     truth = np.array([F.gate_truth(int(a), b, c) for a, b, c in zip(g, x, y)], dtype=np.uint8)

@@ -125,3 +125,17 @@ def test_wide_several_rounds(F, ctx1, keys1):
     want, failed = keys1.oracle.eval_bootstrap_batch(c1[idx], c2[idx], g[idx], keys1.btkey, keys1.kskey)
     assert failed == 0
     assert np.array_equal(out[idx], want)
+
+
+@pytest.mark.parametrize("pipes", [1, 2])
+def test_wide_fpga_compat_mode(F, ctx1, keys1, pipes):
+    """The no-skip issue order (myfpga.cpp:1200-1210) on the 64-bit path with
+    one and two workers per CTA, against the oracle run the same way."""
+    x, y, g, c1, c2 = random_gate_batch(keys1, 4, seed=41)
+    ctx1.set_option(F.OPT_BR_PIPES, pipes)
+    try:
+        out = ctx1.eval_bootstrap_batch(c1, c2, g, flags=F.FLAG_FPGA_COMPAT)
+    finally:
+        ctx1.set_option(F.OPT_BR_PIPES, 0)
+    want, failed = keys1.oracle.eval_bootstrap_batch(c1, c2, g, keys1.btkey, keys1.kskey, fpga_compat=True)
+    assert np.array_equal(out, want)
