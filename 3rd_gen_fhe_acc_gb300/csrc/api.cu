@@ -85,7 +85,8 @@ int bootstrap_device_with(Context &c, const uint64_t *d_c1, const uint64_t *d_c2
     if (!c.d_kskey) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
     int rc = launch_blind_rotate32_with(c, d_c1, d_c2, d_gates, count, flags, (uint32_t *)accs, (uint32_t *)extract,
                                         st);
-    return rc ? rc : launch_lwe_keyswitch32(c, (const uint32_t *)extract, count, true, d_out, st);
+    // the accumulators are free once the blind rotation is done
+    return rc ? rc : launch_lwe_keyswitch32(c, (const uint32_t *)extract, count, true, d_out, st, (uint64_t *)accs);
 }
 
 int bootstrap_device(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
@@ -116,7 +117,8 @@ int bootstrap_device(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, con
     rc = launch_blind_rotate32(c, d_c1, d_c2, d_gates, count, flags, nullptr, ext, max_ctas, st);
     if (rc) return rc;
     if (prof) cudaEventRecord(c.prof[1], st);
-    rc = launch_lwe_keyswitch32(c, ext, count, true, d_out, st);
+    // the accumulator scratch is free once the blind rotation is done
+    rc = launch_lwe_keyswitch32(c, ext, count, true, d_out, st, (uint64_t *)c.accs.ptr);
     if (prof && rc == FHEACC_OK) cudaEventRecord(c.prof[2], st);
     return rc;
 }

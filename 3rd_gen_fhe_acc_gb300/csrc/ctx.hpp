@@ -166,8 +166,10 @@ int launch_lwe_keyswitch32_indexed(Context &c, const uint32_t *d_extract, size_t
                                    uint64_t *d_out, const uint32_t *d_out_idx, cudaStream_t st);
 // LWE key switch (+ optional modulus switch) from extracted RLWEs
 // (lwe_ks.cu).
+// d_partials (optional, count * ks_row u64 words of free scratch): lets a few
+// ciphertexts' rows be split over many CTAs.
 int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
-                           cudaStream_t st);
+                           cudaStream_t st, uint64_t *d_partials = nullptr);
 int launch_extract_from_ntt32(Context &c, const uint64_t *d_rlwe, size_t count, uint32_t *d_extract,
                               cudaStream_t st);
 int launch_modswitch(Context &c, const uint64_t *d_in, size_t count, uint64_t *d_out, cudaStream_t st);

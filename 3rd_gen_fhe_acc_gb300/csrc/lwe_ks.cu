@@ -107,6 +107,55 @@ __global__ void __launch_bounds__(kKsMaxThreads) lwe_ks32_kernel(const __grid_co
     }
 }
 
+// Split form for a few ciphertexts (the one-gate launches): CTA (ci, slice)
+// sums rows [slice * rows_per, ...) of ciphertext ci and adds its 64-bit
+// partial sums into part[ci][ks_row] (zeroed before; the sums stay below
+// N * digitKS * Q < 2^64); ks_final_kernel reduces them.
+__global__ void __launch_bounds__(kKsMaxThreads) ks_partial_kernel(const __grid_constant__ KsArgs A,
+                                                                   unsigned long long *part, int slices)
+{
+    const int N = A.N, D = A.digitKS, t = threadIdx.x;
+    const size_t rs4 = A.ks_row / 4;
+    const uint4 *key4 = reinterpret_cast<const uint4 *>(A.kskey);
+    const int total = N * D, per = (total + slices - 1) / slices;
+    const size_t ci = blockIdx.x / slices;
+    const int r0 = (int)(blockIdx.x % slices) * per, r1 = min(total, r0 + per);
+    if (ci >= A.count) return;
+    const uint32_t *ext = A.ext + ci * kExtractStride;
+    uint64_t s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    for (int r = r0; r < r1; r++) {
+        const int i = r / D, j = r - i * D;
+        uint32_t a = ext[i];
+        for (int jj = 0; jj < j; jj++) a /= A.Bks;
+        const uint32_t d = a % A.Bks;
+        const uint4 v = __ldg(key4 + ((size_t)(d * D + j) * N + i) * rs4 + t);
+        s0 += v.x;
+        s1 += v.y;
+        s2 += v.z;
+        s3 += v.w;
+    }
+    unsigned long long *p = part + ci * A.ks_row + 4 * (size_t)t;
+    atomicAdd(p + 0, (unsigned long long)s0);
+    atomicAdd(p + 1, (unsigned long long)s1);
+    atomicAdd(p + 2, (unsigned long long)s2);
+    atomicAdd(p + 3, (unsigned long long)s3);
+}
+
+__global__ void ks_final_kernel(const __grid_constant__ KsArgs A, const unsigned long long *part)
+{
+    const uint32_t Q = (uint32_t)A.Q, Q8 = Q / 8 + 1;
+    const size_t w = (size_t)A.n + 1;
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < A.count * w; x += (size_t)gridDim.x * blockDim.x) {
+        const size_t ci = x / w;
+        const int k = (int)(x - ci * w);
+        const uint64_t sm = part[ci * A.ks_row + k] % Q;
+        uint64_t v;
+        if (k < A.n) v = sm ? Q - sm : 0;
+        else v = ((uint64_t)(A.ext[ci * kExtractStride + A.N] + Q8) % Q + Q - sm) % Q;
+        A.out[x] = A.modswitch ? scale_round_dev(v, A.q, A.Q) : v;
+    }
+}
+
 __global__ void modswitch_kernel(const uint64_t *__restrict__ in, uint64_t *__restrict__ out, size_t words,
                                  uint64_t q, uint64_t Q)
 {
@@ -117,9 +166,32 @@ __global__ void modswitch_kernel(const uint64_t *__restrict__ in, uint64_t *__re
 }  // namespace dev
 
 int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
-                           cudaStream_t st)
+                           cudaStream_t st, uint64_t *d_partials)
 {
-    return launch_lwe_keyswitch32_indexed(c, d_extract, count, modswitch, d_out, nullptr, st);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
+    // a few ciphertexts: split each one's rows over many CTAs
+    if (!d_partials || count == 0 || count >= 2 * (size_t)std::max(sms, 1) || !c.d_kskey ||
+        c.p.n + 1 > 4 * dev::kKsMaxThreads)
+        return launch_lwe_keyswitch32_indexed(c, d_extract, count, modswitch, d_out, nullptr, st);
+    dev::KsArgs A{};
+    A.ext = d_extract; A.count = count; A.kskey = c.d_kskey; A.out = d_out; A.out_idx = nullptr;
+    A.n = c.p.n; A.N = c.p.N; A.digitKS = (int)c.p.digitKS; A.Bks = c.p.Bks; A.ks_row = c.dp.ks_row;
+    A.q = c.p.q; A.modswitch = modswitch ? 1u : 0u; A.Q = c.p.Q;
+    const int rows = c.p.N * (int)c.p.digitKS;
+    // about 8 CTAs per SM, at least 48 rows each
+    const int slices = (int)std::max<size_t>(1, std::min<size_t>((size_t)rows / 48, (size_t)sms * 8 / count));
+    cudaError_t e = cudaMemsetAsync(d_partials, 0, count * c.dp.ks_row * sizeof(uint64_t), st);
+    if (e != cudaSuccess) return c.cuda_fail(e, "key switch partials reset");
+    dev::ks_partial_kernel<<<(unsigned)(count * slices), c.dp.ks_row / 4, 0, st>>>(
+        A, reinterpret_cast<unsigned long long *>(d_partials), slices);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return c.cuda_fail(e, "key switch partial launch");
+    const size_t words = count * ((size_t)c.p.n + 1);
+    dev::ks_final_kernel<<<(unsigned)std::min<size_t>((words + 255) / 256, 1024), 256, 0, st>>>(
+        A, reinterpret_cast<const unsigned long long *>(d_partials));
+    e = cudaGetLastError();
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "key switch final launch");
 }
 
 int launch_lwe_keyswitch32_indexed(Context &c, const uint32_t *d_extract, size_t count, bool modswitch,

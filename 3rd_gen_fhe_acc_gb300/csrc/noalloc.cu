@@ -78,7 +78,7 @@ extern "C" int fheacc_bootstrap_noalloc(fheacc_ctx *ctx, const uint64_t *d_c1, c
         cudaStream_t st = (cudaStream_t)stream;
         uint32_t *accs = scratch, *ext = scratch + kNoAllocAccWords;
         rc = launch_blind_rotate32_with(c, d_c1, d_c2, d_gates, count, flags, accs, ext, st);
-        if (rc == FHEACC_OK) rc = launch_lwe_keyswitch32(c, ext, count, true, d_out, st);
+        if (rc == FHEACC_OK) rc = launch_lwe_keyswitch32(c, ext, count, true, d_out, st, (uint64_t *)accs);
         if (rc == FHEACC_OK) {
             cudaError_t e = cudaEventRecord(c.done, st);
             if (e != cudaSuccess) rc = c.cuda_fail(e, "event record");
