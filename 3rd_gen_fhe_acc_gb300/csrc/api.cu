@@ -166,6 +166,19 @@ int build_tables64(Context &c)
     k.iw1N = host::mulmod(T.irou[1], c.p.iN, Q);
     k.iw1Ns = shoup64_companion(k.iw1N, Q);
     k.mu64 = c.dp.mu64;
+    // factors of the last-digit identity (DevParams::last_digit_from_acc), for
+    // the bootstrap key and for every RGSW a RLWE x RGSW product takes:
+    // BG^(h - digitG + 1) for h < digitG - 1, BG^-(digitG - 1) for the last row
+    const uint64_t dG = c.p.digitG;
+    const uint64_t bg_inv = host::powmod(((uint64_t)1 << c.p.BG_bits) % Q, Q - 2, Q);
+    std::vector<ulonglong2> cf(dG);
+    for (uint64_t h = 0; h < dG; h++) {
+        const uint64_t f = host::powmod(bg_inv, h + 1 < dG ? dG - 1 - h : dG - 1, Q);
+        cf[h] = make_ulonglong2(f, shoup64_companion(f, Q));
+    }
+    e = cudaMalloc(&c.d_cf64, dG * sizeof(ulonglong2));
+    if (e == cudaSuccess) e = cudaMemcpy(c.d_cf64, cf.data(), dG * sizeof(ulonglong2), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return c.cuda_fail(e, "key factors");
     return FHEACC_OK;
 }
 
@@ -350,6 +363,7 @@ int fheacc_destroy(fheacc_ctx *ctx)
     cudaFree(c->d_tw64);
     cudaFree(c->d_itw64);
     cudaFree(c->d_btkey64);
+    cudaFree(c->d_cf64);
     cudaFree(c->d_kskey64);
     cudaFree(c->d_subs64);
     cudaFree(c->d_rot);
@@ -410,24 +424,9 @@ int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t w
         }
         std::vector<uint64_t> stage(Br * rw);
         uint64_t *d_stage = nullptr;
-        ulonglong2 *d_cf = nullptr;
         cudaError_t e = cudaMalloc(&d_stage, Br * rw * sizeof(uint64_t));
-        if (e == cudaSuccess) e = cudaMalloc(&d_cf, c.p.digitG * sizeof(ulonglong2));
-        if (e != cudaSuccess) {
-            cudaFree(d_stage);
-            return c.cuda_fail(e, "key staging");
-        }
-        // factors of the last-digit identity (DevParams::last_digit_from_acc):
-        // BG^(h - digitG + 1) for h < digitG - 1, BG^-(digitG - 1) for the last row
-        const uint64_t dG = c.p.digitG;
-        const uint64_t bg_inv = host::powmod(((uint64_t)1 << c.p.BG_bits) % Q, Q - 2, Q);
-        std::vector<ulonglong2> cf(dG);
-        for (uint64_t h = 0; h < dG; h++) {
-            const uint64_t f = host::powmod(bg_inv, h + 1 < dG ? dG - 1 - h : dG - 1, Q);
-            cf[h] = make_ulonglong2(f, (uint64_t)(((unsigned __int128)f << 64) / Q));
-        }
-        e = cudaMemcpy(d_cf, cf.data(), dG * sizeof(ulonglong2), cudaMemcpyHostToDevice);
-        int rc = e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "key factors");
+        if (e != cudaSuccess) return c.cuda_fail(e, "key staging");
+        int rc = FHEACC_OK;
         const bool derive = c.dp.last_digit_from_acc != 0;
         for (size_t i = 0; i < n && !rc; i++) {
             for (size_t j = 0; j < dR && !rc; j++) {
@@ -435,13 +434,12 @@ int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t w
                     std::memcpy(stage.data() + r * rw, btkey + ((r * dR + j) * n + i) * rw, rw * sizeof(uint64_t));
                 e = cudaMemcpy(d_stage, stage.data(), Br * rw * sizeof(uint64_t), cudaMemcpyHostToDevice);
                 if (e != cudaSuccess) rc = c.cuda_fail(e, "key upload");
-                else if (derive) rc = launch_derive_keys64(c, d_stage, Br, d_cf, c.stream);
+                else if (derive) rc = launch_derive_keys64(c, d_stage, Br, c.d_cf64, c.stream);
                 if (!rc) rc = launch_shoup_pairs64(c, d_stage, c.d_btkey64 + (i * dR + j) * Br * rw, Br * rw, c.stream);
                 if (!rc && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = c.cuda_fail(cudaGetLastError(), "key pairs");
             }
         }
         cudaFree(d_stage);
-        cudaFree(d_cf);
         return rc;
     }
     if (!c.d_btkey) {

@@ -184,19 +184,22 @@ __global__ void shoup_pairs64_kernel(const uint64_t *__restrict__ in, ulonglong2
 }
 
 // RLWE_mult_RGSW of count (acc, RGSW-pairs) in reference order; acc canonical.
+// derive: the RGSWs carry the last-digit identity (derive_keys64_kernel) and the
+// last digit's NTT is the input accumulator itself.
 __global__ void __launch_bounds__(kT64) rlwe_mult_rgsw64_kernel(const uint64_t *__restrict__ acc_in,
                                                                const ulonglong2 *__restrict__ rgsw, uint64_t *acc_out,
                                                                size_t count, size_t rgsw_stride, int DG, uint32_t bg_bits,
                                                                const ulonglong2 *__restrict__ tw,
                                                                const ulonglong2 *__restrict__ itw,
-                                                               const __grid_constant__ Ntt64Consts c)
+                                                               const __grid_constant__ Ntt64Consts c, int derive)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Step64Smem &s = *reinterpret_cast<Step64Smem *>(smem_raw);
     for (size_t ci = blockIdx.x; ci < count; ci += gridDim.x) {
         for (int e = threadIdx.x; e < 4096; e += kT64) s.acc[e >> 11][e & 2047] = acc_in[ci * 4096 + e];
         __syncthreads();
-        step64(s, rgsw + ci * rgsw_stride, DG, bg_bits, tw, itw, c, nullptr, threadIdx.x, 1);
+        step64(s, rgsw + ci * rgsw_stride, DG, bg_bits, tw, itw, c, derive ? acc_in + ci * 4096 : nullptr,
+               threadIdx.x, 1);
         for (int e = threadIdx.x; e < 4096; e += kT64) {
             const uint64_t v = s.acc[e >> 11][e & 2047];
             acc_out[ci * 4096 + e] = v >= c.Q ? v - c.Q : v;
@@ -581,10 +584,24 @@ int launch_rlwe_mult_rgsw64(Context &c, const uint64_t *d_acc, const uint64_t *d
     const size_t rw = (size_t)c.p.digitG * 4 * 2048;
     if (stride != 0 && stride != rw) return c.fail(FHEACC_EINVAL, "RGSW stride: 0 or one RGSW");
     const size_t words = (stride ? count : 1) * rw;
-    int rc = ensure_scratch(c, c.io, words * sizeof(ulonglong2));
+    // Shoup pairs of the RGSWs, after the last-digit identity when it applies
+    // (2 of the 2 digitG digit NTTs of a product saved); a call of a few
+    // products keeps the plain RGSWs, whose derivation would cost it more
+    // (PSI query: homo_expand 7.87 -> 7.51 ms, its 1-item CMUXes 0.79 -> 0.90 ms)
+    const bool derive = c.dp.last_digit_from_acc && c.d_cf64 && count >= 16;
+    int rc = ensure_scratch(c, c.io, words * (sizeof(ulonglong2) + (derive ? sizeof(uint64_t) : 0)));
     if (rc) return rc;
     ulonglong2 *pairs = (ulonglong2 *)c.io.ptr;
-    rc = launch_shoup_pairs64(c, d_rgsw, pairs, words, st);
+    const uint64_t *src = d_rgsw;
+    if (derive) {
+        uint64_t *staged = reinterpret_cast<uint64_t *>(pairs + words);
+        cudaError_t e = cudaMemcpyAsync(staged, d_rgsw, words * sizeof(uint64_t), cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return c.cuda_fail(e, "RGSW staging");
+        rc = launch_derive_keys64(c, staged, words / rw, c.d_cf64, st);
+        if (rc) return rc;
+        src = staged;
+    }
+    rc = launch_shoup_pairs64(c, src, pairs, words, st);
     if (rc) return rc;
     // no digit tables here: their 20 KB of shared memory cost this kernel more
     // L1 (twiddles, the shared RGSW) than they saved (homo_expand 7.9 -> 8.4 ms)
@@ -592,7 +609,7 @@ int launch_rlwe_mult_rgsw64(Context &c, const uint64_t *d_acc, const uint64_t *d
     cudaFuncSetAttribute(dev::rlwe_mult_rgsw64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     size_t blocks = std::min<size_t>(count, (size_t)sms_of(c) * 2);
     dev::rlwe_mult_rgsw64_kernel<<<(unsigned)blocks, dev::kT64, smem, st>>>(
-        d_acc, pairs, d_out, count, stride, (int)c.p.digitG, c.p.BG_bits, c.d_tw64, c.d_itw64, c.nc64);
+        d_acc, pairs, d_out, count, stride, (int)c.p.digitG, c.p.BG_bits, c.d_tw64, c.d_itw64, c.nc64, derive ? 1 : 0);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "rlwe_mult_rgsw64 launch");
 }

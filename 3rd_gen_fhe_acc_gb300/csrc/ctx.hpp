@@ -95,6 +95,7 @@ struct Context {
     ulonglong2 *d_tw64 = nullptr, *d_itw64 = nullptr;
     dev::Ntt64Consts nc64{};
     ulonglong2 *d_btkey64 = nullptr;   // Shoup pairs, [(i*digitR + j)*Br + r][digitG][2][2][N]
+    ulonglong2 *d_cf64 = nullptr;      // factors of the last-digit identity, digitG Shoup pairs
     ulonglong2 *d_subs64 = nullptr;    // Shoup pairs, [logN][digitKS_R][2][N]
     uint64_t *d_rot = nullptr;         // [logN][N]: NTT(-X^(N - 2^j)), rotate_vector_gen(false)
     uint64_t *d_rot_fwd = nullptr;     // [logN][N]: NTT(X^(2^j)), rotate_vector_gen(true)

@@ -139,3 +139,21 @@ def test_wide_fpga_compat_mode(F, ctx1, keys1, pipes):
         ctx1.set_option(F.OPT_BR_PIPES, 0)
     want, failed = keys1.oracle.eval_bootstrap_batch(c1, c2, g, keys1.btkey, keys1.kskey, fpga_compat=True)
     assert np.array_equal(out, want)
+
+
+def test_wide_rlwe_mult_rgsw_batch(F, ctx1, keys1, cuda_ok):
+    """20 products, one RGSW each: the launch applies the last-digit identity
+    to the RGSWs (from 16 products on) and still gives the oracle's words."""
+    torch = cuda_ok
+    o = keys1.oracle
+    Q = keys1.P.Q
+    rng = np.random.default_rng(12)
+    acc = rng.integers(0, Q, (20, 4096), dtype=np.uint64)
+    acc[0] = Q - 1
+    acc[1] = 0
+    rgsw = rng.integers(0, Q, (20, 6 * 4 * 2048), dtype=np.uint64)
+    out = torch.zeros((20, 4096), dtype=torch.int64, device="cuda")
+    da, dr = dev(torch, acc), dev(torch, rgsw)
+    ctx1.rlwe_mult_rgsw(da.data_ptr(), dr.data_ptr(), out.data_ptr(), 20)
+    torch.cuda.synchronize()
+    assert np.array_equal(host(out), np.stack([o.rlwe_mult_rgsw(acc[i], rgsw[i]) for i in range(20)]))
