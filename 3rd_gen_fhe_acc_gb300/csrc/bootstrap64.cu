@@ -27,9 +27,12 @@ namespace dev {
 constexpr int kMaxGroup64 = 8;   // ciphertexts per worker and claim
 constexpr int kT64 = 256;   // threads per CTA
 
-struct Step64Smem {
-    uint64_t acc[2][2048];   // accumulator; time domain inside a step
-    uint64_t buf[2][2048];   // digit NTTs
+// One worker's polys in shared memory, layout pi<P> (ntt64.cuh): padded in the
+// blind rotation, plain in the RLWE x RGSW kernel (whose L1 the padding costs).
+template <bool P>
+struct Step64SmemT {
+    uint64_t acc[2][poly_words64<P>()];   // accumulator; time domain inside a step
+    uint64_t buf[2][poly_words64<P>()];   // digit NTTs
 };
 
 constexpr int kMaxTableBG64 = 512;   // largest gadget base with digit tables (40 BG bytes of shared memory)
@@ -65,13 +68,14 @@ __device__ __forceinline__ DigitTables64 build_digit_tables64(unsigned char *mem
 // keys were uploaded with K'_h = K_h - BG^(h-DG+1) K_last, K'_last =
 // BG^-(DG-1) K_last (Q < BG^DG, so sum_h BG^h NTT(digit_h) = acc).
 // With dt the digit transforms start from the digit tables (BG <= kMaxTableBG64).
-__device__ __forceinline__ void step64(Step64Smem &s, const ulonglong2 *__restrict__ key, int DG, uint32_t bg_bits,
+template <bool P>
+__device__ __forceinline__ void step64(Step64SmemT<P> &s, const ulonglong2 *__restrict__ key, int DG, uint32_t bg_bits,
                                        const ulonglong2 *__restrict__ tw, const ulonglong2 *__restrict__ itw,
                                        const Ntt64Consts &c, const uint64_t *acc_nd, int tid, int bar,
                                        const DigitTables64 *dt = nullptr)
 {
     const int grp = tid >> 7, gtid = tid & 127;
-    ntt64_inv_2048<128>(s.acc[grp], itw, c, gtid, bar + 1 + grp);
+    ntt64_inv_2048<128, P>(s.acc[grp], itw, c, gtid, bar + 1 + grp);
     group_sync(bar, kT64);
     uint64_t sa[8], sb[8];
 #pragma unroll
@@ -80,17 +84,17 @@ __device__ __forceinline__ void step64(Step64Smem &s, const ulonglong2 *__restri
     const int DH = acc_nd ? DG - 1 : DG;   // digits transformed
     for (int h = 0; h < DH; h++) {
         const uint32_t sh = bg_bits * h;
-        for (int e = gtid; e < 2048; e += 128) s.buf[grp][e] = (s.acc[grp][e] >> sh) & mask;
+        for (int e = gtid; e < 2048; e += 128) s.buf[grp][pi<P>(e)] = (s.acc[grp][pi<P>(e)] >> sh) & mask;
         group_sync(bar + 1 + grp, 128);
-        if (dt) ntt64_fwd_2048_digit<128>(s.buf[grp], tw, c, gtid, bar + 1 + grp, *dt);
-        else ntt64_fwd_2048<128>(s.buf[grp], tw, c, gtid, bar + 1 + grp);
+        if (dt) ntt64_fwd_2048_digit<128, P>(s.buf[grp], tw, c, gtid, bar + 1 + grp, *dt);
+        else ntt64_fwd_2048<128, P>(s.buf[grp], tw, c, gtid, bar + 1 + grp);
         group_sync(bar, kT64);
         const ulonglong2 *k0 = key + (size_t)(h * 2 + 0) * 2 * 2048;   // row c_text[h][0]: times digit of a
         const ulonglong2 *k1 = key + (size_t)(h * 2 + 1) * 2 * 2048;   // row c_text[h][1]: times digit of b
 #pragma unroll
         for (int i = 0; i < 8; i++) {
             const int k = tid + 256 * i;
-            const uint64_t da = s.buf[0][k], db = s.buf[1][k];
+            const uint64_t da = s.buf[0][pi<P>(k)], db = s.buf[1][pi<P>(k)];
             const ulonglong2 a0 = __ldg(k0 + k), b0 = __ldg(k0 + 2048 + k);
             const ulonglong2 a1 = __ldg(k1 + k), b1 = __ldg(k1 + 2048 + k);
             sa[i] += shoup64(da, a0.x, a0.y, c.Q) + shoup64(db, a1.x, a1.y, c.Q);
@@ -114,8 +118,8 @@ __device__ __forceinline__ void step64(Step64Smem &s, const ulonglong2 *__restri
 #pragma unroll
     for (int i = 0; i < 8; i++) {
         const int k = tid + 256 * i;
-        s.acc[0][k] = barrett64_2q(sa[i], c.mu64, c.Q);
-        s.acc[1][k] = barrett64_2q(sb[i], c.mu64, c.Q);
+        s.acc[0][pi<P>(k)] = barrett64_2q(sa[i], c.mu64, c.Q);
+        s.acc[1][pi<P>(k)] = barrett64_2q(sb[i], c.mu64, c.Q);
     }
     group_sync(bar, kT64);
 }
@@ -134,8 +138,8 @@ __global__ void __launch_bounds__(kT64) ntt64_kernel(uint64_t *polys, size_t cou
         uint64_t *poly = polys + pi * 2048;
         for (int e = gtid; e < 2048; e += 128) buf[grp][e] = live ? poly[e] : 0;
         group_sync(1 + grp, 128);
-        if (INV) ntt64_inv_2048<128>(buf[grp], tw, c, gtid, 1 + grp);
-        else ntt64_fwd_2048<128>(buf[grp], tw, c, gtid, 1 + grp);
+        if (INV) ntt64_inv_2048<128, false>(buf[grp], tw, c, gtid, 1 + grp);
+        else ntt64_fwd_2048<128, false>(buf[grp], tw, c, gtid, 1 + grp);
         if (live) {
             for (int e = gtid; e < 2048; e += 128) {
                 uint64_t v = buf[grp][e];
@@ -194,7 +198,7 @@ __global__ void __launch_bounds__(kT64) rlwe_mult_rgsw64_kernel(const uint64_t *
                                                                const __grid_constant__ Ntt64Consts c, int derive)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    Step64Smem &s = *reinterpret_cast<Step64Smem *>(smem_raw);
+    Step64SmemT<false> &s = *reinterpret_cast<Step64SmemT<false> *>(smem_raw);
     for (size_t ci = blockIdx.x; ci < count; ci += gridDim.x) {
         for (int e = threadIdx.x; e < 4096; e += kT64) s.acc[e >> 11][e & 2047] = acc_in[ci * 4096 + e];
         __syncthreads();
@@ -249,7 +253,7 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
                                                           const __grid_constant__ Ntt64Consts c)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint8_t *res = smem_raw + W * sizeof(Step64Smem);   // [group][n * digitR]
+    uint8_t *res = smem_raw + W * sizeof(Step64SmemT<true>);   // [group][n * digitR]
     __shared__ uint32_t bvals[kMaxGroup64 * W], b1s[kMaxGroup64 * W], b2s[kMaxGroup64 * W];
     __shared__ int done[kMaxGroup64 * W];
     __shared__ int plan[W][2];
@@ -257,7 +261,7 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
     __shared__ unsigned long long claim_first;
     __shared__ int claim_m;
     const int wk = threadIdx.x / kT64, tid = threadIdx.x - wk * kT64, bar = 1 + 3 * wk;
-    Step64Smem &s = reinterpret_cast<Step64Smem *>(smem_raw)[wk];
+    Step64SmemT<true> &s = reinterpret_cast<Step64SmemT<true> *>(smem_raw)[wk];
     const int n = A.n, S = n * (int)A.digitR;
     const uint32_t q = A.q, qmask = q - 1;
     const size_t rgsw_pairs = (size_t)A.DG * 4 * 2048;
@@ -318,15 +322,15 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
                     if (b1 < b2) v = (tmp >= b1 && tmp < b2) ? negQ8 : Q8;
                     else v = (tmp >= b2 && tmp < b1) ? Q8 : negQ8;
                 }
-                s.buf[1][e] = v;
+                s.buf[1][px(e)] = v;
             }
             group_sync(bar, kT64);
-            if (tid >= 128) ntt64_fwd_2048<128>(s.buf[1], tw, c, tid - 128, bar + 2);
+            if (tid >= 128) ntt64_fwd_2048<128, true>(s.buf[1], tw, c, tid - 128, bar + 2);
             group_sync(bar, kT64);
             uint64_t *acc = A.accs + gid * 4096;
             for (int e = tid; e < 2048; e += kT64) {
                 acc[e] = 0;
-                uint64_t v = barrett64_2q(s.buf[1][e], c.mu64, c.Q);
+                uint64_t v = barrett64_2q(s.buf[1][px(e)], c.mu64, c.Q);
                 acc[2048 + e] = v >= c.Q ? v - c.Q : v;
             }
             group_sync(bar, kT64);
@@ -382,11 +386,11 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
             if (st < 0) break;
             const uint32_t r = res[k * S + st];
             uint64_t *acc = A.accs + (first + (size_t)k) * 4096;
-            for (int e = tid; e < 4096; e += kT64) s.acc[e >> 11][e & 2047] = __ldcg(acc + e);
+            for (int e = tid; e < 4096; e += kT64) s.acc[e >> 11][px(e & 2047)] = __ldcg(acc + e);
             group_sync(bar, kT64);
             step64(s, A.btkey + ((size_t)st * A.Br + r) * rgsw_pairs, A.DG, A.bg_bits, tw, itw, c,
                    A.derive_last ? acc : nullptr, tid, bar, A.digit_tables ? &dt : nullptr);
-            for (int e = tid; e < 4096; e += kT64) __stcg(acc + e, s.acc[e >> 11][e & 2047]);
+            for (int e = tid; e < 4096; e += kT64) __stcg(acc + e, s.acc[e >> 11][px(e & 2047)]);
             group_sync(bar, kT64);
             if (tid == 0) {
                 __threadfence_block();
@@ -401,14 +405,14 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
             if (A.extract) {
                 // NTT_a_transpose on poly a, then inverse NTT of both polys
                 for (int e = tid; e < 2048; e += kT64) {
-                    s.acc[0][e] = __ldcg(acc + 2047 - e);
-                    s.acc[1][e] = __ldcg(acc + 2048 + e);
+                    s.acc[0][px(e)] = __ldcg(acc + 2047 - e);
+                    s.acc[1][px(e)] = __ldcg(acc + 2048 + e);
                 }
                 group_sync(bar, kT64);
-                ntt64_inv_2048<128>(s.acc[tid >> 7], itw, c, tid & 127, bar + 1 + (tid >> 7));
+                ntt64_inv_2048<128, true>(s.acc[tid >> 7], itw, c, tid & 127, bar + 1 + (tid >> 7));
                 group_sync(bar, kT64);
                 uint64_t *ext = A.extract + gid * kExtract64;
-                for (int e = tid; e < 2048; e += kT64) ext[e] = s.acc[0][e];
+                for (int e = tid; e < 2048; e += kT64) ext[e] = s.acc[0][px(e)];
                 if (tid == 0) ext[2048] = s.acc[1][0];
             } else {
                 for (int e = tid; e < 4096; e += kT64) {
@@ -442,7 +446,7 @@ __global__ void __launch_bounds__(kT64) extract64_kernel(const uint64_t *__restr
             buf[1][e] = in[2048 + e];
         }
         __syncthreads();
-        ntt64_inv_2048<128>(buf[tid >> 7], itw, c, tid & 127, 1 + (tid >> 7));
+        ntt64_inv_2048<128, false>(buf[tid >> 7], itw, c, tid & 127, 1 + (tid >> 7));
         __syncthreads();
         uint64_t *ext = extract + ci * kExtract64;
         for (int e = tid; e < 2048; e += kT64) ext[e] = buf[0][e];
@@ -605,7 +609,7 @@ int launch_rlwe_mult_rgsw64(Context &c, const uint64_t *d_acc, const uint64_t *d
     if (rc) return rc;
     // no digit tables here: their 20 KB of shared memory cost this kernel more
     // L1 (twiddles, the shared RGSW) than they saved (homo_expand 7.9 -> 8.4 ms)
-    const size_t smem = sizeof(dev::Step64Smem);
+    const size_t smem = sizeof(dev::Step64SmemT<false>);
     cudaFuncSetAttribute(dev::rlwe_mult_rgsw64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     size_t blocks = std::min<size_t>(count, (size_t)sms_of(c) * 2);
     dev::rlwe_mult_rgsw64_kernel<<<(unsigned)blocks, dev::kT64, smem, st>>>(
@@ -637,13 +641,13 @@ static int launch_br64_shape(Context &c, dev::Br64Args A, int max_ctas, cudaStre
     // beside a group of at least kMaxGroup64 per worker (else the group first)
     const size_t tbytes = 40 * ((size_t)1 << c.p.BG_bits);
     A.digit_tables = (1 << c.p.BG_bits) <= dev::kMaxTableBG64 &&
-                     W * sizeof(dev::Step64Smem) + 32 + tbytes + (size_t)cap * steps <= kPipeSmemBudget;
-    const size_t fixed = W * sizeof(dev::Step64Smem) + 32 + (A.digit_tables ? tbytes : 0);
+                     W * sizeof(dev::Step64SmemT<true>) + 32 + tbytes + (size_t)cap * steps <= kPipeSmemBudget;
+    const size_t fixed = W * sizeof(dev::Step64SmemT<true>) + 32 + (A.digit_tables ? tbytes : 0);
     if (fixed + (size_t)cap * steps > kPipeSmemBudget)
         cap = fixed < kPipeSmemBudget ? (int)((kPipeSmemBudget - fixed) / steps) : 0;
     if (cap < 1) return c.fail(FHEACC_EINVAL, "n * digitR too large for the blind rotation's residue table");
     auto smem_of = [&](int group) {
-        return W * sizeof(dev::Step64Smem) + ((size_t)group * steps + 15) / 16 * 16 + (A.digit_tables ? tbytes : 0);
+        return W * sizeof(dev::Step64SmemT<true>) + ((size_t)group * steps + 15) / 16 * 16 + (A.digit_tables ? tbytes : 0);
     };
     size_t smem = smem_of(cap);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

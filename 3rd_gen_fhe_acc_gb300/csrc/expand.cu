@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(256) expand64_kernel(const __grid_constant__ E
         const uint64_t *in = A.in + bo + jt * 4096;
         for (int e = gtid; e < 2048; e += 128) t[grp][e] = in[grp * 2048 + e];
         group_sync(1 + grp, 128);
-        ntt64_inv_2048<128>(t[grp], itw, c, gtid, 1 + grp);
+        ntt64_inv_2048<128, false>(t[grp], itw, c, gtid, 1 + grp);
         __syncthreads();
         // transforms: L digits of sigma(a) and sigma(b) (SUBS: sigma(a), sigma(b)),
         // two at a time; MAC after each pair
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(256) expand64_kernel(const __grid_constant__ E
                     buf[grp][e] = digit ? (v >> sh) & mask : v;
                 }
                 group_sync(1 + grp, 128);
-                ntt64_fwd_2048<128>(buf[grp], tw, c, gtid, 1 + grp);
+                ntt64_fwd_2048<128, false>(buf[grp], tw, c, gtid, 1 + grp);
             }
             __syncthreads();
 #pragma unroll

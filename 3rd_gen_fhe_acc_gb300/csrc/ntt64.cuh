@@ -19,6 +19,20 @@
 namespace fheacc {
 namespace dev {
 
+// Shared-memory layouts of a 2048-word polynomial, chosen by the template
+// parameter P of the transforms: P = false, word e at e; P = true, one padding
+// word after every 8, word e at px(e). Padded, the passes whose threads walk 8
+// consecutive words (the last forward and the first inverse pass) spread a
+// warp over all banks instead of two bank pairs; the offsets of a pass's tuple
+// stay linear in the tuple index (strides 1 within an octet, or multiples of
+// 8). The padding costs shared memory, hence L1, which only some kernels spare.
+constexpr int kPoly64 = 2048 + 256;
+__host__ __device__ __forceinline__ int px(int e) { return e + (e >> 3); }
+template <bool P>
+__host__ __device__ __forceinline__ int pi(int e) { return P ? px(e) : e; }
+template <bool P>
+__host__ __device__ constexpr int poly_words64() { return P ? kPoly64 : 2048; }
+
 struct Ntt64Consts {
     uint64_t Q, twoQ;
     uint64_t iN, iNs;       // N^-1 and its Shoup companion
@@ -61,7 +75,7 @@ __device__ __forceinline__ void group_sync(int bar_id, int threads)
 
 // One radix-2^R forward pass: stages t, t/2, ..., t/2^(R-1) (m = N / 2t) on
 // the tuples e0 + k t/2^(R-1) (k < 2^R) of every 2t-block.
-template <int G, int R>
+template <int G, int R, bool P>
 __device__ __forceinline__ void fwd_passR(uint64_t *a, const ulonglong2 *__restrict__ tw, const Ntt64Consts &c,
                                           int tid, int t, int m)
 {
@@ -72,7 +86,7 @@ __device__ __forceinline__ void fwd_passR(uint64_t *a, const ulonglong2 *__restr
         const int e0 = grp * 2 * t + j;
         uint64_t x[K];
 #pragma unroll
-        for (int k = 0; k < K; k++) x[k] = a[e0 + k * h];
+        for (int k = 0; k < K; k++) x[k] = a[pi<P>(e0 + k * h)];
 #pragma unroll
         for (int st = 0; st < R; st++) {
             const int d = K >> (st + 1);
@@ -83,23 +97,23 @@ __device__ __forceinline__ void fwd_passR(uint64_t *a, const ulonglong2 *__restr
             }
         }
 #pragma unroll
-        for (int k = 0; k < K; k++) a[e0 + k * h] = x[k];
+        for (int k = 0; k < K; k++) a[pi<P>(e0 + k * h)] = x[k];
     }
 }
 
-// Forward NTT of a[2048] in shared memory by `G` threads (tid < G) that share
+// Forward NTT of a[poly_words64<P>()] (layout pi<P>) in shared memory by `G` threads (tid < G) that share
 // the named barrier `bar`. tw[k] = (psi^bitrev(k), companion). Input < Q,
 // output < 23Q, bit-reversed order as the reference's. Two radix-16 passes
 // (stages t = 1024..128, 64..8) and one radix-8 pass (t = 4, 2, 1).
-template <int G>
+template <int G, bool P>
 __device__ __forceinline__ void ntt64_fwd_2048(uint64_t *a, const ulonglong2 *__restrict__ tw, const Ntt64Consts &c,
                                                int tid, int bar)
 {
-    fwd_passR<G, 4>(a, tw, c, tid, 1024, 1);   // t = 1024 .. 128
+    fwd_passR<G, 4, P>(a, tw, c, tid, 1024, 1);   // t = 1024 .. 128
     group_sync(bar, G);
-    fwd_passR<G, 4>(a, tw, c, tid, 64, 16);    // t = 64 .. 8
+    fwd_passR<G, 4, P>(a, tw, c, tid, 64, 16);    // t = 64 .. 8
     group_sync(bar, G);
-    fwd_passR<G, 3>(a, tw, c, tid, 4, 256);    // t = 4, 2, 1
+    fwd_passR<G, 3, P>(a, tw, c, tid, 4, 256);    // t = 4, 2, 1
     group_sync(bar, G);
 }
 
@@ -119,14 +133,14 @@ struct DigitTables64 {
 //   x[r + 8]  = x0 - w1 x2 + w3 x1 - w3 w1 x3
 //   x[r + 12] = x0 - w1 x2 - w3 x1 + w3 w1 x3
 // (each below 3Q + BG), the other two stages are Cooley-Tukey butterflies.
-template <int G>
+template <int G, bool P>
 __device__ __forceinline__ void fwd_pass16_digit(uint64_t *a, const ulonglong2 *__restrict__ tw, const Ntt64Consts &c,
                                                  int tid, const DigitTables64 &T)
 {
     for (int j = tid; j < 128; j += G) {
         uint64_t x[16];
 #pragma unroll
-        for (int k = 0; k < 16; k++) x[k] = a[j + k * 128];
+        for (int k = 0; k < 16; k++) x[k] = a[pi<P>(j + k * 128)];
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             const uint64_t x0 = x[r];
@@ -147,27 +161,27 @@ __device__ __forceinline__ void fwd_pass16_digit(uint64_t *a, const ulonglong2 *
             }
         }
 #pragma unroll
-        for (int k = 0; k < 16; k++) a[j + k * 128] = x[k];
+        for (int k = 0; k < 16; k++) a[pi<P>(j + k * 128)] = x[k];
     }
 }
 
 // Forward NTT of a digit polynomial (values < BG) as ntt64_fwd_2048, the
 // first two stages from the digit tables; output < 21Q + BG.
-template <int G>
+template <int G, bool P>
 __device__ __forceinline__ void ntt64_fwd_2048_digit(uint64_t *a, const ulonglong2 *__restrict__ tw,
                                                      const Ntt64Consts &c, int tid, int bar, const DigitTables64 &T)
 {
-    fwd_pass16_digit<G>(a, tw, c, tid, T);      // t = 1024 .. 128
+    fwd_pass16_digit<G, P>(a, tw, c, tid, T);      // t = 1024 .. 128
     group_sync(bar, G);
-    fwd_passR<G, 4>(a, tw, c, tid, 64, 16);    // t = 64 .. 8
+    fwd_passR<G, 4, P>(a, tw, c, tid, 64, 16);    // t = 64 .. 8
     group_sync(bar, G);
-    fwd_passR<G, 3>(a, tw, c, tid, 4, 256);    // t = 4, 2, 1
+    fwd_passR<G, 3, P>(a, tw, c, tid, 4, 256);    // t = 4, 2, 1
     group_sync(bar, G);
 }
 
 // One radix-8 inverse pass: stages t, 2t, 4t (m = N / 2t) on the octets
 // e0 + k t (k < 8) of every 8t-block.
-template <int G>
+template <int G, bool P>
 __device__ __forceinline__ void inv_pass8(uint64_t *a, const ulonglong2 *__restrict__ itw, const Ntt64Consts &c,
                                           int tid, int t, int m)
 {
@@ -176,7 +190,7 @@ __device__ __forceinline__ void inv_pass8(uint64_t *a, const ulonglong2 *__restr
         const int e0 = grp * 8 * t + j;
         uint64_t x[8];
 #pragma unroll
-        for (int k = 0; k < 8; k++) x[k] = a[e0 + k * t];
+        for (int k = 0; k < 8; k++) x[k] = a[pi<P>(e0 + k * t)];
 #pragma unroll
         for (int k = 0; k < 4; k++) gs64(x[2 * k], x[2 * k + 1], __ldg(itw + m + 4 * grp + k), c.Q, c.twoQ);
         const ulonglong2 w2a = __ldg(itw + (m >> 1) + 2 * grp), w2b = __ldg(itw + (m >> 1) + 2 * grp + 1);
@@ -190,37 +204,37 @@ __device__ __forceinline__ void inv_pass8(uint64_t *a, const ulonglong2 *__restr
         gs64(x[2], x[6], w4, c.Q, c.twoQ);
         gs64(x[3], x[7], w4, c.Q, c.twoQ);
 #pragma unroll
-        for (int k = 0; k < 8; k++) a[e0 + k * t] = x[k];
+        for (int k = 0; k < 8; k++) a[pi<P>(e0 + k * t)] = x[k];
     }
 }
 
-// Inverse NTT of a[2048] (values < 2Q, bit-reversed order) in shared memory
+// Inverse NTT of a[poly_words64<P>()] (layout pi<P>; values < 2Q, bit-reversed order) in shared memory
 // -> canonical coefficients times N^-1. itw[k] = (psi^-bitrev(k), companion).
 // Three radix-8 passes (stages t = 1..4, 8..32, 64..256) and one radix-4 pass
 // (t = 512 and the last stage, t = 1024, with N^-1 folded into both outputs).
-template <int G>
+template <int G, bool P>
 __device__ __forceinline__ void ntt64_inv_2048(uint64_t *a, const ulonglong2 *__restrict__ itw, const Ntt64Consts &c,
                                                int tid, int bar)
 {
-    inv_pass8<G>(a, itw, c, tid, 1, 1024);
+    inv_pass8<G, P>(a, itw, c, tid, 1, 1024);
     group_sync(bar, G);
-    inv_pass8<G>(a, itw, c, tid, 8, 128);
+    inv_pass8<G, P>(a, itw, c, tid, 8, 128);
     group_sync(bar, G);
-    inv_pass8<G>(a, itw, c, tid, 64, 16);
+    inv_pass8<G, P>(a, itw, c, tid, 64, 16);
     group_sync(bar, G);
     for (int b = tid; b < 512; b += G) {
-        uint64_t x0 = a[b], x1 = a[b + 512], x2 = a[b + 1024], x3 = a[b + 1536];
+        uint64_t x0 = a[pi<P>(b)], x1 = a[pi<P>(b + 512)], x2 = a[pi<P>(b + 1024)], x3 = a[pi<P>(b + 1536)];
         gs64(x0, x1, __ldg(itw + 2), c.Q, c.twoQ);   // t = 512, m = 2, block 0
         gs64(x2, x3, __ldg(itw + 3), c.Q, c.twoQ);   // block 1
         // t = 1024, m = 1, with N^-1 folded into both outputs
         uint64_t u = shoup64(x0 + x2, c.iN, c.iNs, c.Q);
         uint64_t v = shoup64(x0 - x2 + c.twoQ, c.iw1N, c.iw1Ns, c.Q);
-        a[b] = u >= c.Q ? u - c.Q : u;
-        a[b + 1024] = v >= c.Q ? v - c.Q : v;
+        a[pi<P>(b)] = u >= c.Q ? u - c.Q : u;
+        a[pi<P>(b + 1024)] = v >= c.Q ? v - c.Q : v;
         u = shoup64(x1 + x3, c.iN, c.iNs, c.Q);
         v = shoup64(x1 - x3 + c.twoQ, c.iw1N, c.iw1Ns, c.Q);
-        a[b + 512] = u >= c.Q ? u - c.Q : u;
-        a[b + 1536] = v >= c.Q ? v - c.Q : v;
+        a[pi<P>(b + 512)] = u >= c.Q ? u - c.Q : u;
+        a[pi<P>(b + 1536)] = v >= c.Q ? v - c.Q : v;
     }
     group_sync(bar, G);
 }
