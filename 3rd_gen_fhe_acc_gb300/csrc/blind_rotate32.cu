@@ -210,6 +210,85 @@ __device__ __forceinline__ void pipe_barrier(int id, int threads)
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
 }
 
+// LWE_evaluate, the residues and acc_initialization of ciphertext gid (one
+// warp; res_k: its row of the residue table; buf: the warp's transpose
+// scratch). Kept out of line, so that its registers do not shape the
+// pipeline loop's allocation.
+__device__ __noinline__ void pipe_init_item(const PipeArgs &A, const Ntt32Consts &c, const uint2 *__restrict__ fwd_tw,
+                                            uint32_t *buf, uint8_t *res_k, size_t gid, int lane, uint32_t mu32)
+{
+    const int n = A.n;
+    const uint32_t q = A.q, qmask = q - 1;
+    const int g = A.gates[gid];
+    const bool x2 = (g == 4 || g == 5);
+    const uint64_t *c1 = A.c1 + (A.idx1 ? (size_t)A.idx1[gid] : gid) * (size_t)(n + 1);
+    const uint64_t *c2 = A.c2 + (A.idx2 ? (size_t)A.idx2[gid] : gid) * (size_t)(n + 1);
+    for (int i = lane; i < n; i += 32) {
+        const uint64_t v = x2 ? 2 * (c1[i] - c2[i]) : c1[i] + c2[i];
+        uint32_t nega = (q - (uint32_t)(v & qmask)) & qmask;
+        for (uint32_t j = 0; j < A.digitR; j++) {
+            res_k[i * (int)A.digitR + (int)j] = (uint8_t)(nega % A.Br);
+            nega /= A.Br;
+        }
+    }
+    const uint64_t vb = x2 ? 2 * (c1[n] - c2[n]) : c1[n] + c2[n];
+    const uint32_t bval = (uint32_t)(vb & qmask);
+    const uint64_t gc = A.gate_constant[(unsigned)g < 6u ? g : 6];
+    const uint32_t b1 = (uint32_t)(gc & qmask), b2 = (b1 + q / 2) & qmask;
+    const uint32_t Q8 = A.tv_pos, negQ8 = A.tv_neg;
+    uint32_t x[32];
+#pragma unroll
+    for (int r = 0; r < 32; r++) {
+        const uint32_t idx = lane + 32 * r;
+        uint32_t v = 0;
+        if (idx % A.embed == 0 && idx / A.embed < q / 2) {
+            const uint32_t tmp = (bval - idx / A.embed) & qmask;
+            if (b1 < b2) v = (tmp >= b1 && tmp < b2) ? negQ8 : Q8;
+            else v = (tmp >= b2 && tmp < b1) ? Q8 : negQ8;
+        }
+        x[r] = v;
+    }
+    ntt_fwd_1024(x, c, fwd_tw, buf, lane);
+#pragma unroll
+    for (int r = 0; r < 32; r++) x[r] = reduce32(x[r], mu32, c.Q);
+    uint32_t *acc = A.accs + gid * 2048;
+    store_btile(acc + 1024, x, lane);
+    uint4 *a4 = reinterpret_cast<uint4 *>(acc);
+#pragma unroll
+    for (int qq = 0; qq < 8; qq++) __stcg(a4 + qq * 32 + lane, make_uint4(0, 0, 0, 0));
+    __syncwarp();
+}
+
+// Output of poly P of ciphertext gid: the canonical NTT accumulator, or the
+// extraction for the key switch (NTT_a_transpose and inverse NTT). One warp,
+// out of line as pipe_init_item.
+__device__ __noinline__ void pipe_out_poly(const PipeArgs &A, const Ntt32Consts &c, const uint2 *__restrict__ inv_tw,
+                                           uint32_t *buf, size_t gid, int P, int lane)
+{
+    const uint32_t *acc = A.accs + gid * 2048 + P * 1024;
+    uint32_t x[32];
+    if (A.extract) {
+        if (P == 0) load_btile_reversed(x, acc, lane);
+        else load_btile(x, acc, lane);
+        ntt_inv_1024_noscale(x, c, inv_tw, buf, lane);
+        uint32_t *ext = A.extract + gid * kExtractStride;
+        if (P == 0) {
+#pragma unroll
+            for (int r = 0; r < 32; r++) ext[lane + 32 * r] = x[r];
+        } else if (lane == 0) {
+            ext[1024] = x[0];
+        }
+    } else {
+        load_btile(x, acc, lane);
+        uint64_t *out = A.acc_out + gid * 2048 + P * 1024 + 32 * lane;
+#pragma unroll
+        for (int r = 0; r < 32; r++) {
+            const uint32_t v = shoup32(x[r], A.nmul, A.nmuls, c.Q);   // times N: the key factor's N^-1 out
+            out[r] = min(v, v - c.Q);
+        }
+    }
+}
+
 // NP pipelines per CTA, each of 2 (digitG - 1) digit warps (the last digit's
 // NTT comes from the accumulator) and 2 inverse-NTT warps, all of whose warps
 // share the MAC; pipeline p synchronises on named barrier 1 + p.
@@ -232,8 +311,7 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int pl = warp / NW, pw = warp - pl * NW;
     PipeSmem<GW> &s = pipes[pl];
-    const int n = A.n, S = n * (int)A.digitR;
-    const uint32_t q = A.q, qmask = q - 1;
+    const int S = A.n * (int)A.digitR;
     const size_t rgsw_words = (size_t)DG * 4 * 1024;
     const bool compat = (A.flags & FHEACC_FLAG_FPGA_COMPAT) != 0;
 
@@ -263,47 +341,9 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
         if (m == 0) break;
 
         // ---- prologue: LWE_evaluate, residues, acc_initialization (one warp per ciphertext)
-        for (int k = warp; k < m; k += NP * NW) {
-            const size_t gid = first + (size_t)k;
-            const int g = A.gates[gid];
-            const bool x2 = (g == 4 || g == 5);
-            const uint64_t *c1 = A.c1 + (A.idx1 ? (size_t)A.idx1[gid] : gid) * (size_t)(n + 1);
-            const uint64_t *c2 = A.c2 + (A.idx2 ? (size_t)A.idx2[gid] : gid) * (size_t)(n + 1);
-            for (int i = lane; i < n; i += 32) {
-                const uint64_t v = x2 ? 2 * (c1[i] - c2[i]) : c1[i] + c2[i];
-                uint32_t nega = (q - (uint32_t)(v & qmask)) & qmask;
-                for (uint32_t j = 0; j < A.digitR; j++) {
-                    res[k * S + i * (int)A.digitR + (int)j] = (uint8_t)(nega % A.Br);
-                    nega /= A.Br;
-                }
-            }
-            const uint64_t vb = x2 ? 2 * (c1[n] - c2[n]) : c1[n] + c2[n];
-            const uint32_t bval = (uint32_t)(vb & qmask);
-            const uint64_t gc = A.gate_constant[(unsigned)g < 6u ? g : 6];
-            const uint32_t b1 = (uint32_t)(gc & qmask), b2 = (b1 + q / 2) & qmask;
-            const uint32_t Q8 = A.tv_pos, negQ8 = A.tv_neg;
-            uint32_t x[32];
-#pragma unroll
-            for (int r = 0; r < 32; r++) {
-                const uint32_t idx = lane + 32 * r;
-                uint32_t v = 0;
-                if (idx % A.embed == 0 && idx / A.embed < q / 2) {
-                    const uint32_t tmp = (bval - idx / A.embed) & qmask;
-                    if (b1 < b2) v = (tmp >= b1 && tmp < b2) ? negQ8 : Q8;
-                    else v = (tmp >= b2 && tmp < b1) ? Q8 : negQ8;
-                }
-                x[r] = v;
-            }
-            ntt_fwd_1024(x, c, fwd_tw, pw < GW ? s.dbuf[pw] : s.tslot[0][pw - GW], lane);
-#pragma unroll
-            for (int r = 0; r < 32; r++) x[r] = reduce32(x[r], mu32, c.Q);
-            uint32_t *acc = A.accs + gid * 2048;
-            store_btile(acc + 1024, x, lane);
-            uint4 *a4 = reinterpret_cast<uint4 *>(acc);
-#pragma unroll
-            for (int qq = 0; qq < 8; qq++) __stcg(a4 + qq * 32 + lane, make_uint4(0, 0, 0, 0));
-            __syncwarp();
-        }
+        for (int k = warp; k < m; k += NP * NW)
+            pipe_init_item(A, c, fwd_tw, pw < GW ? s.dbuf[pw] : s.tslot[0][pw - GW], res + k * S, first + (size_t)k,
+                           lane, mu32);
         if (threadIdx.x == 0) cursor = 0;
         for (int k = threadIdx.x; k < m; k += blockDim.x) done[k] = -1;
         if (pw == 0 && lane == 0) {
@@ -371,32 +411,9 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
         __syncthreads();
 
         // ---- epilogue: NTT accumulators out, or extraction for the key switch
-        for (int t = warp; t < 2 * m; t += NP * NW) {
-            const int k = t >> 1, P = t & 1;
-            const size_t gid = first + (size_t)k;
-            const uint32_t *acc = A.accs + gid * 2048 + P * 1024;
-            uint32_t x[32];
-            if (A.extract) {
-                if (P == 0) load_btile_reversed(x, acc, lane);
-                else load_btile(x, acc, lane);
-                ntt_inv_1024_noscale(x, c, inv_tw, pw < GW ? s.dbuf[pw] : s.tslot[0][pw - GW], lane);
-                uint32_t *ext = A.extract + gid * kExtractStride;
-                if (P == 0) {
-#pragma unroll
-                    for (int r = 0; r < 32; r++) ext[lane + 32 * r] = x[r];
-                } else if (lane == 0) {
-                    ext[1024] = x[0];
-                }
-            } else {
-                load_btile(x, acc, lane);
-                uint64_t *out = A.acc_out + gid * 2048 + P * 1024 + 32 * lane;
-#pragma unroll
-                for (int r = 0; r < 32; r++) {
-                    const uint32_t v = shoup32(x[r], A.nmul, A.nmuls, c.Q);   // times N: the key factor's N^-1 out
-                    out[r] = min(v, v - c.Q);
-                }
-            }
-        }
+        for (int t = warp; t < 2 * m; t += NP * NW)
+            pipe_out_poly(A, c, inv_tw, pw < GW ? s.dbuf[pw] : s.tslot[0][pw - GW], first + (size_t)(t >> 1), t & 1,
+                          lane);
         __syncthreads();
     }
 }
