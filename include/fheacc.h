@@ -128,7 +128,13 @@ typedef struct fheacc_ctx fheacc_ctx;
 
 /* Create a context on CUDA device `device`: derives the parameter set and
  * builds the twiddle tables on the device. Replaces OCL_config_wr_rd
- * (myfpga.cpp:82-326) and BAR1_ROU_table_{1k,2k}_wr (myfpga.cpp:399-594). */
+ * (myfpga.cpp:82-326) and BAR1_ROU_table_{1k,2k}_wr (myfpga.cpp:399-594).
+ * A context is used by one host thread at a time, and its asynchronous calls
+ * on different streams must not overlap: they share the context's scratch
+ * (accumulators, staging, claim and window counters), as the reference's
+ * FPGA slot is used by one caller at a time. For concurrent work use one
+ * context per stream (keys are uploaded to each), or a CUDA graph
+ * (fheacc_graph_*), which owns its scratch. */
 int fheacc_create(const fheacc_params *p, int device, fheacc_ctx **out);
 int fheacc_destroy(fheacc_ctx *ctx);
 /* Last error message of ctx (or of the last failed create when ctx is NULL). */
