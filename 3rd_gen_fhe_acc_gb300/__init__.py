@@ -32,6 +32,7 @@ OPT_BR_CTAS_PER_SM = 2
 OPT_BR_GROUP = 3
 OPT_BR_WINDOW = 4
 OPT_BR_PIPES = 5
+OPT_BR_POOL = 6
 GRAPH_CONCURRENT = 1
 KIND_LWE_SK, KIND_RLWE_SK, KIND_BOOTSTRAP_KEY, KIND_LWE_KS_KEY, KIND_SUBS_KEY, KIND_LWE_CT, KIND_RLWE_CT, \
     KIND_RGSW_CT = range(1, 9)

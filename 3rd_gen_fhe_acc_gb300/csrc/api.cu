@@ -748,6 +748,9 @@ int fheacc_set_option(fheacc_ctx *ctx, int option, int value)
         if (value < -1 || value > 1024) return c.fail(FHEACC_EINVAL, "step window out of range");
         c.tune.br_window = value;
         return FHEACC_OK;
+    case FHEACC_OPT_BR_POOL:
+        c.tune.br_pool = value < 0 ? -1 : value ? 1 : 0;
+        return FHEACC_OK;
 
     default:
         return c.fail(FHEACC_EINVAL, "unknown option");

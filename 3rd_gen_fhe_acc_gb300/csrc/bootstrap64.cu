@@ -229,11 +229,181 @@ struct Br64Args {
     unsigned long long *claim_next;   // next unclaimed ciphertext (zeroed before the launch)
     unsigned *status;          // set to kStatusWaitLimit if a worker gave up waiting
     int digit_tables;          // digit NTTs start from tables (DigitTables64) after the residues
+    size_t claim_limit;        // ciphertexts [0, claim_limit) are claimed in groups
+    // remainder pool: ciphertexts [pool_first, pool_first + pool_count) that all
+    // CTAs share item by item (0: none); their state after the claim words
+    int pool_count;
+    size_t pool_first;
+    unsigned long long *pool_cursor;   // next (step, pool ciphertext) item, step-major (zeroed)
+    int *pool_done;            // [pool_count] last finished step (-1: none yet)
+    int *pool_last;            // [pool_count] last step with a non-zero residue (-1: none)
+    uint8_t *pool_res;         // [pool_count][n * digitR] residues
 };
+
+// LWE_evaluate (LWE.cpp:203-222) of ciphertext gid and the residues of its
+// refresh steps, the base-Br digits of (q - a_i) mod q (RLWE.cpp:740-760), into
+// res[n * digitR]; the thread that takes i = n writes the b value and the gate's
+// two test-vector bounds. Threads t0, t0 + nt, ... take part.
+__device__ __forceinline__ void br64_residues(const Br64Args &A, size_t gid, uint8_t *res, uint32_t *bval,
+                                              uint32_t *b1, uint32_t *b2, int t0, int nt)
+{
+    const int n = A.n;
+    const uint32_t q = A.q, qmask = q - 1;
+    const int g = A.gates[gid];
+    const bool x2 = (g == 4 || g == 5);
+    const uint64_t *c1 = A.c1 + gid * (size_t)(n + 1), *c2 = A.c2 + gid * (size_t)(n + 1);
+    for (int i = t0; i <= n; i += nt) {
+        const uint64_t v = x2 ? 2 * (c1[i] - c2[i]) : c1[i] + c2[i];
+        if (i < n) {
+            uint32_t nega = (q - (uint32_t)(v & qmask)) & qmask;
+            for (uint32_t j = 0; j < A.digitR; j++) {
+                res[i * (int)A.digitR + (int)j] = (uint8_t)(nega % A.Br);
+                nega /= A.Br;
+            }
+        } else {
+            const uint64_t gc = A.gate_constant[(unsigned)g < 6u ? g : 6];
+            *bval = (uint32_t)(v & qmask);
+            *b1 = (uint32_t)(gc & qmask);
+            *b2 = (*b1 + q / 2) & qmask;
+        }
+    }
+}
+
+// acc_initialization (RLWE.cpp:706-724) of ciphertext gid into its accumulator:
+// a = 0, b = the test vector, forward NTT. buf: a shared poly (layout pi<P>)
+// that the worker's second 128-thread group transforms; bar: the worker's
+// barrier (its groups on bar + 1 and bar + 2).
+template <bool P>
+__device__ __forceinline__ void br64_acc_init(const Br64Args &A, const Ntt64Consts &c, const ulonglong2 *tw,
+                                              size_t gid, uint32_t val, uint32_t b1, uint32_t b2, uint64_t *buf,
+                                              int tid, int bar)
+{
+    const uint32_t q = A.q, qmask = q - 1;
+    const uint64_t Q8 = c.Q / 8 + 1, negQ8 = c.Q - Q8;
+    for (int e = tid; e < 2048; e += kT64) {
+        uint64_t v = 0;
+        if (e % A.embed == 0 && (uint32_t)e / A.embed < q / 2) {
+            const uint32_t tmp = (val - (uint32_t)e / A.embed) & qmask;
+            if (b1 < b2) v = (tmp >= b1 && tmp < b2) ? negQ8 : Q8;
+            else v = (tmp >= b2 && tmp < b1) ? Q8 : negQ8;
+        }
+        buf[pi<P>(e)] = v;
+    }
+    group_sync(bar, kT64);
+    if (tid >= 128) ntt64_fwd_2048<128, P>(buf, tw, c, tid - 128, bar + 2);
+    group_sync(bar, kT64);
+    uint64_t *acc = A.accs + gid * 4096;
+    for (int e = tid; e < 2048; e += kT64) {
+        acc[e] = 0;
+        const uint64_t v = barrett64_2q(buf[pi<P>(e)], c.mu64, c.Q);
+        acc[2048 + e] = v >= c.Q ? v - c.Q : v;
+    }
+    group_sync(bar, kT64);
+}
+
+// Output of ciphertext gid from its accumulator: the extracted RLWE
+// (NTT_a_transpose, RLWE.cpp:218-226, then the inverse NTT of both polys) or
+// the canonical NTT accumulator. a0, a1: shared polys (layout pi<P>).
+template <bool P>
+__device__ __noinline__ void br64_output(const Br64Args &A, const Ntt64Consts &c, const ulonglong2 *itw,
+                                            size_t gid, uint64_t *a0, uint64_t *a1, int tid, int bar)
+{
+    const uint64_t *acc = A.accs + gid * 4096;
+    if (A.extract) {
+        for (int e = tid; e < 2048; e += kT64) {
+            a0[pi<P>(e)] = __ldcg(acc + 2047 - e);
+            a1[pi<P>(e)] = __ldcg(acc + 2048 + e);
+        }
+        group_sync(bar, kT64);
+        ntt64_inv_2048<128, P>(tid < 128 ? a0 : a1, itw, c, tid & 127, bar + 1 + (tid >> 7));
+        group_sync(bar, kT64);
+        uint64_t *ext = A.extract + gid * kExtract64;
+        for (int e = tid; e < 2048; e += kT64) ext[e] = a0[pi<P>(e)];
+        if (tid == 0) ext[2048] = a1[pi<P>(0)];
+    } else {
+        for (int e = tid; e < 4096; e += kT64) {
+            const uint64_t v = __ldcg(acc + e);
+            A.acc_out[gid * 4096 + e] = v >= c.Q ? v - c.Q : v;
+        }
+    }
+    group_sync(bar, kT64);
+}
+
+// Remainder pool set-up, one 256-thread CTA per pool ciphertext, before the
+// blind rotation on the same stream: residues, last non-zero step, the
+// initialised accumulator, and the output of a ciphertext without steps.
+__global__ void __launch_bounds__(kT64) br64_pool_init_kernel(const __grid_constant__ Br64Args A,
+                                                             const ulonglong2 *__restrict__ tw,
+                                                             const ulonglong2 *__restrict__ itw,
+                                                             const __grid_constant__ Ntt64Consts c)
+{
+    __shared__ uint64_t buf[2][2048];
+    __shared__ uint32_t bv[3];
+    __shared__ int last;
+    const int p = blockIdx.x, tid = threadIdx.x;
+    const int S = A.n * (int)A.digitR;
+    const size_t gid = A.pool_first + (size_t)p;
+    uint8_t *res = A.pool_res + (size_t)p * S;
+    br64_residues(A, gid, res, &bv[0], &bv[1], &bv[2], tid, kT64);
+    __syncthreads();
+    if (tid == 0) {
+        int l = -1;
+        if (A.flags & FHEACC_FLAG_FPGA_COMPAT) l = S - 1;
+        else
+            for (int x = S - 1; x >= 0; x--)
+                if (res[x]) {
+                    l = x;
+                    break;
+                }
+        last = l;
+        A.pool_last[p] = l;
+        A.pool_done[p] = -1;
+    }
+    br64_acc_init<false>(A, c, tw, gid, bv[0], bv[1], bv[2], buf[1], tid, 1);
+    __syncthreads();
+    if (last < 0) br64_output<false>(A, c, itw, gid, buf[0], buf[1], tid, 1);
+}
 
 // Polls of a worker waiting for another worker's step of the same ciphertext
 // (about 60 ns each) before it gives up and flags the launch.
 constexpr unsigned kWorkerWaitLimit = 1u << 26;
+
+// Takes the next item of the remainder pool whose step is at most `reach`,
+// skipping items of zero residue (unless compat); false when there is none.
+// prev: the item's ciphertext's last earlier step with a non-zero residue.
+// seen: the CTA's last view of the pool cursor, which only grows, so the
+// cursor is read only when the view leaves an item to take.
+__device__ __forceinline__ bool pool_take(const Br64Args &A, int S, bool compat, unsigned long long reach,
+                                          unsigned long long *seen, int &st, int &k, int &prev)
+{
+    const unsigned long long R = (unsigned long long)A.pool_count, total = R * (unsigned long long)S;
+    unsigned long long v = *(volatile unsigned long long *)seen;
+    if (v >= total || v / R > reach) return false;
+    v = *(volatile unsigned long long *)A.pool_cursor;
+    for (;;) {
+        if (v >= total || v / R > reach) {
+            atomicMax(seen, v);
+            return false;
+        }
+        const unsigned long long old = atomicCAS(A.pool_cursor, v, v + 1);
+        if (old != v) {
+            v = old;
+            continue;
+        }
+        const int s_ = (int)(v / R), k_ = (int)(v - (unsigned long long)s_ * R);
+        const uint8_t *pr = A.pool_res + (size_t)k_ * S;
+        if (compat || pr[s_]) {
+            atomicMax(seen, v + 1);
+            st = s_;
+            k = k_;
+            prev = st - 1;
+            if (!compat)
+                while (prev >= 0 && !pr[prev]) prev--;
+            return true;
+        }
+        v++;   // an item of zero residue, taken and skipped
+    }
+}
 
 // W workers of 256 threads per CTA (W = 1: 3 CTAs per SM, 80 registers; the
 // extra resident warps hide the latency of the key stream better than the
@@ -244,7 +414,9 @@ constexpr unsigned kWorkerWaitLimit = 1u << 26;
 // earlier step with a non-zero residue) has finished, so every ciphertext's
 // steps keep the reference's order and the workers finish together. Worker w
 // synchronises on named barrier 1 + 3w (its two 128-thread groups on 2 + 3w and
-// 3 + 3w). An XOR swizzle of the shared-memory passes removed their bank
+// 3 + 3w). When the batch does not divide evenly among the CTAs, the remainder
+// ciphertexts form a pool that all CTAs share item by item (pool_take), their
+// steps ordered by done words in global memory. An XOR swizzle of the shared-memory passes removed their bank
 // conflicts but cost more in index arithmetic than it saved.
 template <int W, int MINB>
 __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_constant__ Br64Args A,
@@ -256,20 +428,21 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
     uint8_t *res = smem_raw + W * sizeof(Step64SmemT<true>);   // [group][n * digitR]
     __shared__ uint32_t bvals[kMaxGroup64 * W], b1s[kMaxGroup64 * W], b2s[kMaxGroup64 * W];
     __shared__ int done[kMaxGroup64 * W];
-    __shared__ int plan[W][2];
+    __shared__ int plan[W][3];
     __shared__ int cursor, wcur, won;
+    __shared__ unsigned long long pool_seen;
     __shared__ unsigned long long claim_first;
     __shared__ int claim_m;
     const int wk = threadIdx.x / kT64, tid = threadIdx.x - wk * kT64, bar = 1 + 3 * wk;
     Step64SmemT<true> &s = reinterpret_cast<Step64SmemT<true> *>(smem_raw)[wk];
-    const int n = A.n, S = n * (int)A.digitR;
-    const uint32_t q = A.q, qmask = q - 1;
+    const int S = A.n * (int)A.digitR;
     const size_t rgsw_pairs = (size_t)A.DG * 4 * 2048;
     const bool compat = (A.flags & FHEACC_FLAG_FPGA_COMPAT) != 0;
     const unsigned target = gridDim.x;   // the window is used with one round of claims
     if (threadIdx.x == 0) {
         wcur = 0;
         won = 1;
+        pool_seen = 0;
     }
     // digit tables after the residue table of the largest group
     const DigitTables64 dt = build_digit_tables64(res + ((size_t)A.group * S + 15) / 16 * 16,
@@ -278,71 +451,41 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
         if (threadIdx.x == 0) {
             const unsigned long long f = atomicAdd(A.claim_next, (unsigned long long)A.group);
             claim_first = f;
-            claim_m = f < A.count ? (int)min((unsigned long long)A.group, (unsigned long long)A.count - f) : 0;
+            claim_m = f < A.claim_limit ? (int)min((unsigned long long)A.group, (unsigned long long)A.claim_limit - f) : 0;
         }
         __syncthreads();
         const size_t first = claim_first;
         const int m = claim_m;
         if (m == 0) break;
         // LWE_evaluate and residues
-        for (int k = 0; k < m; k++) {
-            const size_t gid = first + (size_t)k;
-            const int g = A.gates[gid];
-            const bool x2 = (g == 4 || g == 5);
-            const uint64_t *c1 = A.c1 + gid * (size_t)(n + 1), *c2 = A.c2 + gid * (size_t)(n + 1);
-            for (int i = threadIdx.x; i <= n; i += blockDim.x) {
-                const uint64_t v = x2 ? 2 * (c1[i] - c2[i]) : c1[i] + c2[i];
-                if (i < n) {
-                    uint32_t nega = (q - (uint32_t)(v & qmask)) & qmask;
-                    for (uint32_t j = 0; j < A.digitR; j++) {
-                        res[k * S + i * (int)A.digitR + (int)j] = (uint8_t)(nega % A.Br);
-                        nega /= A.Br;
-                    }
-                } else {
-                    const uint64_t gc = A.gate_constant[(unsigned)g < 6u ? g : 6];
-                    bvals[k] = (uint32_t)(v & qmask);
-                    b1s[k] = (uint32_t)(gc & qmask);
-                    b2s[k] = (b1s[k] + q / 2) & qmask;
-                }
-            }
-        }
+        for (int k = 0; k < m; k++)
+            br64_residues(A, first + (size_t)k, res + k * S, bvals + k, b1s + k, b2s + k, threadIdx.x, blockDim.x);
         for (int k = threadIdx.x; k < m; k += blockDim.x) done[k] = -1;
         if (threadIdx.x == 0) cursor = 0;
         __syncthreads();
         // acc_initialization, one ciphertext per worker: a = 0, b = test vector,
         // forward NTT (the worker's group 1 transforms b)
-        for (int k = wk; k < m; k += W) {
-            const size_t gid = first + (size_t)k;
-            const uint64_t Q8 = c.Q / 8 + 1, negQ8 = c.Q - Q8;
-            const uint32_t b1 = b1s[k], b2 = b2s[k], val = bvals[k];
-            for (int e = tid; e < 2048; e += kT64) {
-                uint64_t v = 0;
-                if (e % A.embed == 0 && (uint32_t)e / A.embed < q / 2) {
-                    const uint32_t tmp = (val - (uint32_t)e / A.embed) & qmask;
-                    if (b1 < b2) v = (tmp >= b1 && tmp < b2) ? negQ8 : Q8;
-                    else v = (tmp >= b2 && tmp < b1) ? Q8 : negQ8;
-                }
-                s.buf[1][px(e)] = v;
-            }
-            group_sync(bar, kT64);
-            if (tid >= 128) ntt64_fwd_2048<128, true>(s.buf[1], tw, c, tid - 128, bar + 2);
-            group_sync(bar, kT64);
-            uint64_t *acc = A.accs + gid * 4096;
-            for (int e = tid; e < 2048; e += kT64) {
-                acc[e] = 0;
-                uint64_t v = barrett64_2q(s.buf[1][px(e)], c.mu64, c.Q);
-                acc[2048 + e] = v >= c.Q ? v - c.Q : v;
-            }
-            group_sync(bar, kT64);
-        }
+        for (int k = wk; k < m; k += W)
+            br64_acc_init<true>(A, c, tw, first + (size_t)k, bvals[k], b1s[k], b2s[k], s.buf[1], tid, bar);
         __syncthreads();
         // blind rotation: the workers take the group's items from the cursor
         for (;;) {
             if (tid == 0) {
-                int st = -1, k = -1, prev = -1;
-                for (;;) {
+                int st = -1, k = -1, prev = -1, pool = 0;
+                // an item of the remainder pool of a step this CTA has reached
+                // (of any step once the CTA's own items are all issued)
+                if (A.pool_count) {
+                    const int own = *(volatile int *)&cursor;
+                    pool = pool_take(A, S, compat, own < S * m ? (unsigned long long)(own / m) : ~0ull, &pool_seen,
+                                     st, k, prev);
+                }
+                for (; !pool;) {
                     const int idx = atomicAdd(&cursor, 1);
-                    if (idx >= S * m) break;
+                    if (idx >= S * m) {
+                        // own items all issued: the rest of the pool
+                        if (A.pool_count) pool = pool_take(A, S, compat, ~0ull, &pool_seen, st, k, prev);
+                        break;
+                    }
                     const int s_ = idx / m, k_ = idx - s_ * m;
                     if (compat || res[k_ * S + s_]) {
                         st = s_;
@@ -353,7 +496,7 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
                         break;
                     }
                 }
-                if (st >= 0 && A.win.count) {
+                if (!pool && st >= 0 && A.win.count) {
                     // step window: count this CTA into the buckets it has left, then
                     // wait for the slowest CTA
                     const int b = st / A.win.steps;
@@ -365,8 +508,9 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
                     if (!on) won = 0;
                 }
                 if (st >= 0) {
-                    // the previous item of the ciphertext must have finished
-                    const volatile int *dk = done + k;
+                    // the previous item of the ciphertext must have finished (a
+                    // pool ciphertext's: on any CTA)
+                    const volatile int *dk = pool ? A.pool_done + k : done + k;
                     unsigned polls = 0;
                     while (*dk != prev) {
                         if (++polls > kWorkerWaitLimit) {
@@ -376,52 +520,47 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
                         }
                         __nanosleep(32);
                     }
-                    __threadfence_block();
+                    if (pool) __threadfence();
+                    else __threadfence_block();
                 }
                 plan[wk][0] = st;
                 plan[wk][1] = k;
+                plan[wk][2] = pool;
             }
             group_sync(bar, kT64);
-            const int st = plan[wk][0], k = plan[wk][1];
-            if (st < 0) break;
-            const uint32_t r = res[k * S + st];
-            uint64_t *acc = A.accs + (first + (size_t)k) * 4096;
-            for (int e = tid; e < 4096; e += kT64) s.acc[e >> 11][px(e & 2047)] = __ldcg(acc + e);
-            group_sync(bar, kT64);
-            step64(s, A.btkey + ((size_t)st * A.Br + r) * rgsw_pairs, A.DG, A.bg_bits, tw, itw, c,
-                   A.derive_last ? acc : nullptr, tid, bar, A.digit_tables ? &dt : nullptr);
+            {
+                const int st = plan[wk][0], k = plan[wk][1], pool = plan[wk][2];
+                if (st < 0) break;
+                const uint32_t r = pool ? A.pool_res[(size_t)k * S + st] : res[k * S + st];
+                const uint64_t *acc = A.accs + ((pool ? A.pool_first : first) + (size_t)k) * 4096;
+                for (int e = tid; e < 4096; e += kT64) s.acc[e >> 11][px(e & 2047)] = __ldcg(acc + e);
+                group_sync(bar, kT64);
+                step64(s, A.btkey + ((size_t)st * A.Br + r) * rgsw_pairs, A.DG, A.bg_bits, tw, itw, c,
+                       A.derive_last ? acc : nullptr, tid, bar, A.digit_tables ? &dt : nullptr);
+            }
+            // the item again from the plan (not held in registers across the step;
+            // the plan changes only after the barrier below)
+            const volatile int *pv = plan[wk];
+            const int st = pv[0], k = pv[1], pool = pv[2];
+            const size_t gid = (pool ? A.pool_first : first) + (size_t)k;
+            uint64_t *acc = A.accs + gid * 4096;
             for (int e = tid; e < 4096; e += kT64) __stcg(acc + e, s.acc[e >> 11][px(e & 2047)]);
+            if (pool) __threadfence();
             group_sync(bar, kT64);
             if (tid == 0) {
-                __threadfence_block();
-                done[k] = st;
+                if (pool) {
+                    atomicExch(A.pool_done + k, st);
+                } else {
+                    __threadfence_block();
+                    done[k] = st;
+                }
             }
+            // a pool ciphertext's output right after its last step
+            if (pool && st == A.pool_last[k]) br64_output<true>(A, c, itw, gid, s.acc[0], s.acc[1], tid, bar);
         }
         __syncthreads();
         // output, one ciphertext per worker
-        for (int k = wk; k < m; k += W) {
-            const size_t gid = first + (size_t)k;
-            const uint64_t *acc = A.accs + gid * 4096;
-            if (A.extract) {
-                // NTT_a_transpose on poly a, then inverse NTT of both polys
-                for (int e = tid; e < 2048; e += kT64) {
-                    s.acc[0][px(e)] = __ldcg(acc + 2047 - e);
-                    s.acc[1][px(e)] = __ldcg(acc + 2048 + e);
-                }
-                group_sync(bar, kT64);
-                ntt64_inv_2048<128, true>(s.acc[tid >> 7], itw, c, tid & 127, bar + 1 + (tid >> 7));
-                group_sync(bar, kT64);
-                uint64_t *ext = A.extract + gid * kExtract64;
-                for (int e = tid; e < 2048; e += kT64) ext[e] = s.acc[0][px(e)];
-                if (tid == 0) ext[2048] = s.acc[1][0];
-            } else {
-                for (int e = tid; e < 4096; e += kT64) {
-                    const uint64_t v = __ldcg(acc + e);
-                    A.acc_out[gid * 4096 + e] = v >= c.Q ? v - c.Q : v;
-                }
-            }
-            group_sync(bar, kT64);
-        }
+        for (int k = wk; k < m; k += W) br64_output<true>(A, c, itw, first + (size_t)k, s.acc[0], s.acc[1], tid, bar);
         __syncthreads();
     }
     // a CTA counts into every bucket it has not counted into yet
@@ -662,11 +801,33 @@ static int launch_br64_shape(Context &c, dev::Br64Args A, int max_ctas, cudaStre
     // equal claims: the fewest rounds of at most `cap` ciphertexts per CTA
     const size_t rounds = (A.count + blocks * cap - 1) / (blocks * cap);
     A.group = (int)((A.count + blocks * rounds - 1) / (blocks * rounds));
-    smem = smem_of(A.group);
-    // claim counter after the accumulators
+    A.claim_limit = A.count;
+    // claim counters after the accumulators, then the remainder pool's state
     A.claim_next = reinterpret_cast<unsigned long long *>(A.accs + A.count * 4096);
+    A.pool_cursor = A.claim_next + 1;
+    A.pool_done = reinterpret_cast<int *>(A.claim_next + kClaimWords / 2);
+    A.pool_last = A.pool_done + kPool64;
+    A.pool_res = reinterpret_cast<uint8_t *>(A.pool_last + kPool64);
+    // One round of claims whose CTAs would not all take the same number of
+    // ciphertexts: each takes count / blocks of its own, and the remainder is
+    // shared by all CTAs item by item (a whole ciphertext more on some CTAs
+    // would hold the launch for its steps: 2048 gates on 152 CTAs, 14 against
+    // a mean of 13.5)
+    if (rounds == 1 && c.tune.br_pool != 0 && A.count > blocks && A.count % blocks != 0 &&
+        A.count % blocks <= kPool64) {
+        A.group = (int)(A.count / blocks);
+        A.claim_limit = (size_t)A.group * blocks;
+        A.pool_first = A.claim_limit;
+        A.pool_count = (int)(A.count - A.claim_limit);
+    }
+    smem = smem_of(A.group);
     e = cudaMemsetAsync(A.claim_next, 0, kClaimWords * sizeof(uint32_t), st);
     if (e != cudaSuccess) return c.cuda_fail(e, "br64 claim reset");
+    if (A.pool_count) {
+        dev::br64_pool_init_kernel<<<(unsigned)A.pool_count, dev::kT64, 0, st>>>(A, c.d_tw64, c.d_itw64, c.nc64);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return c.cuda_fail(e, "br64 pool launch");
+    }
     // the window's per-bucket targets assume one round of claims
     int rc = rounds == 1 ? prepare_window(c, (int)steps, st, A.win) : FHEACC_OK;
     if (rc) return rc;

@@ -41,11 +41,15 @@ struct Tuning {
     int br_group = 0;         // cap on ciphertexts per CTA and chunk (0: kernel maximum)
     int br_window = -1;       // 64-bit path: steps per bucket of the step window (0: off; -1: default)
     int br_pipes = 0;         // 32-bit path: pipelines per CTA, 1..3 (0: by gates per SM)
+    int br_pool = -1;         // 64-bit path: remainder gates shared by all CTAs (0: off; -1: on)
 };
 
 constexpr size_t kPipeSmemBudget = 220 * 1024;   // dynamic shared memory of one blind-rotation CTA
 
 constexpr size_t kClaimWords = 64;   // u32 words of claim counters after the blind-rotation accumulators
+// 64-bit blind rotation: most remainder gates of a batch that the CTAs share
+// item by item (their per-gate state follows the claim words)
+constexpr size_t kPool64 = 256;
 // Device status bits (Context::d_status): a kernel that gave up a bounded wait
 // on another worker of its CTA sets kStatusWaitLimit; its results are not valid.
 constexpr unsigned kStatusWaitLimit = FHEACC_STATUS_WAIT_LIMIT;
@@ -212,7 +216,8 @@ constexpr size_t kExtract64 = 2048 + 8;        // u64 words per extracted RLWE (
 // accumulators and extracted RLWEs (bytes of each).
 inline size_t bootstrap_accs_bytes(const Context &c, size_t count)
 {
-    return c.wide ? count * 4096 * sizeof(uint64_t) + kClaimWords * sizeof(uint32_t)
+    return c.wide ? count * 4096 * sizeof(uint64_t) + kClaimWords * sizeof(uint32_t) +
+                        kPool64 * (2 * sizeof(int) + (size_t)c.p.n * c.p.digitR)
                   : (count * 2048 + kClaimWords) * sizeof(uint32_t);
 }
 inline size_t bootstrap_extract_bytes(const Context &c, size_t count)

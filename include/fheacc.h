@@ -232,12 +232,19 @@ int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t cou
  *                             share its group of ciphertexts item by item, so
  *                             they finish together; with one per CTA, up to 3
  *                             CTAs share an SM and finish at different times.
+ *  FHEACC_OPT_BR_POOL       : 64-bit words: when the batch does not divide
+ *                             evenly among the CTAs, each CTA takes
+ *                             count / CTAs ciphertexts of its own and all
+ *                             CTAs share the remainder step by step; 0 = off
+ *                             (some CTAs take one ciphertext more), -1
+ *                             (default) = on
  * Results never depend on the options. */
 #define FHEACC_OPT_BR_REGS_FOR_3  1
 #define FHEACC_OPT_BR_CTAS_PER_SM 2
 #define FHEACC_OPT_BR_GROUP       3
 #define FHEACC_OPT_BR_WINDOW      4
 #define FHEACC_OPT_BR_PIPES       5
+#define FHEACC_OPT_BR_POOL        6
 int fheacc_set_option(fheacc_ctx *ctx, int option, int value);
 
 /* Per-kernel device times (ms) of the most recent call made with

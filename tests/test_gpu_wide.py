@@ -157,3 +157,64 @@ def test_wide_rlwe_mult_rgsw_batch(F, ctx1, keys1, cuda_ok):
     ctx1.rlwe_mult_rgsw(da.data_ptr(), dr.data_ptr(), out.data_ptr(), 20)
     torch.cuda.synchronize()
     assert np.array_equal(host(out), np.stack([o.rlwe_mult_rgsw(acc[i], rgsw[i]) for i in range(20)]))
+
+
+@pytest.mark.parametrize("pipes,window,compat", [(2, -1, False), (3, 0, False), (2, -1, True)])
+def test_wide_remainder_pool(F, ctx1, keys1, pipes, window, compat):
+    """13 gates on 2-worker CTAs (7 CTAs of 1 gate, a remainder pool of 6
+    that all CTAs share step by step) or 3-worker CTAs (5 of 2, a pool of 3),
+    with the step window on and off and in the no-skip issue order: the oracle's
+    words, the same as with the pool off, and every gate decrypts."""
+    x, y, g, c1, c2 = random_gate_batch(keys1, 13, seed=53)
+    flags = F.FLAG_FPGA_COMPAT if compat else 0
+    ctx1.set_option(F.OPT_BR_PIPES, pipes)
+    ctx1.set_option(F.OPT_BR_WINDOW, window)
+    try:
+        out = ctx1.eval_bootstrap_batch(c1, c2, g, flags=flags)
+        assert ctx1.device_status() == 0
+        ctx1.set_option(F.OPT_BR_POOL, 0)
+        off = ctx1.eval_bootstrap_batch(c1, c2, g, flags=flags)
+    finally:
+        ctx1.set_option(F.OPT_BR_POOL, -1)
+        ctx1.set_option(F.OPT_BR_PIPES, 0)
+        ctx1.set_option(F.OPT_BR_WINDOW, -1)
+    want, failed = keys1.oracle.eval_bootstrap_batch(c1, c2, g, keys1.btkey, keys1.kskey, fpga_compat=compat)
+    assert failed == 0 or compat
+    assert np.array_equal(out, want)
+    assert np.array_equal(off, want)
+    if not compat:
+        truth = np.array([F.gate_truth(int(a), b, c) for a, b, c in zip(g, x, y)], dtype=np.uint8)
+        assert np.array_equal(keys1.decrypt(out), truth)
+
+
+def test_wide_remainder_pool_full_grid(F, ctx1, keys1, cuda_ok):
+    """2 x SMs + 37 gates with the default launch: every CTA takes 2 gates of
+    its own and the last 37 are shared; all decrypt, a sample on both sides of
+    the split equals the oracle, and the NTT-domain accumulators of the
+    blind-rotation entry point equal those with the pool off."""
+    torch = cuda_ok
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    count = 2 * sms + 37
+    x, y, g, c1, c2 = random_gate_batch(keys1, count, seed=57)
+    out = ctx1.eval_bootstrap_batch(c1, c2, g)
+    assert ctx1.device_status() == 0
+    truth = np.array([F.gate_truth(int(a), b, c) for a, b, c in zip(g, x, y)], dtype=np.uint8)
+    assert np.array_equal(keys1.decrypt(out), truth)
+    idx = np.array([0, 2 * sms - 1, 2 * sms, 2 * sms + 20, count - 1])
+    want, failed = keys1.oracle.eval_bootstrap_batch(c1[idx], c2[idx], g[idx], keys1.btkey, keys1.kskey)
+    assert failed == 0
+    assert np.array_equal(out[idx], want)
+    d1, d2, dg = dev(torch, c1), dev(torch, c2), torch.from_numpy(g).cuda()
+    accs = []
+    for pool in (-1, 0):
+        ctx1.set_option(F.OPT_BR_POOL, pool)
+        try:
+            acc = torch.zeros((count, 4096), dtype=torch.int64, device="cuda")
+            ctx1.blind_rotate_async(d1.data_ptr(), d2.data_ptr(), dg.data_ptr(), count, acc.data_ptr())
+            ctx1.sync()
+            accs.append(host(acc))
+        finally:
+            ctx1.set_option(F.OPT_BR_POOL, -1)
+    assert np.array_equal(accs[0], accs[1])
+    want_acc, steps = keys1.oracle.blind_rotate(c1[count - 1], c2[count - 1], int(g[count - 1]), keys1.btkey)
+    assert np.array_equal(accs[0][count - 1], want_acc)
