@@ -153,6 +153,7 @@ def lib():
             "fheacc_lwe_modswitch_async": (ctypes.c_int, [vp, vp, sz, vp, vp]),
             "fheacc_sync": (ctypes.c_int, [vp, ctypes.c_uint32]),
             "fheacc_device_status": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_uint32)]),
+            "fheacc_kernel_launches": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_uint64)]),
             "fheacc_kernel_times": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_float)]),
             "fheacc_set_option": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
             "fheacc_measure_imad_rate": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
@@ -496,6 +497,13 @@ class Context:
 
     def set_option(self, option, value):
         self.check(lib().fheacc_set_option(self._h, option, value))
+
+    def kernel_launches(self):
+        """Kernels this context has launched so far (one per kernel captured
+        into a graph, at capture)."""
+        n = ctypes.c_uint64()
+        self.check(lib().fheacc_kernel_launches(self._h, ctypes.byref(n)))
+        return n.value
 
     def kernel_times(self):
         """(blind rotation ms, key switch ms) of the last FLAG_PROFILE call."""

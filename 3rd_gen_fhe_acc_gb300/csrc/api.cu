@@ -880,6 +880,13 @@ int fheacc_device_status(fheacc_ctx *ctx, uint32_t *bits)
     return take_device_status(c, bits);
 }
 
+int fheacc_kernel_launches(const fheacc_ctx *ctx, uint64_t *count)
+{
+    if (!ctx || !count) return FHEACC_EINVAL;
+    *count = reinterpret_cast<const Context *>(ctx)->launches;
+    return FHEACC_OK;
+}
+
 int fheacc_sync(fheacc_ctx *ctx, uint32_t timeout_ms)
 {
     if (!ctx) return FHEACC_EINVAL;

@@ -461,6 +461,7 @@ static int launch_pipe_dg(Context &c, dev::PipeArgs A, int max_ctas, cudaStream_
     e = cudaMemsetAsync(A.claim_next, 0, kClaimWords * sizeof(uint32_t), st);
     if (e != cudaSuccess) return c.cuda_fail(e, "blind rotation claim reset");
     kern<<<(unsigned)blocks, threads, smem, st>>>(A, c.nc, c.d_fwd_tw, c.d_inv_tw, (uint32_t)((1ULL << 32) / c.p.Q));
+    c.launches++;
     e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "blind rotation launch");
 }

@@ -139,10 +139,12 @@ int launch_ntt32(Context &c, uint64_t *d_polys, size_t count, bool inverse, cuda
         cudaFuncSetAttribute(dev::ntt32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         dev::ntt32_kernel<true><<<(unsigned)blocks, 256, smem, st>>>(d_polys, count, c.nc, c.d_inv_tw,
                                                                      mu32_of(c.p.Q));
+        c.launches++;
     } else {
         cudaFuncSetAttribute(dev::ntt32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         dev::ntt32_kernel<false><<<(unsigned)blocks, 256, smem, st>>>(d_polys, count, c.nc, c.d_fwd_tw,
                                                                       mu32_of(c.p.Q));
+        c.launches++;
     }
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "ntt32 launch");
@@ -157,6 +159,7 @@ static int launch_mult_rgsw_dg(Context &c, const uint64_t *d_acc, const uint64_t
     size_t blocks = std::min<size_t>(count, (size_t)num_sms(c) * 4);
     dev::rlwe_mult_rgsw32_kernel<DG><<<(unsigned)blocks, 256, smem, st>>>(
         d_acc, d_rgsw, d_out, count, stride, c.nc, c.d_fwd_tw, c.d_inv_tw, c.p.BG_bits, c.dp.mu64);
+    c.launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "rlwe_mult_rgsw32 launch");
 }
@@ -179,6 +182,7 @@ int launch_extract_from_ntt32(Context &c, const uint64_t *d_rlwe, size_t count, 
     if (!count) return FHEACC_OK;
     size_t blocks = std::min<size_t>(count, (size_t)num_sms(c) * 16);
     dev::extract32_kernel<<<(unsigned)blocks, 64, 0, st>>>(d_rlwe, count, d_extract, c.nc, c.d_inv_tw);
+    c.launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "extract32 launch");
 }

@@ -212,6 +212,65 @@ __global__ void __launch_bounds__(kT64) rlwe_mult_rgsw64_kernel(const uint64_t *
     }
 }
 
+// RLWE x RGSW of a few products, split over the gadget digits for latency: CTA
+// (product ci, digit h) takes the inverse NTT of the product's accumulator,
+// digit h of both polys and their forward NTTs, and writes the digit's share of
+// the multiply-accumulate to partial[ci][h] (two Shoup products per word, < 4Q);
+// rlwe_split_sum64_kernel adds the digitG shares. A lone product's inverse and
+// digit NTTs then take two rounds instead of 1 + digitG.
+__global__ void __launch_bounds__(kT64) rlwe_mult_rgsw64_split_kernel(const uint64_t *__restrict__ acc_in,
+                                                                     const ulonglong2 *__restrict__ rgsw,
+                                                                     uint64_t *__restrict__ partial, size_t rgsw_stride,
+                                                                     int DG, uint32_t bg_bits,
+                                                                     const ulonglong2 *__restrict__ tw,
+                                                                     const ulonglong2 *__restrict__ itw,
+                                                                     const __grid_constant__ Ntt64Consts c)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Step64SmemT<false> &s = *reinterpret_cast<Step64SmemT<false> *>(smem_raw);
+    const size_t ci = blockIdx.x / (unsigned)DG;
+    const int h = (int)(blockIdx.x - ci * (unsigned)DG);
+    const int tid = threadIdx.x, grp = tid >> 7, gtid = tid & 127;
+    for (int e = tid; e < 4096; e += kT64) s.acc[e >> 11][e & 2047] = acc_in[ci * 4096 + e];
+    __syncthreads();
+    ntt64_inv_2048<128, false>(s.acc[grp], itw, c, gtid, 2 + grp);   // ends with the group's barrier
+    const uint64_t mask = (1ULL << bg_bits) - 1;
+    const uint32_t sh = bg_bits * (uint32_t)h;
+    for (int e = gtid; e < 2048; e += 128) s.buf[grp][e] = (s.acc[grp][e] >> sh) & mask;
+    group_sync(2 + grp, 128);
+    ntt64_fwd_2048<128, false>(s.buf[grp], tw, c, gtid, 2 + grp);
+    __syncthreads();
+    const ulonglong2 *key = rgsw + ci * rgsw_stride;
+    const ulonglong2 *k0 = key + (size_t)(h * 2 + 0) * 2 * 2048;   // row c_text[h][0]: times digit of a
+    const ulonglong2 *k1 = key + (size_t)(h * 2 + 1) * 2 * 2048;   // row c_text[h][1]: times digit of b
+    uint64_t *out = partial + (ci * (unsigned)DG + (unsigned)h) * 4096;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int k = tid + 256 * i;
+        const uint64_t da = s.buf[0][k], db = s.buf[1][k];
+        const ulonglong2 a0 = __ldg(k0 + k), b0 = __ldg(k0 + 2048 + k);
+        const ulonglong2 a1 = __ldg(k1 + k), b1 = __ldg(k1 + 2048 + k);
+        out[k] = shoup64(da, a0.x, a0.y, c.Q) + shoup64(db, a1.x, a1.y, c.Q);
+        out[2048 + k] = shoup64(da, b0.x, b0.y, c.Q) + shoup64(db, b1.x, b1.y, c.Q);
+    }
+}
+
+// acc_out[ci] = sum over h of partial[ci][h] mod Q (canonical); the sum of
+// digitG shares < 4Q stays below 2^64 (checked by the launcher).
+__global__ void rlwe_split_sum64_kernel(const uint64_t *__restrict__ partial, uint64_t *__restrict__ acc_out,
+                                        size_t count, int DG, const __grid_constant__ Ntt64Consts c)
+{
+    const size_t words = count * 4096;
+    for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += (size_t)gridDim.x * blockDim.x) {
+        const size_t ci = w / 4096, e = w - ci * 4096;
+        const uint64_t *p = partial + ci * (unsigned)DG * 4096 + e;
+        uint64_t sum = 0;
+        for (int h = 0; h < DG; h++) sum += p[(size_t)h * 4096];
+        const uint64_t v = barrett64_2q(sum, c.mu64, c.Q);
+        acc_out[w] = v >= c.Q ? v - c.Q : v;
+    }
+}
+
 struct Br64Args {
     const uint64_t *c1, *c2;
     const int32_t *gates;
@@ -697,6 +756,7 @@ int launch_derive_keys64(Context &c, uint64_t *d_keys, size_t count, const ulong
     if (!count) return FHEACC_OK;
     dev::derive_keys64_kernel<<<(unsigned)std::min<size_t>((count * 4 * c.p.N + 255) / 256, 8192), 256, 0, st>>>(
         d_keys, count, (int)c.p.digitG, c.p.N, d_cf, c.p.Q);
+    c.launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "derive keys launch");
 }
@@ -706,6 +766,7 @@ int launch_shoup_pairs64(Context &c, const uint64_t *d_in, ulonglong2 *d_out, si
     if (!n) return FHEACC_OK;
     unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)sms_of(c) * 32);
     dev::shoup_pairs64_kernel<<<blocks, 256, 0, st>>>(d_in, d_out, n, c.p.Q);
+    c.launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "shoup pairs launch");
 }
@@ -714,8 +775,13 @@ int launch_ntt64(Context &c, uint64_t *d_polys, size_t count, bool inverse, cuda
 {
     if (!count) return FHEACC_OK;
     size_t blocks = std::min<size_t>((count + 1) / 2, (size_t)sms_of(c) * 8);
-    if (inverse) dev::ntt64_kernel<true><<<(unsigned)blocks, dev::kT64, 0, st>>>(d_polys, count, c.d_itw64, c.nc64);
-    else dev::ntt64_kernel<false><<<(unsigned)blocks, dev::kT64, 0, st>>>(d_polys, count, c.d_tw64, c.nc64);
+    if (inverse) {
+        dev::ntt64_kernel<true><<<(unsigned)blocks, dev::kT64, 0, st>>>(d_polys, count, c.d_itw64, c.nc64);
+        c.launches++;
+    } else {
+        dev::ntt64_kernel<false><<<(unsigned)blocks, dev::kT64, 0, st>>>(d_polys, count, c.d_tw64, c.nc64);
+        c.launches++;
+    }
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "ntt64 launch");
 }
@@ -731,8 +797,15 @@ int launch_rlwe_mult_rgsw64(Context &c, const uint64_t *d_acc, const uint64_t *d
     // (2 of the 2 digitG digit NTTs of a product saved); a call of a few
     // products keeps the plain RGSWs, whose derivation would cost it more
     // (PSI query: homo_expand 7.87 -> 7.51 ms, its 1-item CMUXes 0.79 -> 0.90 ms)
-    const bool derive = c.dp.last_digit_from_acc && c.d_cf64 && count >= 16;
-    int rc = ensure_scratch(c, c.io, words * (sizeof(ulonglong2) + (derive ? sizeof(uint64_t) : 0)));
+    // a call of at most two CTAs per SM of (product, digit) pairs splits each
+    // product over its digits, for latency (PSI query: the 11 one-RLWE CMUXes of
+    // its blind rotation 0.84 -> 0.48 ms, the 7-level CMUX tree 0.53 -> 0.33 ms)
+    const size_t DG = c.p.digitG;
+    const bool split = count * DG <= (size_t)sms_of(c) * 2 && (uint64_t)DG * 4 < UINT64_MAX / c.p.Q;
+    const bool derive = !split && c.dp.last_digit_from_acc && c.d_cf64 && count >= 16;
+    const size_t partial_words = split ? count * DG * 4096 : 0;
+    int rc = ensure_scratch(c, c.io, words * (sizeof(ulonglong2) + (derive ? sizeof(uint64_t) : 0)) +
+                                         partial_words * sizeof(uint64_t));
     if (rc) return rc;
     ulonglong2 *pairs = (ulonglong2 *)c.io.ptr;
     const uint64_t *src = d_rgsw;
@@ -746,6 +819,21 @@ int launch_rlwe_mult_rgsw64(Context &c, const uint64_t *d_acc, const uint64_t *d
     }
     rc = launch_shoup_pairs64(c, src, pairs, words, st);
     if (rc) return rc;
+    if (split) {
+        uint64_t *partial = reinterpret_cast<uint64_t *>(pairs + words);
+        const size_t smem = sizeof(dev::Step64SmemT<false>);
+        cudaFuncSetAttribute(dev::rlwe_mult_rgsw64_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        dev::rlwe_mult_rgsw64_split_kernel<<<(unsigned)(count * DG), dev::kT64, smem, st>>>(
+            d_acc, pairs, partial, stride, (int)DG, c.p.BG_bits, c.d_tw64, c.d_itw64, c.nc64);
+        c.launches++;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return c.cuda_fail(e, "rlwe_mult_rgsw64 split launch");
+        const unsigned blocks = (unsigned)std::min<size_t>((count * 4096 + 255) / 256, (size_t)sms_of(c) * 4);
+        dev::rlwe_split_sum64_kernel<<<blocks, 256, 0, st>>>(partial, d_out, count, (int)DG, c.nc64);
+        c.launches++;
+        e = cudaGetLastError();
+        return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "rlwe_mult_rgsw64 split sum launch");
+    }
     // no digit tables here: their 20 KB of shared memory cost this kernel more
     // L1 (twiddles, the shared RGSW) than they saved (homo_expand 7.9 -> 8.4 ms)
     const size_t smem = sizeof(dev::Step64SmemT<false>);
@@ -753,6 +841,7 @@ int launch_rlwe_mult_rgsw64(Context &c, const uint64_t *d_acc, const uint64_t *d
     size_t blocks = std::min<size_t>(count, (size_t)sms_of(c) * 2);
     dev::rlwe_mult_rgsw64_kernel<<<(unsigned)blocks, dev::kT64, smem, st>>>(
         d_acc, pairs, d_out, count, stride, (int)c.p.digitG, c.p.BG_bits, c.d_tw64, c.d_itw64, c.nc64, derive ? 1 : 0);
+    c.launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "rlwe_mult_rgsw64 launch");
 }
@@ -825,6 +914,7 @@ static int launch_br64_shape(Context &c, dev::Br64Args A, int max_ctas, cudaStre
     if (e != cudaSuccess) return c.cuda_fail(e, "br64 claim reset");
     if (A.pool_count) {
         dev::br64_pool_init_kernel<<<(unsigned)A.pool_count, dev::kT64, 0, st>>>(A, c.d_tw64, c.d_itw64, c.nc64);
+        c.launches++;
         e = cudaGetLastError();
         if (e != cudaSuccess) return c.cuda_fail(e, "br64 pool launch");
     }
@@ -832,6 +922,7 @@ static int launch_br64_shape(Context &c, dev::Br64Args A, int max_ctas, cudaStre
     int rc = rounds == 1 ? prepare_window(c, (int)steps, st, A.win) : FHEACC_OK;
     if (rc) return rc;
     kern<<<(unsigned)blocks, W * dev::kT64, smem, st>>>(A, c.d_tw64, c.d_itw64, c.nc64);
+    c.launches++;
     e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "br64 launch");
 }
@@ -866,6 +957,7 @@ int launch_extract64(Context &c, const uint64_t *d_rlwe, size_t count, uint64_t 
     if (!count) return FHEACC_OK;
     size_t blocks = std::min<size_t>(count, (size_t)sms_of(c) * 4);
     dev::extract64_kernel<<<(unsigned)blocks, dev::kT64, 0, st>>>(d_rlwe, count, d_extract, c.d_itw64, c.nc64);
+    c.launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "extract64 launch");
 }
@@ -887,6 +979,7 @@ int launch_lwe_keyswitch64(Context &c, const uint64_t *d_extract, size_t count, 
     const unsigned threads = c.dp.ks_row / 2;   // ks_row: a multiple of 32 words, > n
     size_t blocks = std::min<size_t>(count, (size_t)sms_of(c) * 6);
     dev::lwe_ks64_kernel<<<(unsigned)blocks, threads, smem, st>>>(A);
+    c.launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "lwe_ks64 launch");
 }

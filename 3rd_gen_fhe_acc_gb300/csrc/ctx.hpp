@@ -120,6 +120,7 @@ struct Context {
     Scratch psi;                   // CMUX / blind-rotation / homo_expand intermediates (psi.cu)
     unsigned *d_window = nullptr;  // step-window counters, kWindowCapacity + 1 (window.cuh)
     unsigned *d_status = nullptr;  // device status word (kStatus*), after the window counters
+    uint64_t launches = 0;         // kernels launched (or captured into a graph) so far
 
     size_t device_bytes() const
     {

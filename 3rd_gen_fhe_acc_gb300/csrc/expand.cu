@@ -296,11 +296,13 @@ int launch_expand(Context &c, int mode, const uint64_t *d_in, uint64_t *d_out, s
         const size_t smem = 4 * 2048 * sizeof(uint64_t);
         cudaFuncSetAttribute(dev::expand64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         dev::expand64_kernel<<<(unsigned)blocks, 256, smem, st>>>(A, c.d_tw64, c.d_itw64, c.nc64);
+        c.launches++;
     } else {
         if (A.L > 4) return c.fail(FHEACC_EINVAL, "digitKS_R too large for the 32-bit path");
         A.ksk32 = (const uint32_t *)ksk;
         dev::expand32_kernel<<<(unsigned)blocks, 256, 0, st>>>(A, c.nc, c.d_fwd_tw, c.d_inv_tw,
                                                               (uint32_t)((1ULL << 32) / c.p.Q));
+        c.launches++;
     }
     e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "expand launch");
@@ -311,6 +313,7 @@ int launch_to_u32(Context &c, const uint64_t *d_in, uint32_t *d_out, size_t n, c
     if (!n) return FHEACC_OK;
     unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, (size_t)sms(c) * 32);
     dev::to_u32_kernel<<<blocks, 256, 0, st>>>(d_in, d_out, n, c.p.Q);
+    c.launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "convert launch");
 }

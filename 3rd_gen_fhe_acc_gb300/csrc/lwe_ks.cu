@@ -185,11 +185,13 @@ int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, 
     if (e != cudaSuccess) return c.cuda_fail(e, "key switch partials reset");
     dev::ks_partial_kernel<<<(unsigned)(count * slices), c.dp.ks_row / 4, 0, st>>>(
         A, reinterpret_cast<unsigned long long *>(d_partials), slices);
+    c.launches++;
     e = cudaGetLastError();
     if (e != cudaSuccess) return c.cuda_fail(e, "key switch partial launch");
     const size_t words = count * ((size_t)c.p.n + 1);
     dev::ks_final_kernel<<<(unsigned)std::min<size_t>((words + 255) / 256, 1024), 256, 0, st>>>(
         A, reinterpret_cast<const unsigned long long *>(d_partials));
+    c.launches++;
     e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "key switch final launch");
 }
@@ -210,6 +212,7 @@ int launch_lwe_keyswitch32_indexed(Context &c, const uint32_t *d_extract, size_t
     const unsigned threads = (unsigned)(c.dp.ks_row / 4);   // ks_row: multiple of 32 words, > n
     size_t blocks = std::min<size_t>(count, (size_t)std::max(sms, 1) * 16);
     dev::lwe_ks32_kernel<<<(unsigned)blocks, threads, smem, st>>>(A);
+    c.launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "lwe_ks32 launch");
 }
@@ -220,6 +223,7 @@ int launch_modswitch(Context &c, const uint64_t *d_in, size_t count, uint64_t *d
     size_t words = count * ((size_t)c.p.n + 1);
     unsigned blocks = (unsigned)std::min<size_t>((words + 255) / 256, 4096);
     dev::modswitch_kernel<<<blocks, 256, 0, st>>>(d_in, d_out, words, c.p.q, c.p.Q);
+    c.launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "modswitch launch");
 }

@@ -58,6 +58,7 @@ static int launch_elementwise(Context &c, int mode, const uint64_t *a, size_t a_
     const size_t blocks = std::max<size_t>(1, std::min<size_t>((words + 255) / 256, (size_t)std::max(sms, 1) * 8));
     dev::rlwe_elementwise_kernel<<<(unsigned)blocks, 256, 0, st>>>(mode, a, a_stride, b, b_stride, rot, out, count,
                                                                   c.p.N, c.p.Q);
+    c.launches++;
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "elementwise launch");
 }

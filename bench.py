@@ -396,10 +396,13 @@ def run_mixed(args):
     cgraph.close()
     for S in sets:
         S["dout"].zero_()
+    n0 = sum(S["ctx"].kernel_launches() for S in sets)
     for _ in range(args.warmup):
         flush.fill_(1)
         graph.launch(stream.cuda_stream)
     torch.cuda.synchronize()
+    # the graph is captured at its first launch: its kernels, launched by every replay
+    per_replay = sum(S["ctx"].kernel_launches() for S in sets) - n0
     outs_ok = all(np.array_equal(S["dout"].cpu().numpy().view(np.uint64), S["ref_out"]) for S in sets)
     clocks = ClockSampler(0)
     clocks.start()
@@ -494,7 +497,7 @@ def run_mixed(args):
         "concurrent_branches": {"ms_per_step": min(conc_ms), "bitexact": bool(conc_same),
                                 "note": "the two sets as concurrent graph branches; the persistent grids then "
                                         "share SMs unevenly"},
-        "cpu_baseline": cpu, "clocks": clk, "gpu_launches": 4 * args.steps,
+        "cpu_baseline": cpu, "clocks": clk, "gpu_launches": per_replay * args.steps,
         "checks": {"decrypt_ok": dec_ok, "graph_equals_separate_launches": bool(outs_ok),
                    "tuned_equals_untuned": all(S["tuned_same"] for S in sets),
                    "every_request_decrypts": bool(per_request_ok), "setup_s": setup_s},
@@ -591,6 +594,7 @@ def run_psi(args):
     clocks = ClockSampler(0)
     clocks.start()
     phases = []
+    n0 = ctx.kernel_launches()
     for _ in range(args.steps):
         flush.fill_(1)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
@@ -599,6 +603,7 @@ def run_psi(args):
         torch.cuda.synchronize()
         phases.append([ev[i].elapsed_time(ev[i + 1]) for i in range(3)])
     clk = clocks.stop()
+    launches = ctx.kernel_launches() - n0
     step_ms = [sum(ph) for ph in phases]
     value = args.steps / (sum(step_ms) / 1e3)
     repeat_ok = np.array_equal(out.cpu().numpy().view(np.uint64), first_out)
@@ -683,7 +688,7 @@ def run_psi(args):
                 "d2h_bytes_per_step": int(rw * 8), "ms_per_step": 1e3 * statistics.mean(e2e)},
         "phases_ms": {"homo_expand": float(ph[:, 0].mean()), "cmux_tree": float(ph[:, 1].mean()),
                       "blind_rotate": float(ph[:, 2].mean())},
-        "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+        "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
         "checks": {"result_decodes": bool(decodes(first_out)), "e2e_decodes": bool(e2e_ok),
                    "steps_repeatable": bool(repeat_ok), "setup_s": setup_s},
     }
@@ -797,6 +802,7 @@ def main():
     step_ms, br_ms, ks_ms = [], [], []
     D.barrier()
     torch.cuda.synchronize()
+    n0 = ctx.kernel_launches()
     for _ in range(args.steps):
         flush.fill_(1)
         e0, e1 = step_device(True)
@@ -805,6 +811,7 @@ def main():
         b, k = ctx.kernel_times()
         br_ms.append(b)
         ks_ms.append(k)
+    launches = ctx.kernel_launches() - n0
     torch.cuda.synchronize()
     D.barrier()
     clk = clocks.stop()
@@ -947,7 +954,7 @@ def main():
                 "ms_per_step": 1e3 * statistics.mean(e2e_s)},
         "roofline": roofline, "roofline_hbm": roofline_hbm,
         "cpu_baseline": cpu, "clocks": clk,
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": launches * D.ws,
         "plain": {"value": plain_value, "unit": "bootstraps/s", "gates": Pn,
                   "latency_ms_p50": statistics.median(lat), "latency_ms_p99": float(np.percentile(lat, 99)),
                   "batched_over_plain": value / plain_value / D.ws},

@@ -416,6 +416,12 @@ int fheacc_sync(fheacc_ctx *ctx, uint32_t timeout_ms);
 #define FHEACC_STATUS_WAIT_LIMIT 1u
 int fheacc_device_status(fheacc_ctx *ctx, uint32_t *bits);
 
+/* Kernels the context has launched since its creation, counting a kernel
+ * captured into a CUDA graph once (at capture, not per replay); *count = the
+ * total. Reading it around a call gives the number of kernels the call
+ * launched. */
+int fheacc_kernel_launches(const fheacc_ctx *ctx, uint64_t *count);
+
 #ifdef __cplusplus
 }
 #endif

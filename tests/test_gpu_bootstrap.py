@@ -83,6 +83,19 @@ def test_errors(F, ctx0, keys0):
     assert res is None and rc == -1
 
 
+def test_kernel_launch_count(F, ctx0, keys0):
+    """The context counts its kernel launches: a batched bootstrap launches a
+    fixed, small number of kernels (blind rotation, key switch), the same for
+    the same call."""
+    x, y, g, c1, c2 = random_gate_batch(keys0, 40, seed=61)
+    counts = []
+    for _ in range(2):
+        n0 = ctx0.kernel_launches()
+        ctx0.eval_bootstrap_batch(c1, c2, g)
+        counts.append(ctx0.kernel_launches() - n0)
+    assert counts[0] == counts[1] and 2 <= counts[0] <= 4
+
+
 def test_fixed_width_wrappers(F, ctx0, keys0):
     x, y, g, c1, c2 = random_gate_batch(keys0, 4, seed=44)
     res, rc = ctx0.gpu_eval_bootstrap_x4(list(c1), list(c2), list(g))

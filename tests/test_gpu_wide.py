@@ -141,22 +141,25 @@ def test_wide_fpga_compat_mode(F, ctx1, keys1, pipes):
     assert np.array_equal(out, want)
 
 
-def test_wide_rlwe_mult_rgsw_batch(F, ctx1, keys1, cuda_ok):
-    """20 products, one RGSW each: the launch applies the last-digit identity
-    to the RGSWs (from 16 products on) and still gives the oracle's words."""
+@pytest.mark.parametrize("count", [20, 60])
+def test_wide_rlwe_mult_rgsw_batch(F, ctx1, keys1, cuda_ok, count):
+    """One RGSW per product. 20 products (120 product-digit CTAs, at most two
+    per SM) take the digit-split kernel; 60 take the one-CTA-per-product kernel
+    with the last-digit identity applied to the RGSWs. Both give the oracle's
+    words."""
     torch = cuda_ok
     o = keys1.oracle
     Q = keys1.P.Q
     rng = np.random.default_rng(12)
-    acc = rng.integers(0, Q, (20, 4096), dtype=np.uint64)
+    acc = rng.integers(0, Q, (count, 4096), dtype=np.uint64)
     acc[0] = Q - 1
     acc[1] = 0
-    rgsw = rng.integers(0, Q, (20, 6 * 4 * 2048), dtype=np.uint64)
-    out = torch.zeros((20, 4096), dtype=torch.int64, device="cuda")
+    rgsw = rng.integers(0, Q, (count, 6 * 4 * 2048), dtype=np.uint64)
+    out = torch.zeros((count, 4096), dtype=torch.int64, device="cuda")
     da, dr = dev(torch, acc), dev(torch, rgsw)
-    ctx1.rlwe_mult_rgsw(da.data_ptr(), dr.data_ptr(), out.data_ptr(), 20)
+    ctx1.rlwe_mult_rgsw(da.data_ptr(), dr.data_ptr(), out.data_ptr(), count)
     torch.cuda.synchronize()
-    assert np.array_equal(host(out), np.stack([o.rlwe_mult_rgsw(acc[i], rgsw[i]) for i in range(20)]))
+    assert np.array_equal(host(out), np.stack([o.rlwe_mult_rgsw(acc[i], rgsw[i]) for i in range(count)]))
 
 
 @pytest.mark.parametrize("pipes,window,compat", [(2, -1, False), (3, 0, False), (2, -1, True)])

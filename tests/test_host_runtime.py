@@ -76,6 +76,10 @@ def test_context_without_gpu_fails_cleanly(F):
     with pytest.raises(F.FheaccError) as e:
         F.Context(F.params_preset(0), 0)
     assert e.value.code == F.ENODEV
+    # entry points given no context return EINVAL instead of touching memory
+    import ctypes
+    n = ctypes.c_uint64()
+    assert F.lib().fheacc_kernel_launches(None, ctypes.byref(n)) == F.EINVAL
 
 
 def test_keygen_deterministic_and_distributions(F, keys0):
