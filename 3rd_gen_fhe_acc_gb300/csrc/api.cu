@@ -375,6 +375,7 @@ int fheacc_destroy(fheacc_ctx *ctx)
     cudaFree(c->extract.ptr);
     cudaFree(c->io.ptr);
     cudaFree(c->psi.ptr);
+    cudaFree(c->expand.ptr);
     cudaFree(c->d_window);
     if (c->done) cudaEventDestroy(c->done);
     for (auto &ev : c->prof)

@@ -118,14 +118,15 @@ struct Context {
     Scratch extract;               // extracted RLWEs between blind rotation and key switch
     Scratch io;                    // device staging for the host-buffer entry points
     Scratch psi;                   // CMUX / blind-rotation / homo_expand intermediates (psi.cu)
+    Scratch expand;                // shares of the split expand_RLWE levels (expand.cu)
     unsigned *d_window = nullptr;  // step-window counters, kWindowCapacity + 1 (window.cuh)
     unsigned *d_status = nullptr;  // device status word (kStatus*), after the window counters
     uint64_t launches = 0;         // kernels launched (or captured into a graph) so far
 
     size_t device_bytes() const
     {
-        return btkey_bytes + kskey_bytes + subs_bytes + accs.bytes + extract.bytes + io.bytes +
-               2 * (size_t)p.N * sizeof(uint2);
+        return btkey_bytes + kskey_bytes + subs_bytes + accs.bytes + extract.bytes + io.bytes + psi.bytes +
+               expand.bytes + 2 * (size_t)p.N * sizeof(uint2);
     }
     int fail(int code, const std::string &msg)
     {

@@ -250,6 +250,116 @@ __global__ void __launch_bounds__(256) expand64_kernel(const __grid_constant__ E
     }
 }
 
+// An expand_RLWE level of few RLWEs (64-bit words), split over the transform
+// pairs for latency: CTA (item, pair p) takes the item's inverse NTTs, transforms
+// 2p and 2p + 1 of the L + 1 (the key-switch digits of sigma(a), transform L
+// sigma(b)) and their share of the key multiply-accumulate, written to
+// part[item][p] as [sa | sb | fb][2048], each word < 4Q. expand64_combine_kernel
+// adds the shares and applies the level's epilogue. One RLWE's transforms then
+// take two rounds instead of 1 + ceil((L + 1) / 2).
+__global__ void __launch_bounds__(256) expand64_split_kernel(const __grid_constant__ ExpArgs A,
+                                                            uint64_t *__restrict__ part, int P,
+                                                            const ulonglong2 *__restrict__ tw,
+                                                            const ulonglong2 *__restrict__ itw,
+                                                            const __grid_constant__ Ntt64Consts c)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint64_t(*t)[2048] = reinterpret_cast<uint64_t(*)[2048]>(smem_raw);                 // [2][2048]
+    uint64_t(*buf)[2048] = reinterpret_cast<uint64_t(*)[2048]>(smem_raw + 2 * 2048 * 8);  // [2][2048]
+    const int tid = threadIdx.x, grp = tid >> 7, gtid = tid & 127;
+    const uint64_t Q = c.Q;
+    const int L = A.L, nt = L + 1;
+    const size_t per = (size_t)1 << A.f;
+    const size_t it = blockIdx.x / (unsigned)P;
+    const int p = (int)(blockIdx.x - it * (unsigned)P);
+    const size_t bo = it / per * A.bstride, jt = it % per;
+    const uint64_t *in = A.in + bo + jt * 4096;
+    for (int e = gtid; e < 2048; e += 128) t[grp][e] = in[grp * 2048 + e];
+    group_sync(1 + grp, 128);
+    ntt64_inv_2048<128, false>(t[grp], itw, c, gtid, 1 + grp);
+    __syncthreads();
+    const int tr = 2 * p + grp;
+    if (tr < nt) {
+        const int poly = tr == L ? 1 : 0;
+        const bool digit = tr < L;
+        const uint32_t sh = A.bits * (uint32_t)tr;
+        const uint64_t mask = (1ULL << A.bits) - 1;
+        for (int e = gtid; e < 2048; e += 128) {
+            bool neg;
+            const uint32_t s = subs_src((uint32_t)e, A.ipow, 2048, neg);
+            uint64_t v = t[poly][s];
+            if (neg && v) v = Q - v;
+            buf[grp][e] = digit ? (v >> sh) & mask : v;
+        }
+        group_sync(1 + grp, 128);
+        ntt64_fwd_2048<128, false>(buf[grp], tw, c, gtid, 1 + grp);
+    }
+    __syncthreads();
+    uint64_t *o = part + (it * (unsigned)P + (unsigned)p) * 3 * 2048;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int k = tid + 256 * i;
+        uint64_t sa = 0, sb = 0, fb = 0;
+#pragma unroll
+        for (int g2 = 0; g2 < 2; g2++) {
+            const int tq = 2 * p + g2;
+            if (tq >= nt) continue;
+            const uint64_t dv = buf[g2][k];
+            if (tq == L) {
+                fb = barrett64_2q(dv, c.mu64, Q);
+            } else {
+                const ulonglong2 ka = __ldg(A.ksk64 + (size_t)(tq * 2 + 0) * 2048 + k);
+                const ulonglong2 kb = __ldg(A.ksk64 + (size_t)(tq * 2 + 1) * 2048 + k);
+                sa += shoup64(dv, ka.x, ka.y, Q);
+                sb += shoup64(dv, kb.x, kb.y, Q);
+            }
+        }
+        o[k] = sa;
+        o[2048 + k] = sb;
+        o[4096 + k] = fb;
+    }
+}
+
+// The shares of expand64_split_kernel added (P of them, < 4PQ < 2^64, checked
+// by the launcher) and the expand level's epilogue, one thread per item word:
+// s = (-sa, sigma(b) - sb), r[j] <- r[j] + s, r[j + 2^f] <- (r[j] - s) * rot.
+__global__ void expand64_combine_kernel(const __grid_constant__ ExpArgs A, const uint64_t *__restrict__ part, int P,
+                                        size_t items, const __grid_constant__ Ntt64Consts c)
+{
+    const uint64_t Q = c.Q;
+    const size_t per = (size_t)1 << A.f;
+    for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < items * 2048;
+         w += (size_t)gridDim.x * blockDim.x) {
+        const size_t it = w / 2048;
+        const int k = (int)(w - it * 2048);
+        const size_t bo = it / per * A.bstride, jt = it % per;
+        const uint64_t *pp = part + it * (unsigned)P * 3 * 2048 + k;
+        uint64_t sa = 0, sb = 0, fb = 0;
+        for (int p = 0; p < P; p++) {
+            sa += pp[(size_t)(p * 3 + 0) * 2048];
+            sb += pp[(size_t)(p * 3 + 1) * 2048];
+            fb += pp[(size_t)(p * 3 + 2) * 2048];
+        }
+        uint64_t ra = barrett64_2q(sa, c.mu64, Q), rb = barrett64_2q(sb, c.mu64, Q);
+        ra = ra >= Q ? ra - Q : ra;
+        rb = rb >= Q ? rb - Q : rb;
+        const uint64_t nb = fb >= Q ? fb - Q : fb;
+        const uint64_t oa = ra ? Q - ra : 0;
+        const uint64_t ob = nb >= rb ? nb - rb : nb + Q - rb;
+        const uint64_t *in = A.in + bo + jt * 4096;
+        uint64_t *out = A.out + bo + jt * 4096;
+        uint64_t *hi = A.out + bo + (jt + per) * 4096;
+        const uint64_t ta = in[k], tb = in[2048 + k];
+        const uint64_t rot = A.rot[k];
+        const uint64_t s1 = ta + oa, s2 = tb + ob;
+        out[k] = s1 >= Q ? s1 - Q : s1;
+        out[2048 + k] = s2 >= Q ? s2 - Q : s2;
+        const uint64_t d1 = ta >= oa ? ta - oa : ta + Q - oa, d2 = tb >= ob ? tb - ob : tb + Q - ob;
+        hi[k] = (uint64_t)((unsigned __int128)d1 * rot % Q);
+        hi[2048 + k] = (uint64_t)((unsigned __int128)d2 * rot % Q);
+    }
+}
+
 __global__ void to_u32_kernel(const uint64_t *__restrict__ in, uint32_t *__restrict__ out, size_t n, uint64_t Q)
 {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -294,6 +404,26 @@ int launch_expand(Context &c, int mode, const uint64_t *d_in, uint64_t *d_out, s
         if (A.L > 8) return c.fail(FHEACC_EINVAL, "digitKS_R too large");
         A.ksk64 = (const ulonglong2 *)ksk;
         const size_t smem = 4 * 2048 * sizeof(uint64_t);
+        // an expand level of at most two CTAs per SM of (item, transform pair)
+        // splits each item over its transform pairs, for latency
+        const int P = (A.L + 2) / 2;
+        if (mode == dev::kExpand && items * P <= (size_t)sms(c) * 2 && (uint64_t)4 * P < UINT64_MAX / c.p.Q) {
+            const size_t words = items * P * 3 * 2048;
+            int rc = ensure_scratch(c, c.expand, words * sizeof(uint64_t));
+            if (rc) return rc;
+            uint64_t *part = (uint64_t *)c.expand.ptr;
+            cudaFuncSetAttribute(dev::expand64_split_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            dev::expand64_split_kernel<<<(unsigned)(items * P), 256, smem, st>>>(A, part, P, c.d_tw64, c.d_itw64,
+                                                                                 c.nc64);
+            c.launches++;
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return c.cuda_fail(e, "expand split launch");
+            const unsigned cb = (unsigned)std::min<size_t>((items * 2048 + 255) / 256, (size_t)sms(c) * 4);
+            dev::expand64_combine_kernel<<<cb, 256, 0, st>>>(A, part, P, items, c.nc64);
+            c.launches++;
+            e = cudaGetLastError();
+            return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "expand combine launch");
+        }
         cudaFuncSetAttribute(dev::expand64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         dev::expand64_kernel<<<(unsigned)blocks, 256, smem, st>>>(A, c.d_tw64, c.d_itw64, c.nc64);
         c.launches++;
