@@ -884,7 +884,7 @@ int fheacc_device_status(fheacc_ctx *ctx, uint32_t *bits)
 int fheacc_kernel_launches(const fheacc_ctx *ctx, uint64_t *count)
 {
     if (!ctx || !count) return FHEACC_EINVAL;
-    *count = reinterpret_cast<const Context *>(ctx)->launches;
+    *count = reinterpret_cast<const Context *>(ctx)->launches.load(std::memory_order_relaxed);
     return FHEACC_OK;
 }
 

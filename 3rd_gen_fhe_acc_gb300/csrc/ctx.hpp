@@ -2,6 +2,7 @@
 // the kernel translation units. Internal to libfheacc.so.
 #pragma once
 #include <cuda_runtime.h>
+#include <atomic>
 #include <cstdint>
 #include <string>
 #include "fheacc.h"
@@ -121,7 +122,8 @@ struct Context {
     Scratch expand;                // shares of the split expand_RLWE levels (expand.cu)
     unsigned *d_window = nullptr;  // step-window counters, kWindowCapacity + 1 (window.cuh)
     unsigned *d_status = nullptr;  // device status word (kStatus*), after the window counters
-    uint64_t launches = 0;         // kernels launched (or captured into a graph) so far
+    std::atomic<uint64_t> launches{0};   // kernels launched (or captured into a graph) so far;
+                                         // atomic: a server's worker thread launches while others read
 
     size_t device_bytes() const
     {
