@@ -158,6 +158,7 @@ def lib():
             "fheacc_set_option": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int]),
             "fheacc_measure_imad_rate": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
             "fheacc_measure_components": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
+            "fheacc_measure_l2_read_rate": (ctypes.c_int, [vp, ctypes.POINTER(ctypes.c_double)]),
             "fheacc_autotune": (ctypes.c_int, [vp, sz, ctypes.POINTER(TuneTrial), ctypes.c_int,
                                                ctypes.POINTER(ctypes.c_int)]),
             "fheacc_graph_create": (ctypes.c_int, [ctypes.POINTER(vp), ctypes.c_uint32]),
@@ -515,6 +516,12 @@ class Context:
         """IMAD lane operations per second of this device."""
         v = ctypes.c_double()
         self.check(lib().fheacc_measure_imad_rate(self._h, ctypes.byref(v)))
+        return v.value
+
+    def measure_l2_read_rate(self):
+        """L2 read bytes per second of this device (streaming probe)."""
+        v = ctypes.c_double()
+        self.check(lib().fheacc_measure_l2_read_rate(self._h, ctypes.byref(v)))
         return v.value
 
     def measure_components(self):

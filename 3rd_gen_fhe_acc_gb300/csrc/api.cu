@@ -781,6 +781,14 @@ int fheacc_measure_imad_rate(fheacc_ctx *ctx, double *imad_per_s)
     return measure_imad_rate(c, imad_per_s);
 }
 
+int fheacc_measure_l2_read_rate(fheacc_ctx *ctx, double *bytes_per_s)
+{
+    if (!ctx || !bytes_per_s) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    DeviceGuard g(c.device);
+    return measure_l2_read_rate(c, bytes_per_s);
+}
+
 int fheacc_measure_components(fheacc_ctx *ctx, double ns[4])
 {
     if (!ctx || !ns) return FHEACC_EINVAL;

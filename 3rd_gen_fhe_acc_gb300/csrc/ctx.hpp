@@ -47,6 +47,10 @@ struct Tuning {
 
 constexpr size_t kPipeSmemBudget = 220 * 1024;   // dynamic shared memory of one blind-rotation CTA
 
+// Threads of a 32-bit LWE key-switch CTA, four words of a key row each: rows
+// of up to n + 1 <= 1024 words.
+constexpr int kKsMaxThreads = 256;
+
 constexpr size_t kClaimWords = 64;   // u32 words of claim counters after the blind-rotation accumulators
 // 64-bit blind rotation: most remainder gates of a batch that the CTAs share
 // item by item (their per-gate state follows the claim words)
@@ -212,6 +216,7 @@ int launch_to_u32(Context &c, const uint64_t *d_in, uint32_t *d_out, size_t n, c
 // IMAD throughput probe (probe.cu)
 int measure_imad_rate(Context &c, double *imad_per_s);
 int measure_components(Context &c, double ns[4]);
+int measure_l2_read_rate(Context &c, double *bytes_per_s);
 
 constexpr size_t kExtractStride = 1024 + 32;   // u32 words per extracted RLWE (N = 1024)
 constexpr size_t kExtract64 = 2048 + 8;        // u64 words per extracted RLWE (N = 2048)

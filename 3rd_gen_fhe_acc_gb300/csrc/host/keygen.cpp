@@ -1,13 +1,14 @@
 // keygen.cpp -- seeded key generation, encryption and decryption on the host.
 //
 // The reference draws its randomness from std::default_random_engine seeded by
-// std::random_device (RNG.cpp:3-37), which is neither reproducible nor the same
+// std::random_device (src/RNG.cpp:3-36), which is neither reproducible nor the same
 // across standard libraries. Here every object is drawn from its own SplitMix64
 // stream keyed by (seed, object kind, object index), so a seed gives the same
 // words on every machine and for any thread count. The distributions are the
 // reference's: uniform mod q / mod Q, ternary {-1, 0, 1} secrets with the
 // reference's rejection bounds, and a normal variate (sigma 3.19) truncated
-// toward zero and reduced '% bound' (RNG.cpp:40-48), sampled from an integer
+// toward zero and reduced '% bound' (RNG_norm::generate_norm, include/RNG.h:27,
+// src/RNG.cpp:19-36), sampled from an integer
 // cumulative table (gauss_cdt.inc).
 #include "host_math.hpp"
 #include <algorithm>
@@ -59,7 +60,7 @@ struct Rng {
         }
     }
     int64_t ternary() { return (int64_t)uniform(3) - 1; }
-    // RNG_norm::generate_norm(bound), RNG.cpp:40-48
+    // RNG_norm::generate_norm(bound), include/RNG.h:27, src/RNG.cpp:19-36
     int64_t gauss(uint64_t bound)
     {
         uint64_t u = next();

@@ -30,8 +30,6 @@ struct KsArgs {
     uint64_t Q;
 };
 
-constexpr int kKsMaxThreads = 256;   // up to n + 1 <= 1024 coefficients (4 per thread)
-
 __device__ __forceinline__ uint64_t scale_round_dev(uint64_t x, uint64_t new_mod, uint64_t old_mod)
 {
     // LWE.cpp:255-260: (old + 2 x new) / (2 old), exact integer
@@ -172,7 +170,7 @@ int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, 
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
     // a few ciphertexts: split each one's rows over many CTAs
     if (!d_partials || count == 0 || count >= 2 * (size_t)std::max(sms, 1) || !c.d_kskey ||
-        c.p.n + 1 > 4 * dev::kKsMaxThreads)
+        c.p.n + 1 > 4 * kKsMaxThreads)
         return launch_lwe_keyswitch32_indexed(c, d_extract, count, modswitch, d_out, nullptr, st);
     dev::KsArgs A{};
     A.ext = d_extract; A.count = count; A.kskey = c.d_kskey; A.out = d_out; A.out_idx = nullptr;
@@ -201,7 +199,7 @@ int launch_lwe_keyswitch32_indexed(Context &c, const uint32_t *d_extract, size_t
 {
     if (!count) return FHEACC_OK;
     if (!c.d_kskey) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
-    if (c.p.n + 1 > 4 * dev::kKsMaxThreads) return c.fail(FHEACC_EINVAL, "n too large for key switch");
+    if (c.p.n + 1 > 4 * kKsMaxThreads) return c.fail(FHEACC_EINVAL, "n too large for key switch");
     dev::KsArgs A{};
     A.ext = d_extract; A.count = count; A.kskey = c.d_kskey; A.out = d_out; A.out_idx = d_out_idx;
     A.n = c.p.n; A.N = c.p.N; A.digitKS = (int)c.p.digitKS; A.Bks = c.p.Bks; A.ks_row = c.dp.ks_row;

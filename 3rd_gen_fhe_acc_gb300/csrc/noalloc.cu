@@ -22,6 +22,13 @@ constexpr size_t kNoAllocAccWords = (size_t)FHEACC_NOALLOC_MAX_GATES * 2048 + kC
 constexpr size_t kNoAllocWords = kNoAllocAccWords + (size_t)FHEACC_NOALLOC_MAX_GATES * kExtractStride;
 static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWords];
 
+// The split key switch of a call (launch_lwe_keyswitch32 with partial sums)
+// keeps ks_row 64-bit sums per gate in the accumulator area, 2048 words per
+// gate; ks_row is at most 4 * kKsMaxThreads words (the key-switch CTA width),
+// and the upload refuses wider rows, so the sums fit.
+static_assert(4 * kKsMaxThreads * sizeof(uint64_t) <= 2048 * sizeof(uint32_t),
+              "key-switch partial sums must fit in one gate's accumulator words");
+
 namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
@@ -66,19 +73,29 @@ extern "C" int fheacc_bootstrap_noalloc(fheacc_ctx *ctx, const uint64_t *d_c1, c
     if (!d_c1 || !d_c2 || !d_gates || !d_out) return c.fail(FHEACC_EINVAL, "null buffer");
     if (!c.d_btkey) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
     if (!c.d_kskey) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
+    if (c.dp.ks_row > 4 * kKsMaxThreads) return c.fail(FHEACC_EINVAL, "fheacc_bootstrap_noalloc: n too large");
     int prev = -1;
     cudaGetDevice(&prev);
     if (prev != c.device) cudaSetDevice(c.device);
     uint32_t *scratch = nullptr;
     int rc = noalloc_scratch(c, &scratch);
-    // Every word of the scratch a call reads was written earlier in the same
-    // call (accumulators by the blind rotation's prologue, extracted RLWEs by
-    // its epilogue), so nothing has to be cleared between calls.
+    // The array keeps the previous call's words. The accumulators and the
+    // extracted RLWEs are written by this call before they are read (the blind
+    // rotation's prologue and epilogue); the two parts that must start at zero
+    // are reset on the stream with cudaMemsetAsync, which allocates nothing:
+    // the blind rotation's claim counter (after the accumulators) and the
+    // split key switch's 64-bit partial sums (in the accumulator area, free
+    // once the blind rotation is done).
     if (rc == FHEACC_OK) {
         cudaStream_t st = (cudaStream_t)stream;
         uint32_t *accs = scratch, *ext = scratch + kNoAllocAccWords;
+        const bool prof = (flags & FHEACC_FLAG_PROFILE) != 0;
+        flags &= ~(uint32_t)FHEACC_FLAG_PROFILE;
+        if (prof) cudaEventRecord(c.prof[0], st);
         rc = launch_blind_rotate32_with(c, d_c1, d_c2, d_gates, count, flags, accs, ext, st);
+        if (rc == FHEACC_OK && prof) cudaEventRecord(c.prof[1], st);
         if (rc == FHEACC_OK) rc = launch_lwe_keyswitch32(c, ext, count, true, d_out, st, (uint64_t *)accs);
+        if (rc == FHEACC_OK && prof) cudaEventRecord(c.prof[2], st);
         if (rc == FHEACC_OK) {
             cudaError_t e = cudaEventRecord(c.done, st);
             if (e != cudaSuccess) rc = c.cuda_fail(e, "event record");

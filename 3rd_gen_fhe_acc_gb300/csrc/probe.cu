@@ -6,6 +6,9 @@
 // condition that never holds, so the work cannot be removed by the compiler
 // and nothing is stored.
 //
+// measure_l2_read_rate: the device's L2 read bandwidth, the peak the
+// blind rotation's key streaming (RGSW words served from L2) is compared with.
+//
 // measure_components: the SM time of each piece of one RLWE x RGSW step when
 // run alone at the blind-rotation kernel's occupancy (10-warp CTAs, two per
 // SM): the forward, digit and inverse NTTs of ntt32.cuh on the context's
@@ -14,6 +17,7 @@
 // time the pipeline would take with perfect overlap.
 #include "ctx.hpp"
 #include "step32.cuh"
+#include <algorithm>
 
 namespace fheacc {
 namespace dev {
@@ -99,7 +103,56 @@ __global__ void __launch_bounds__(32 * (2 * DG + 2), 2) mac_rate_kernel(const ui
     }
 }
 
+// Streaming read of a buffer that fits in L2 (after a warm-up pass it is
+// L2-resident): every thread reads 16-byte words with ld.global.cg (cached in
+// L2 only) over `passes` sweeps of its grid-strided share; the XOR of the
+// words is stored only under a condition that never holds.
+__global__ void l2_read_kernel(const uint4 *__restrict__ buf, size_t words, int passes, uint32_t *sink)
+{
+    uint32_t h = 0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (int p = 0; p < passes; p++) {
+        for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < words; i += 4 * stride) {
+            uint4 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) v[u] = i + u * stride < words ? __ldcg(buf + i + u * stride) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+            for (int u = 0; u < 4; u++) h ^= v[u].x ^ v[u].y ^ v[u].z ^ v[u].w;
+        }
+    }
+    if (h == 0x9E3779B9u && sink) sink[0] = h;
+}
+
 }  // namespace dev
+
+template <class F>
+static int time_best(Context &c, F launch, float *best_ms);
+
+int measure_l2_read_rate(Context &c, double *bytes_per_s)
+{
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
+    int l2 = 0;
+    cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c.device);
+    // a third of L2: resident after the first sweep on either L2 partition
+    const size_t bytes = std::max<size_t>((size_t)std::max(l2, 1 << 20) / 3 / 4096 * 4096, 1 << 20);
+    void *buf = nullptr;
+    if (cudaMalloc(&buf, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return c.fail(FHEACC_ENOMEM, "L2 probe buffer");
+    }
+    cudaMemsetAsync(buf, 1, bytes, c.stream);
+    const int blocks = (sms > 0 ? sms : 1) * 4, threads = 512, passes = 40;
+    const size_t words = bytes / 16;
+    float ms = 0;
+    int rc = time_best(c, [&] {
+        dev::l2_read_kernel<<<blocks, threads, 0, c.stream>>>((const uint4 *)buf, words, passes, nullptr);
+    }, &ms);
+    cudaFree(buf);
+    if (rc) return rc;
+    *bytes_per_s = (double)bytes * passes / (ms * 1e-3);
+    return FHEACC_OK;
+}
 
 int measure_imad_rate(Context &c, double *imad_per_s)
 {

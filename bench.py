@@ -159,22 +159,23 @@ def cpu_cores():
 
 
 def run_reference(args):
-    """CPU restatement of eval_bootstrap (oracle/), all host cores."""
+    """CPU restatement of eval_bootstrap (oracle/), all host cores. Keys,
+    inputs and parameters come from the oracle alone (its own seeded key
+    generation): this arm loads no product library."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    import __graft_entry__
-    __graft_entry__.build_product()
-    __graft_entry__._build_oracle()
-    import importlib
-    F = importlib.import_module("3rd_gen_fhe_acc_gb300")
     from oracle_lib import Oracle
-    P = F.params_preset(args.preset)
-    lsk, rsk, x, y, c1, c2, gates = make_inputs(F, P, args.batch, 0)
-    bt = F.bootstrap_key(P, SEEDS["btkey"], lsk, rsk)
-    ks = F.keyswitch_key(P, SEEDS["kskey"], rsk, lsk)
-    ora = Oracle.from_params(P)
+    ora = Oracle.preset(args.preset)
+    P = ora.p
     cores = cpu_cores()
+    lsk, rsk, bt, ks = ora.keygen(SEEDS["lwe_sk"], threads=cores)
+    rng = np.random.default_rng(1000)
+    x = rng.integers(0, 2, args.batch).astype(np.uint8)
+    y = rng.integers(0, 2, args.batch).astype(np.uint8)
+    c = ora.lwe_encrypt(SEEDS["enc"], lsk, np.concatenate([x, y]))
+    c1, c2 = c[:args.batch].copy(), c[args.batch:].copy()
+    gates = np.full(args.batch, 3, dtype=np.int32)   # NAND (params.h:107)
     per_step = args.cpu_sample or (2 if P.N == 1024 else 1) * cores
     times = []
     for s in range(args.warmup + args.steps):
@@ -184,6 +185,8 @@ def run_reference(args):
                                                bt, ks, threads=cores)
         dt = time.perf_counter() - t0
         assert failed == 0
+        dec = np.array([ora.lwe_decrypt(lsk, o) for o in out], dtype=np.uint8)
+        assert np.array_equal(dec, 1 - (x[lo:lo + per_step] & y[lo:lo + per_step])), "oracle NAND decrypts wrong"
         if s >= args.warmup:
             times.append(dt)
     value = per_step / statistics.mean(times)
@@ -191,15 +194,25 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "bootstraps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": config_of(P, args),
+        "config": config_of(param_view(P), args),
         "cpu_baseline": {"value": value, "unit": "bootstraps/s", "cores": cores, "kind": "port",
                          "sample": "%d gates per step of the %d-gate batch, oracle eval_bootstrap "
-                                   "(C restatement of RLWE.cpp:726-786) on %d threads" % (per_step, args.batch,
-                                                                                        cores)},
+                                   "(C restatement of RLWE.cpp:726-786) on %d threads; keys from the oracle's own "
+                                   "generator" % (per_step, args.batch, cores)},
         "e2e": {"value": value, "unit": "bootstraps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
+
+
+def param_view(p):
+    """The fields config_of reads, from an oracle parameter set."""
+    class V:
+        pass
+    v = V()
+    v.n, v.q, v.N, v.Q, v.BG_bits, v.digitG = p.n, p.q, p.N, p.Q, p.BGbits, p.digitG
+    v.Br, v.digitR, v.Bks, v.digitKS = p.Br, p.digitR, p.Bks, p.digitKS
+    return v
 
 
 def profile_case(preset=0):
@@ -891,6 +904,12 @@ def main():
             peaks_src = "measured (MEASURED_PEAKS.json hbm_gbs)"
     hbm_peak = hbm_peak or 6800.0
     key_stream_gbs = total_steps * rgsw_bytes / br_s / 1e9
+    l2_peak_gbs = ctx.measure_l2_read_rate() / 1e9
+    # plain form: one gate per launch sequence streams its own RGSW per step
+    # and its key-switch rows; the mean gate of the sample
+    ks_rows = P.N * P.digitKS
+    plain_bytes = float(steps[:Pn].mean()) * rgsw_bytes + ks_rows * (P.n + 1) * word
+    plain_gbs = plain_bytes / (statistics.mean(lat) / 1e3) / 1e9
     roofline = {
         "bound": "int", "achieved": achieved_modmul / 1e9, "peak": peak_modmul / 1e9, "unit": "G modmul/s",
         "frac": achieved_modmul / peak_modmul, "traffic": traffic,
@@ -916,9 +935,23 @@ def main():
         "bound": "hbm", "achieved": btkey_bytes / br_s / 1e9, "peak": hbm_peak, "unit": "GB/s",
         "frac": btkey_bytes / br_s / 1e9 / hbm_peak, "traffic": traffic,
         "algorithmic_bytes": btkey_bytes, "peak_source": peaks_src,
-        "key_stream_gbs": key_stream_gbs, "key_stream_frac": key_stream_gbs / hbm_peak,
-        "note": "algorithmic bytes = bootstrap key read once per launch; key_stream = RGSW bytes consumed by "
-                "all steps of all gates (served mostly from L2)",
+        "plain": {"achieved": plain_gbs, "frac": plain_gbs / hbm_peak, "algorithmic_bytes_per_gate": plain_bytes,
+                  "note": "one gate per launch sequence: its RGSW per step and its key-switch rows, over the "
+                          "plain latency"},
+        "target_60pct_met": False,
+        "note": "batched: algorithmic bytes = the bootstrap key read once per launch; the batch shares every key "
+                "tile, so the launch is bound by the integer multiply pipe and its HBM fraction is small by "
+                "construction. Plain: one gate's steps are a serial chain of RLWE x RGSW products on one SM, "
+                "latency-bound. Neither form reaches 60% of HBM.",
+    }
+    roofline_l2 = {
+        "bound": "l2", "achieved": key_stream_gbs, "peak": l2_peak_gbs, "unit": "GB/s",
+        "frac": key_stream_gbs / l2_peak_gbs,
+        "algorithmic_bytes": total_steps * rgsw_bytes,
+        "peak_source": "fheacc_measure_l2_read_rate in this run: every SM streaming a buffer of a third of L2 "
+                       "with 16-byte L2-only loads",
+        "note": "key streaming: the RGSW bytes all steps of all gates consume (each gate reads its residue's "
+                "RGSW every step), served from L2",
     }
 
     cpu = None
@@ -952,7 +985,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": "bootstraps/s",
                 "h2d_bytes_per_step": int(2 * B * W * 8 + B * 4), "d2h_bytes_per_step": int(B * W * 8),
                 "ms_per_step": 1e3 * statistics.mean(e2e_s)},
-        "roofline": roofline, "roofline_hbm": roofline_hbm,
+        "roofline": roofline, "roofline_hbm": roofline_hbm, "roofline_l2": roofline_l2,
         "cpu_baseline": cpu, "clocks": clk,
         "gpu_launches": launches * D.ws,
         "plain": {"value": plain_value, "unit": "bootstraps/s", "gates": Pn,

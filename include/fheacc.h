@@ -178,8 +178,11 @@ int fheacc_bootstrap_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t
  * device looks up the array's device address (make that first call before any
  * stream capture). All calls share the one array: calls whose work overlaps on
  * the GPU (different streams, or different contexts on the same device) race
- * and give wrong results; order them on one stream or synchronise. Keys must
- * have been uploaded to ctx beforehand. */
+ * and give wrong results; order them on one stream or synchronise. Each call
+ * resets the array's claim counter and key-switch partial sums with
+ * cudaMemsetAsync on `stream` (no allocation), then launches the kernels;
+ * FHEACC_FLAG_PROFILE records the same events as fheacc_bootstrap_async. Keys
+ * must have been uploaded to ctx beforehand. */
 #define FHEACC_NOALLOC_MAX_GATES 64
 int fheacc_bootstrap_noalloc(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2,
                              const int32_t *d_gates, size_t count, uint64_t *d_out, uint32_t flags,
@@ -255,6 +258,11 @@ int fheacc_kernel_times(fheacc_ctx *ctx, float ms[2]);
  * operations per second) with a short dependent-chain kernel of this library;
  * the denominator of the integer roofline. */
 int fheacc_measure_imad_rate(fheacc_ctx *ctx, double *imad_per_s);
+/* Measures this device's L2 read bandwidth (bytes per second): a streaming
+ * read of a buffer of a third of L2, resident after a warm-up sweep, by every
+ * SM with 16-byte L2-only loads; the peak against which the blind rotation's
+ * key streaming (RGSW words served from L2) is reported. */
+int fheacc_measure_l2_read_rate(fheacc_ctx *ctx, double *bytes_per_s);
 /* SM time, in ns per unit per SM, of the pieces of one blind-rotation step run
  * alone at the blind-rotation kernel's occupancy: ns[0] forward NTT, ns[1]
  * digit NTT (table-driven first stages), ns[2] inverse NTT, ns[3] multiply-

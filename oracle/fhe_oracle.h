@@ -148,6 +148,18 @@ void ora_rlwe_blind_rotate(const ora_params *p, const uint64_t *c, int forward, 
 void ora_homo_expand(const ora_params *p, const uint64_t *packed, const uint64_t *enc_sec,
                      const uint64_t *subs_key, uint64_t *out);
 
+/* Key generation and LWE encryption (fhe_keygen.c): the reference's key
+ * formats and distributions from a seeded generator of the oracle's own (not
+ * the product's words). */
+int ora_keygen_lwe_sk(const ora_params *p, uint64_t seed, uint64_t *sk);              /* LWE.cpp:22-53   */
+int ora_keygen_rlwe_sk(const ora_params *p, uint64_t seed, uint64_t *sk_ntt);         /* RLWE.cpp:243-279 */
+int ora_keygen_bootstrap_key(const ora_params *p, uint64_t seed, uint64_t E_rlwe, const uint64_t *lwe_sk,
+                             const uint64_t *rlwe_sk_ntt, uint64_t *btkey, int threads);   /* RLWE.cpp:561-606 */
+int ora_keygen_lwe_ks_key(const ora_params *p, uint64_t seed, uint64_t E_rlwe, const uint64_t *rlwe_sk_ntt,
+                          const uint64_t *lwe_sk, uint64_t *kskey, int threads);         /* LWE.cpp:55-106  */
+int ora_lwe_encrypt(const ora_params *p, uint64_t seed, uint64_t E, const uint64_t *sk, const uint8_t *bits,
+                    size_t count, uint64_t *out);                                        /* LWE.cpp:134-145 */
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,6 +1,7 @@
 """Extracts the reference's golden transcripts into compact fixtures.
 
-Sources (reference project, read where it is mounted; default /root/reference):
+Sources (reference project: the path given as the first argument, else the
+link oracle/_ref/reference that oracle/build_ref.sh leaves where it is mounted):
   cl_fhe_acc/verif/tests/mem_init_content/top_verify/bootstrap/bk/RLWExRGSW_output.txt
       one RLWE_mult_RGSW at N=1024, Q=0x7FFF801, BG=2^9, digitG=3
       (printed by the commented-out trace in FHE_ACC_runtime/src/RLWE.cpp:649-700)
@@ -122,7 +123,8 @@ def params(ref):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    here = os.path.dirname(os.path.abspath(__file__))
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.path.join(here, "..", "..", "oracle", "_ref", "reference")
     rlwe_x_rgsw(ref)
     rlwesubs(ref)
     params(ref)

@@ -2,9 +2,10 @@
 reference sources by oracle/build_ref.sh) on keys and ciphertexts generated
 from fixed seeds by this package, and stores the outputs as a fixture.
 
-The GPU test tests/test_gpu_reference_fixture.py regenerates the same keys
-from the same seeds (the generator is integer-only, so every machine gets the
-same words) and compares the GPU outputs with these reference outputs.
+The GPU test test_reference_fixture (tests/test_gpu_bootstrap.py) regenerates
+the same keys from the same seeds (the generator is integer-only, so every
+machine gets the same words) and compares the GPU outputs with these
+reference outputs; test_oracle_equals_reference_outputs checks the oracle.
 
 Run here, where the reference is mounted:
     python tests/golden/make_ref_fixtures.py

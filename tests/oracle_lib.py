@@ -24,10 +24,15 @@ def pkg():
     return importlib.import_module("3rd_gen_fhe_acc_gb300")
 
 
+ORACLE_SOURCES = ["fhe_oracle.c", "fhe_keygen.c"]
+
+
 def build_oracle():
-    src = os.path.join(ORACLE_DIR, "fhe_oracle.c")
-    if not os.path.exists(ORACLE_LIB) or os.path.getmtime(ORACLE_LIB) < os.path.getmtime(src):
-        subprocess.check_call(["gcc", "-O3", "-fPIC", "-shared", "-pthread", src, "-o", ORACLE_LIB + ".tmp"])
+    srcs = [os.path.join(ORACLE_DIR, s) for s in ORACLE_SOURCES]
+    deps = srcs + [os.path.join(ORACLE_DIR, "fhe_oracle.h")]
+    if not os.path.exists(ORACLE_LIB) or any(os.path.getmtime(ORACLE_LIB) < os.path.getmtime(d) for d in deps):
+        subprocess.check_call(["gcc", "-O3", "-fPIC", "-shared", "-pthread"] + srcs + ["-lm", "-o",
+                                                                                       ORACLE_LIB + ".tmp"])
         os.replace(ORACLE_LIB + ".tmp", ORACLE_LIB)
     return ORACLE_LIB
 
@@ -86,6 +91,14 @@ class Oracle:
             ("ora_cmux", None, [ctypes.POINTER(OraParams), _u64p, _u64p, _u64p, _u64p]),
             ("ora_rlwe_blind_rotate", None, [ctypes.POINTER(OraParams), _u64p, ctypes.c_int, _u64p, _u64p]),
             ("ora_homo_expand", None, [ctypes.POINTER(OraParams), _u64p, _u64p, _u64p, _u64p]),
+            ("ora_keygen_lwe_sk", ctypes.c_int, [ctypes.POINTER(OraParams), ctypes.c_uint64, _u64p]),
+            ("ora_keygen_rlwe_sk", ctypes.c_int, [ctypes.POINTER(OraParams), ctypes.c_uint64, _u64p]),
+            ("ora_keygen_bootstrap_key", ctypes.c_int, [ctypes.POINTER(OraParams), ctypes.c_uint64, ctypes.c_uint64,
+                                                        _u64p, _u64p, _u64p, ctypes.c_int]),
+            ("ora_keygen_lwe_ks_key", ctypes.c_int, [ctypes.POINTER(OraParams), ctypes.c_uint64, ctypes.c_uint64,
+                                                     _u64p, _u64p, _u64p, ctypes.c_int]),
+            ("ora_lwe_encrypt", ctypes.c_int, [ctypes.POINTER(OraParams), ctypes.c_uint64, ctypes.c_uint64, _u64p,
+                                               ctypes.POINTER(ctypes.c_uint8), ctypes.c_size_t, _u64p]),
         ]:
             f = getattr(L, name)
             f.restype = res
@@ -99,6 +112,35 @@ class Oracle:
             p.gate_constant[i] = gc[i]
         assert L.ora_params_setup(ctypes.byref(p)) == 0
         self.p = p
+
+    # The measured parameter sets, stated without the product (the CPU
+    # reference arm of bench.py builds its oracle from these):
+    # 0: n=500, N=1024, Q = largest prime < 2^27 with Q = 1 mod 2N, BG=2^7;
+    # 1: n=630, N=2048, Q < 2^54, BG=2^9; both q=512, Br=23, Bks=25, Bks_R=2^9.
+    PRESETS = {0: dict(n=500, q=512, N=1024, nbit=27, BGbits=7, Br=23, Bks=25, Bks_R_bits=9),
+               1: dict(n=630, q=512, N=2048, nbit=54, BGbits=9, Br=23, Bks=25, Bks_R_bits=9)}
+
+    @classmethod
+    def preset(cls, k, n=None):
+        """A preset with the reference's derivations (digit counts as the
+        smallest that cover the modulus, fhe_wo_fpga.cpp:89-161)."""
+        d = dict(cls.PRESETS[k])
+        if n is not None:
+            d["n"] = n
+        L = ctypes.CDLL(build_oracle())
+        L.ora_find_Q.restype = ctypes.c_uint64
+        L.ora_find_Q.argtypes = [ctypes.c_int, ctypes.c_int]
+        Q = L.ora_find_Q(d["nbit"], d["N"])
+
+        def digits(base, mod):
+            c, v = 0, 1
+            while v < mod:
+                v *= base
+                c += 1
+            return c
+        return cls(d["n"], d["q"], d["N"], Q, d["BGbits"], digits(1 << d["BGbits"], Q), d["Br"],
+                   digits(d["Br"], d["q"]), d["Bks"], digits(d["Bks"], Q), d["Bks_R_bits"],
+                   digits(1 << d["Bks_R_bits"], Q))
 
     @classmethod
     def from_params(cls, P):
@@ -189,6 +231,29 @@ class Oracle:
                                                  c1.shape[0], p64(btkey), p64(kskey), int(fpga_compat), threads,
                                                  p64(out))
         return out, failed
+
+    def keygen(self, seed, threads=0, E_rlwe=18):
+        """(lwe_sk, rlwe_sk_ntt, btkey, kskey) from the oracle's own seeded
+        generator (fhe_keygen.c), in the reference's layouts."""
+        p = self.p
+        threads = threads or os.cpu_count() or 1
+        lsk = np.zeros(p.n, dtype=np.uint64)
+        rsk = np.zeros(p.N, dtype=np.uint64)
+        assert self.L.ora_keygen_lwe_sk(ctypes.byref(p), seed, p64(lsk)) == 0
+        assert self.L.ora_keygen_rlwe_sk(ctypes.byref(p), seed + 1, p64(rsk)) == 0
+        bt = np.zeros(p.Br * p.digitR * p.n * p.digitG * 4 * p.N, dtype=np.uint64)
+        ks = np.zeros(p.Bks * p.digitKS * p.N * (p.n + 1), dtype=np.uint64)
+        self.L.ora_keygen_bootstrap_key(ctypes.byref(p), seed + 2, E_rlwe, p64(lsk), p64(rsk), p64(bt), threads)
+        self.L.ora_keygen_lwe_ks_key(ctypes.byref(p), seed + 3, E_rlwe, p64(rsk), p64(lsk), p64(ks), threads)
+        return lsk, rsk, bt, ks
+
+    def lwe_encrypt(self, seed, sk, bits):
+        """LWE_encrypt (t = 4, E = q/16) of each bit: [count][n+1]."""
+        bits = np.ascontiguousarray(bits, dtype=np.uint8)
+        out = np.zeros((bits.size, self.p.n + 1), dtype=np.uint64)
+        self.L.ora_lwe_encrypt(ctypes.byref(self.p), seed, self.p.q // 16, p64(np.ascontiguousarray(sk)),
+                               bits.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), bits.size, p64(out))
+        return out
 
     def lwe_decrypt(self, sk, c, t=4):
         return self.L.ora_lwe_decrypt(ctypes.byref(self.p), p64(np.ascontiguousarray(sk, dtype=np.uint64)),

@@ -9,7 +9,8 @@ import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-REF_INC = "/root/reference/FHE_ACC_runtime/include"
+# the reference runtime's headers, through the link oracle/build_ref.sh leaves
+REF_INC = os.path.join(ROOT, "oracle", "_ref", "reference", "FHE_ACC_runtime", "include")
 
 
 def test_c_client_links_and_runs(F, tmp_path):
