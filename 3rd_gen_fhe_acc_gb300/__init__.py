@@ -26,6 +26,7 @@ OR, AND, NOR, NAND, XOR, XNOR = range(6)
 GATES = {"OR": OR, "AND": AND, "NOR": NOR, "NAND": NAND, "XOR": XOR, "XNOR": XNOR}
 FLAG_FPGA_COMPAT = 1
 FLAG_PROFILE = 2
+FLAG_FPGA_X1 = 4
 NOALLOC_MAX_GATES = 64
 OPT_BR_REGS_FOR_3 = 1
 OPT_BR_CTAS_PER_SM = 2
@@ -33,7 +34,10 @@ OPT_BR_GROUP = 3
 OPT_BR_WINDOW = 4
 OPT_BR_PIPES = 5
 OPT_BR_POOL = 6
+OPT_DEBUG_WAIT_LIMIT = 7
+OPT_KS_TILED = 8
 GRAPH_CONCURRENT = 1
+STATUS_WAIT_LIMIT = 1
 KIND_LWE_SK, KIND_RLWE_SK, KIND_BOOTSTRAP_KEY, KIND_LWE_KS_KEY, KIND_SUBS_KEY, KIND_LWE_CT, KIND_RLWE_CT, \
     KIND_RGSW_CT = range(1, 9)
 
@@ -394,33 +398,39 @@ class Context:
         """RLWE::eval_bootstrap (RLWE.cpp:726) of one gate."""
         return self.eval_bootstrap_batch(c1, c2, [gate], flags)[0]
 
-    def _fixed(self, width, c1, c2, gates):
-        # fpga_eval_bootstrap_x* check the batch size (myfpga.cpp:1140-1144)
+    def _fixed(self, width, c1, c2, gates, flags):
+        # fpga_eval_bootstrap_x* check the batch size of c1 and c2
+        # (myfpga.cpp:1140-1144; x16 takes exactly 10, myfpga.cpp:1540-1544)
         if len(c1) != width or len(c2) != width or len(gates) != width:
             return None, -1
         try:
-            return list(self.eval_bootstrap_batch(np.array(c1), np.array(c2), gates)), 0
+            return list(self.eval_bootstrap_batch(np.array(c1), np.array(c2), gates, flags)), 0
         except FheaccError as e:
             return None, e.code
 
-    def gpu_eval_bootstrap_x1(self, c1, c2, gate):
+    # The fixed-width calls give the CPU path's results (flags 0, the
+    # bit-exact target) unless the caller asks for an FPGA issue order:
+    # FLAG_FPGA_X1 for x1's (myfpga.cpp:1037-1046), FLAG_FPGA_COMPAT for
+    # x4..x16's (myfpga.cpp:1200-1210).
+    def gpu_eval_bootstrap_x1(self, c1, c2, gate, flags=0):
         """Counterpart of fpga_eval_bootstrap_x1 (myfpga.h:287): (result, rc)."""
         try:
-            return self.eval_bootstrap(c1, c2, gate), 0
+            return self.eval_bootstrap(c1, c2, gate, flags), 0
         except FheaccError as e:
             return None, e.code
 
-    def gpu_eval_bootstrap_x4(self, c1, c2, gates):
-        return self._fixed(4, c1, c2, gates)
+    def gpu_eval_bootstrap_x4(self, c1, c2, gates, flags=0):
+        return self._fixed(4, c1, c2, gates, flags)
 
-    def gpu_eval_bootstrap_x8(self, c1, c2, gates):
-        return self._fixed(8, c1, c2, gates)
+    def gpu_eval_bootstrap_x8(self, c1, c2, gates, flags=0):
+        return self._fixed(8, c1, c2, gates, flags)
 
-    def gpu_eval_bootstrap_x12(self, c1, c2, gates):
-        return self._fixed(12, c1, c2, gates)
+    def gpu_eval_bootstrap_x12(self, c1, c2, gates, flags=0):
+        return self._fixed(12, c1, c2, gates, flags)
 
-    def gpu_eval_bootstrap_x16(self, c1, c2, gates):
-        return self._fixed(16, c1, c2, gates)
+    def gpu_eval_bootstrap_x16(self, c1, c2, gates, flags=0):
+        """fpga_eval_bootstrap_x16 takes exactly 10 gates (myfpga.cpp:1540-1544)."""
+        return self._fixed(10, c1, c2, gates, flags)
 
     # device-pointer entry points (ints are raw device addresses, e.g.
     # torch.Tensor.data_ptr(); stream is a raw cudaStream_t or 0)

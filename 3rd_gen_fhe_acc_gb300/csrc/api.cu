@@ -64,7 +64,7 @@ int prepare_window(Context &c, int steps, cudaStream_t st, dev::StepWindow &w)
     w.buckets = buckets;
     // a bucket of the slowest CTAs takes well under a millisecond (32-bit) or a
     // few milliseconds (64-bit); CTAs stop waiting after about 10 / 40 ms
-    w.spin_limit = c.wide ? 160000u : 40000u;
+    w.spin_limit = c.tune.debug_wait_limit >= 0 ? (unsigned)c.tune.debug_wait_limit : c.wide ? 160000u : 40000u;
     return FHEACC_OK;
 }
 
@@ -86,7 +86,8 @@ int bootstrap_device_with(Context &c, const uint64_t *d_c1, const uint64_t *d_c2
     int rc = launch_blind_rotate32_with(c, d_c1, d_c2, d_gates, count, flags, (uint32_t *)accs, (uint32_t *)extract,
                                         st);
     // the accumulators are free once the blind rotation is done
-    return rc ? rc : launch_lwe_keyswitch32(c, (const uint32_t *)extract, count, true, d_out, st, (uint64_t *)accs);
+    return rc ? rc : launch_lwe_keyswitch32(c, (const uint32_t *)extract, count, true, d_out, st, accs,
+                                            bootstrap_accs_bytes(c, count));
 }
 
 int bootstrap_device(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,
@@ -118,7 +119,7 @@ int bootstrap_device(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, con
     if (rc) return rc;
     if (prof) cudaEventRecord(c.prof[1], st);
     // the accumulator scratch is free once the blind rotation is done
-    rc = launch_lwe_keyswitch32(c, ext, count, true, d_out, st, (uint64_t *)c.accs.ptr);
+    rc = launch_lwe_keyswitch32(c, ext, count, true, d_out, st, c.accs.ptr, c.accs.bytes);
     if (prof && rc == FHEACC_OK) cudaEventRecord(c.prof[2], st);
     return rc;
 }
@@ -751,6 +752,13 @@ int fheacc_set_option(fheacc_ctx *ctx, int option, int value)
         return FHEACC_OK;
     case FHEACC_OPT_BR_POOL:
         c.tune.br_pool = value < 0 ? -1 : value ? 1 : 0;
+        return FHEACC_OK;
+    case FHEACC_OPT_KS_TILED:
+        c.tune.ks_tiled = value < 0 ? -1 : value ? 1 : 0;
+        return FHEACC_OK;
+    case FHEACC_OPT_DEBUG_WAIT_LIMIT:
+        if (value < -1) return c.fail(FHEACC_EINVAL, "wait limit must be -1 (built-in) or >= 0");
+        c.tune.debug_wait_limit = value;
         return FHEACC_OK;
 
     default:

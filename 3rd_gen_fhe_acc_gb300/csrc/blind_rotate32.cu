@@ -84,6 +84,7 @@ struct PipeArgs {
     uint64_t gate_constant[8];
     unsigned long long *claim_next;   // next unclaimed ciphertext (zeroed before the launch)
     unsigned *status;                 // set to kStatusWaitLimit if a pipeline gave up waiting
+    int idle_limit;                   // idle periods before such a wait gives up (kIdleLimit)
 };
 
 // Periods a pipeline idles with a claimed item whose ciphertext's previous step
@@ -153,7 +154,7 @@ __device__ __forceinline__ void store_btile(uint32_t *dst, const uint32_t (&x)[3
 // none) and the step its ciphertext must have finished; [11] periods idled in
 // a row waiting for it. done[k]: last finished step of ciphertext k.
 __device__ __noinline__ void pipe_plan(const int *C, int *Nx, volatile int *done, int *cursor, const uint8_t *res,
-                                       int m, int S, bool compat, unsigned *status)
+                                       int m, int S, int mode, unsigned *status, int idle_limit)
 {
     // period t's inverse-NTT item moves to the digit warps
     Nx[2] = C[6] ? C[0] : -1;
@@ -170,10 +171,9 @@ __device__ __noinline__ void pipe_plan(const int *C, int *Nx, volatile int *done
                 break;
             }
             const int st = idx / m, k = idx - st * m;
-            if (compat || res[k * S + st]) {
+            if (step_issued(res + k * S, st, mode)) {
                 int prev = st - 1;
-                if (!compat)
-                    while (prev >= 0 && !res[k * S + prev]) prev--;
+                while (prev >= 0 && !step_issued(res + k * S, prev, mode)) prev--;
                 Nx[8] = st;
                 Nx[9] = k;
                 Nx[10] = prev;
@@ -194,7 +194,7 @@ __device__ __noinline__ void pipe_plan(const int *C, int *Nx, volatile int *done
     // a wait on another pipeline ends within a few periods; one that does not
     // is abandoned (bounded wait) and flagged
     Nx[11] = (!hv && Nx[3] < 0 && Nx[8] >= 0) ? C[11] + 1 : 0;
-    if (Nx[11] > kIdleLimit) {
+    if (Nx[11] > idle_limit) {
         atomicOr(status, kStatusWaitLimit);
         Nx[8] = -1;
         Nx[5] = 1;
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
     PipeSmem<GW> &s = pipes[pl];
     const int S = A.n * (int)A.digitR;
     const size_t rgsw_words = (size_t)DG * 4 * 1024;
-    const bool compat = (A.flags & FHEACC_FLAG_FPGA_COMPAT) != 0;
+    const int mode = issue_mode(A.flags);
 
     // digit tables (ntt_fwd_1024_digit): t1 [BG], t23 [BG], t123 [BG]
     const int BG = A.digit_tables ? 1 << A.bg_bits : 0;
@@ -361,7 +361,7 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
         // ---- NP pipelines over the (step, ciphertext) items of the group. One
         // thread of each plans the pipeline's next period after each period
         // and publishes the plan in shared memory.
-        if (pw == 0 && lane == 0) pipe_plan(s.ctl[1], s.ctl[0], done, &cursor, res, m, S, compat, A.status);
+        if (pw == 0 && lane == 0) pipe_plan(s.ctl[1], s.ctl[0], done, &cursor, res, m, S, mode, A.status, A.idle_limit);
         pipe_barrier(1 + pl, PT);
         for (int t = 0;; t ^= 1) {
             const int *ctl = s.ctl[t];
@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
             // item once its digit NTTs are in shared memory; one thread first
             // plans the next period
             pipe_barrier(1 + pl, PT);
-            if (pw == 0 && lane == 0) pipe_plan(ctl, s.ctl[t ^ 1], done, &cursor, res, m, S, compat, A.status);
+            if (pw == 0 && lane == 0) pipe_plan(ctl, s.ctl[t ^ 1], done, &cursor, res, m, S, mode, A.status, A.idle_limit);
             if (ctl[3] >= 0) {
                 const int gk = ctl[3], gs = ctl[2];
                 const uint32_t rr = res[gk * S + gs];
@@ -497,6 +497,7 @@ static void fill_pipe_params(Context &c, dev::PipeArgs &A, uint32_t flags)
     A.w31 = (uint32_t)((uint64_t)c.nc.fw[3] * c.nc.fw[1] % Q);
     A.derive_last = c.dp.last_digit_from_acc;
     A.status = c.d_status;
+    A.idle_limit = c.tune.debug_wait_limit >= 0 ? c.tune.debug_wait_limit : dev::kIdleLimit;
     A.digit_tables = (1u << c.p.BG_bits) <= (uint32_t)dev::kMaxTableBG;
     for (int i = 0; i < 8; i++) A.gate_constant[i] = c.dp.gate_constant[i];
 }

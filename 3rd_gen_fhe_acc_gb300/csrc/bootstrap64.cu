@@ -287,6 +287,7 @@ struct Br64Args {
     StepWindow win;            // keeps the CTAs within a few steps of each other (window.cuh)
     unsigned long long *claim_next;   // next unclaimed ciphertext (zeroed before the launch)
     unsigned *status;          // set to kStatusWaitLimit if a worker gave up waiting
+    unsigned wait_limit;       // polls before such a wait gives up (kWorkerWaitLimit)
     int digit_tables;          // digit NTTs start from tables (DigitTables64) after the residues
     size_t claim_limit;        // ciphertexts [0, claim_limit) are claimed in groups
     // remainder pool: ciphertexts [pool_first, pool_first + pool_count) that all
@@ -407,13 +408,12 @@ __global__ void __launch_bounds__(kT64) br64_pool_init_kernel(const __grid_const
     __syncthreads();
     if (tid == 0) {
         int l = -1;
-        if (A.flags & FHEACC_FLAG_FPGA_COMPAT) l = S - 1;
-        else
-            for (int x = S - 1; x >= 0; x--)
-                if (res[x]) {
-                    l = x;
-                    break;
-                }
+        const int mode = issue_mode(A.flags);
+        for (int x = S - 1; x >= 0; x--)
+            if (step_issued(res, x, mode)) {
+                l = x;
+                break;
+            }
         last = l;
         A.pool_last[p] = l;
         A.pool_done[p] = -1;
@@ -428,11 +428,11 @@ __global__ void __launch_bounds__(kT64) br64_pool_init_kernel(const __grid_const
 constexpr unsigned kWorkerWaitLimit = 1u << 26;
 
 // Takes the next item of the remainder pool whose step is at most `reach`,
-// skipping items of zero residue (unless compat); false when there is none.
+// skipping the items the issue mode skips (step_issued); false when there is none.
 // prev: the item's ciphertext's last earlier step with a non-zero residue.
 // seen: the CTA's last view of the pool cursor, which only grows, so the
 // cursor is read only when the view leaves an item to take.
-__device__ __forceinline__ bool pool_take(const Br64Args &A, int S, bool compat, unsigned long long reach,
+__device__ __forceinline__ bool pool_take(const Br64Args &A, int S, int mode, unsigned long long reach,
                                           unsigned long long *seen, int &st, int &k, int &prev)
 {
     const unsigned long long R = (unsigned long long)A.pool_count, total = R * (unsigned long long)S;
@@ -451,13 +451,12 @@ __device__ __forceinline__ bool pool_take(const Br64Args &A, int S, bool compat,
         }
         const int s_ = (int)(v / R), k_ = (int)(v - (unsigned long long)s_ * R);
         const uint8_t *pr = A.pool_res + (size_t)k_ * S;
-        if (compat || pr[s_]) {
+        if (step_issued(pr, s_, mode)) {
             atomicMax(seen, v + 1);
             st = s_;
             k = k_;
             prev = st - 1;
-            if (!compat)
-                while (prev >= 0 && !pr[prev]) prev--;
+            while (prev >= 0 && !step_issued(pr, prev, mode)) prev--;
             return true;
         }
         v++;   // an item of zero residue, taken and skipped
@@ -496,7 +495,7 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
     Step64SmemT<true> &s = reinterpret_cast<Step64SmemT<true> *>(smem_raw)[wk];
     const int S = A.n * (int)A.digitR;
     const size_t rgsw_pairs = (size_t)A.DG * 4 * 2048;
-    const bool compat = (A.flags & FHEACC_FLAG_FPGA_COMPAT) != 0;
+    const int mode = issue_mode(A.flags);
     const unsigned target = gridDim.x;   // the window is used with one round of claims
     if (threadIdx.x == 0) {
         wcur = 0;
@@ -535,23 +534,22 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
                 // (of any step once the CTA's own items are all issued)
                 if (A.pool_count) {
                     const int own = *(volatile int *)&cursor;
-                    pool = pool_take(A, S, compat, own < S * m ? (unsigned long long)(own / m) : ~0ull, &pool_seen,
+                    pool = pool_take(A, S, mode, own < S * m ? (unsigned long long)(own / m) : ~0ull, &pool_seen,
                                      st, k, prev);
                 }
                 for (; !pool;) {
                     const int idx = atomicAdd(&cursor, 1);
                     if (idx >= S * m) {
                         // own items all issued: the rest of the pool
-                        if (A.pool_count) pool = pool_take(A, S, compat, ~0ull, &pool_seen, st, k, prev);
+                        if (A.pool_count) pool = pool_take(A, S, mode, ~0ull, &pool_seen, st, k, prev);
                         break;
                     }
                     const int s_ = idx / m, k_ = idx - s_ * m;
-                    if (compat || res[k_ * S + s_]) {
+                    if (step_issued(res + k_ * S, s_, mode)) {
                         st = s_;
                         k = k_;
                         prev = st - 1;
-                        if (!compat)
-                            while (prev >= 0 && !res[k * S + prev]) prev--;
+                        while (prev >= 0 && !step_issued(res + k * S, prev, mode)) prev--;
                         break;
                     }
                 }
@@ -572,7 +570,7 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
                     const volatile int *dk = pool ? A.pool_done + k : done + k;
                     unsigned polls = 0;
                     while (*dk != prev) {
-                        if (++polls > kWorkerWaitLimit) {
+                        if (++polls > A.wait_limit) {
                             atomicOr(A.status, kStatusWaitLimit);
                             st = -1;
                             break;
@@ -921,9 +919,23 @@ static int launch_br64_shape(Context &c, dev::Br64Args A, int max_ctas, cudaStre
     // the window's per-bucket targets assume one round of claims
     int rc = rounds == 1 ? prepare_window(c, (int)steps, st, A.win) : FHEACC_OK;
     if (rc) return rc;
-    kern<<<(unsigned)blocks, W * dev::kT64, smem, st>>>(A, c.d_tw64, c.d_itw64, c.nc64);
+    // CTAs that wait on other CTAs (the remainder pool's done words, the step
+    // window) need the whole grid resident: a cooperative launch, which fails
+    // instead of starting a grid that cannot be co-resident (the grid is sized
+    // from the occupancy calculator, so it fits on an idle GPU)
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(W * dev::kT64);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = (A.pool_count || A.win.count) ? 1 : 0;
+    e = cudaLaunchKernelEx(&cfg, kern, A, (const ulonglong2 *)c.d_tw64, (const ulonglong2 *)c.d_itw64, c.nc64);
     c.launches++;
-    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaGetLastError();
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "br64 launch");
 }
 
@@ -939,6 +951,7 @@ int launch_blind_rotate64_with(Context &c, const uint64_t *d_c1, const uint64_t 
     A.n = c.p.n; A.DG = (int)c.p.digitG; A.q = c.p.q; A.embed = c.dp.embed; A.Br = c.p.Br; A.digitR = c.p.digitR;
     A.bg_bits = c.p.BG_bits; A.flags = flags; A.derive_last = (int)c.dp.last_digit_from_acc;
     A.status = c.d_status;
+    A.wait_limit = c.tune.debug_wait_limit >= 0 ? (unsigned)c.tune.debug_wait_limit : dev::kWorkerWaitLimit;
     for (int i = 0; i < 8; i++) A.gate_constant[i] = c.dp.gate_constant[i];
     // workers per CTA, by default from the gates per SM (one GB300): up to 1
     // one worker per CTA (3 CTAs per SM), beyond that two, whose shared memory

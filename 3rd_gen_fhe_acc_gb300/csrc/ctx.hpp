@@ -43,6 +43,8 @@ struct Tuning {
     int br_window = -1;       // 64-bit path: steps per bucket of the step window (0: off; -1: default)
     int br_pipes = 0;         // 32-bit path: pipelines per CTA, 1..3 (0: by gates per SM)
     int br_pool = -1;         // 64-bit path: remainder gates shared by all CTAs (0: off; -1: on)
+    int debug_wait_limit = -1;   // tests: polls / idle periods before a bounded wait gives up (-1: built-in)
+    int ks_tiled = -1;        // 32-bit LWE key switch: tiled form 1 always (scratch allowing), 0 never, -1 by size
 };
 
 constexpr size_t kPipeSmemBudget = 220 * 1024;   // dynamic shared memory of one blind-rotation CTA
@@ -63,6 +65,23 @@ constexpr unsigned kStatusWaitLimit = FHEACC_STATUS_WAIT_LIMIT;
 // values and Shoup companions, is 18 MB).
 constexpr int kWindowWide = 1;
 constexpr int kWindowCapacity = 4096;   // buckets of the context's counter buffer
+
+#ifdef __CUDACC__
+// Issue rule of a blind-rotation step s of one ciphertext (res: its residues,
+// one per step): the reference CPU order applies the steps of non-zero
+// residue (RLWE.cpp:759); mode 1 (FHEACC_FLAG_FPGA_X1) also the first step
+// (myfpga.cpp:1037-1046); mode 2 (FHEACC_FLAG_FPGA_COMPAT) every step
+// (myfpga.cpp:1200-1210).
+__device__ __forceinline__ bool step_issued(const uint8_t *res, int s, int mode)
+{
+    return mode == 2 || res[s] != 0 || (mode == 1 && s == 0);
+}
+// The issue mode of a call's flags.
+__host__ __device__ __forceinline__ int issue_mode(uint32_t flags)
+{
+    return (flags & FHEACC_FLAG_FPGA_COMPAT) ? 2 : (flags & FHEACC_FLAG_FPGA_X1) ? 1 : 0;
+}
+#endif
 
 // Makes `dev` current for a scope and restores the caller's device.
 struct DeviceGuard {
@@ -178,11 +197,15 @@ int launch_blind_rotate32_indexed(Context &c, const uint64_t *d_c1, const uint64
 int launch_lwe_keyswitch32_indexed(Context &c, const uint32_t *d_extract, size_t count, bool modswitch,
                                    uint64_t *d_out, const uint32_t *d_out_idx, cudaStream_t st);
 // LWE key switch (+ optional modulus switch) from extracted RLWEs
-// (lwe_ks.cu).
-// d_partials (optional, count * ks_row u64 words of free scratch): lets a few
-// ciphertexts' rows be split over many CTAs.
+// (lwe_ks.cu). d_scratch (optional, scratch_bytes of free device memory, 16-byte
+// aligned; the blind rotation's accumulators once it is done) lets a few
+// ciphertexts' rows be split over many CTAs (count * ks_row u64 words of
+// partial sums) and large batches take the tiled form (their digits,
+// N * digitKS bytes per gate).
 int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
-                           cudaStream_t st, uint64_t *d_partials = nullptr);
+                           cudaStream_t st, void *d_scratch = nullptr, size_t scratch_bytes = 0);
+// Batches from this many gates take the tiled key switch.
+constexpr size_t kKsTiledMinGates = 1024;
 int launch_extract_from_ntt32(Context &c, const uint64_t *d_rlwe, size_t count, uint32_t *d_extract,
                               cudaStream_t st);
 int launch_modswitch(Context &c, const uint64_t *d_in, size_t count, uint64_t *d_out, cudaStream_t st);

@@ -7,12 +7,26 @@
 //
 // Input is the extracted RLWE (time-domain a[N] after NTT_a_transpose, and
 // b[0]). For every coefficient i < N and digit j < digitKS the LWE row
-// kskey[d][j][i], d = base-Bks digit j of a[i], is subtracted. One CTA per
-// ciphertext: the digits are computed once into shared memory, then the CTA
-// walks the N * digitKS rows; a row is n+1 consecutive words, read by
-// consecutive threads (coalesced). Sums are kept in 64-bit registers without
-// reduction (N * digitKS * Q < 2^64) and reduced once at the end; the modulus
-// switch is fused into the same epilogue.
+// kskey[d][j][i], d = base-Bks digit j of a[i], is subtracted.
+//
+// Batches of at least two gates per SM take the tiled form
+// (lwe_ks32_tiled_kernel): ks_digits_kernel first writes every gate's digits
+// gate-minor, [(i * digitKS + j)][gate]; then a CTA takes a block of gates and
+// a 128-word slice of the key rows and walks the N * digitKS row groups (the
+// Bks rows of one (i, j)) in order, staging each group's row slices (and the
+// block's digits) in shared memory with cp.async, several groups ahead, while
+// each warp adds the slice its gates select. A row group is then read from L2
+// once per gate block instead of once per gate (4096 gates: 32 blocks, the
+// 315 MB key 32 times instead of 4096), and because every CTA walks the groups
+// in the same order the key streams from HBM about once.
+//
+// Smaller batches: one CTA per ciphertext, the digits computed once into
+// shared memory, then the CTA walks the N * digitKS rows; a row is n+1
+// consecutive words, read by consecutive threads (coalesced). One or two
+// gates per launch split each gate's rows over many CTAs (ks_partial_kernel).
+// Sums are kept in 64-bit registers without reduction (N * digitKS * Q <
+// 2^64) and reduced once at the end; the modulus switch is fused into the
+// same epilogue.
 #include "ctx.hpp"
 #include <algorithm>
 
@@ -154,6 +168,157 @@ __global__ void ks_final_kernel(const __grid_constant__ KsArgs A, const unsigned
     }
 }
 
+// ---- tiled form
+
+constexpr int kKsTileWarps = 16;   // warps of a tiled CTA
+constexpr int kKsTileCols = 128;   // key-row words per CTA (4 per lane)
+constexpr int kKsTileStages = 4;   // row groups in flight (cp.async ring)
+
+struct KsTiledArgs {
+    KsArgs k;
+    const uint8_t *digits;   // [(i * digitKS + j)][gstride]: digit j of a[i] of each gate
+    size_t gstride;          // gates per digit row (a multiple of the gate block, padded with zeros)
+    int slices;              // column slices of kKsTileCols words
+};
+
+// digits[(i * D + j) * gstride + g] = (a_i / Bks^j) mod Bks of gate g (0 for
+// gates >= count). A CTA of 32 x 8 threads handles 32 gates x 32
+// coefficients: the extracted words are read row-wise (coalesced), transposed
+// in shared memory, and each digit row is written 32 gates at a time.
+__global__ void __launch_bounds__(256) ks_digits_kernel(const uint32_t *__restrict__ ext, size_t count,
+                                                        uint8_t *__restrict__ digits, size_t gstride, int D,
+                                                        uint32_t Bks)
+{
+    __shared__ uint32_t tile[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const size_t g0 = (size_t)blockIdx.x * 32;
+    const int i0 = blockIdx.y * 32;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const size_t g = g0 + ty + 8 * r;
+        tile[ty + 8 * r][tx] = g < count ? ext[g * kExtractStride + i0 + tx] : 0u;
+    }
+    __syncthreads();
+    if (g0 + tx >= gstride) return;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const int ci = ty + 8 * r;
+        uint32_t a = tile[tx][ci];
+        uint8_t *dst = digits + (size_t)(i0 + ci) * D * gstride + g0 + tx;
+        for (int j = 0; j < D; j++) {
+            dst[(size_t)j * gstride] = (uint8_t)(a % Bks);
+            a /= Bks;
+        }
+    }
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory"); }
+
+// CTA (gate block b, column slice s): gates [b G, b G + G), G = 16 GW, key
+// words [s 128, s 128 + 128). Stage t of the ring holds row group t's Bks row
+// slices ([Bks][128] words) and the block's G digits of that group. Warp w
+// owns gates w GW .. w GW + GW - 1 and lane l the words 4 l .. 4 l + 3 of the
+// slice: per row group it adds, for each of its gates, the row slice the
+// gate's digit selects (one 128-bit shared load; all lanes read one row, so a
+// warp's load is 512 contiguous bytes). Sums stay below 32 Q < 2^32 with a
+// conditional subtraction of 16 Q every 16 row groups (rows are canonical,
+// Q < 2^27).
+template <int GW>
+__global__ void __launch_bounds__(kKsTileWarps * 32, 1) lwe_ks32_tiled_kernel(const __grid_constant__ KsTiledArgs T)
+{
+    extern __shared__ __align__(16) uint32_t ring[];
+    constexpr int G = kKsTileWarps * GW;
+    const KsArgs &A = T.k;
+    const int N = A.N, D = A.digitKS, Bks = (int)A.Bks, n = A.n;
+    const int rows_words = Bks * kKsTileCols;           // row slices of one stage
+    const int stage_words = rows_words + G / 4;         // then the digits
+    const int rows_chunks = rows_words / 4, chunks = stage_words / 4;
+    const int slice = blockIdx.x % T.slices;
+    const size_t gb = blockIdx.x / T.slices;
+    const size_t g0 = gb * G;
+    const int c0 = slice * kKsTileCols;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t Q = (uint32_t)A.Q, Q16 = 16 * Q;
+    const int total = N * D;
+    const size_t row_stride = (size_t)D * N * A.ks_row;   // words between digits d and d + 1
+
+    auto issue = [&](int rg) {
+        uint32_t *dst = ring + (rg % kKsTileStages) * stage_words;
+        const int i = rg / D, j = rg - i * D;
+        const uint32_t *rows = A.kskey + ((size_t)j * N + i) * A.ks_row + c0;
+        for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
+            if (c < rows_chunks) {
+                const int d = c >> 5, part = c & 31;
+                cp_async16(dst + 4 * c, rows + d * row_stride + 4 * part);
+            } else {
+                const int part = c - rows_chunks;
+                cp_async16(dst + 4 * c, T.digits + (size_t)rg * T.gstride + g0 + 16 * part);
+            }
+        }
+    };
+
+#pragma unroll
+    for (int s = 0; s < kKsTileStages - 1; s++) {
+        if (s < total) issue(s);
+        cp_async_commit();
+    }
+    uint32_t acc[GW][4];
+#pragma unroll
+    for (int k = 0; k < GW; k++) acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = 0;
+
+    for (int rg = 0; rg < total; rg++) {
+        cp_async_wait<kKsTileStages - 2>();
+        __syncthreads();
+        // the stage read in the previous iteration is free: fetch ahead into it
+        if (rg + kKsTileStages - 1 < total) issue(rg + kKsTileStages - 1);
+        cp_async_commit();
+        const uint32_t *st = ring + (rg % kKsTileStages) * stage_words;
+        const uint8_t *dg = reinterpret_cast<const uint8_t *>(st + rows_words) + warp * GW;
+        const uint4 *rows4 = reinterpret_cast<const uint4 *>(st);
+#pragma unroll
+        for (int k = 0; k < GW; k++) {
+            const uint4 v = rows4[(int)dg[k] * (kKsTileCols / 4) + lane];
+            acc[k][0] += v.x;
+            acc[k][1] += v.y;
+            acc[k][2] += v.z;
+            acc[k][3] += v.w;
+        }
+        if ((rg & 15) == 15) {
+#pragma unroll
+            for (int k = 0; k < GW; k++)
+#pragma unroll
+                for (int e = 0; e < 4; e++) acc[k][e] = min(acc[k][e], acc[k][e] - Q16);
+        }
+    }
+    cp_async_wait<0>();
+
+    const uint32_t Q8 = Q / 8 + 1;
+#pragma unroll
+    for (int k = 0; k < GW; k++) {
+        const size_t g = g0 + warp * GW + k;
+        if (g >= A.count) continue;
+        const uint32_t b0 = A.ext[g * kExtractStride + N];
+        uint64_t *out = A.out + (A.out_idx ? (size_t)A.out_idx[g] : g) * (size_t)(n + 1);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            const int col = c0 + 4 * lane + e;
+            if (col > n) continue;
+            const uint32_t s = acc[k][e] % Q;
+            uint64_t v;
+            if (col < n) v = s ? Q - s : 0;
+            else v = ((uint64_t)(b0 + Q8) % Q + Q - s) % Q;
+            out[col] = A.modswitch ? scale_round_dev(v, A.q, A.Q) : v;
+        }
+    }
+}
+
 __global__ void modswitch_kernel(const uint64_t *__restrict__ in, uint64_t *__restrict__ out, size_t words,
                                  uint64_t q, uint64_t Q)
 {
@@ -163,19 +328,91 @@ __global__ void modswitch_kernel(const uint64_t *__restrict__ in, uint64_t *__re
 
 }  // namespace dev
 
+template <int GW>
+static int launch_ks_tiled_gw(Context &c, const dev::KsTiledArgs &T, size_t blocks, size_t smem, cudaStream_t st)
+{
+    auto kern = dev::lwe_ks32_tiled_kernel<GW>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return c.cuda_fail(e, "tiled key switch smem attribute");
+    kern<<<(unsigned)blocks, dev::kKsTileWarps * 32, smem, st>>>(T);
+    c.launches++;
+    e = cudaGetLastError();
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "tiled key switch launch");
+}
+
+// Gates per warp of the tiled form: gate blocks of 16 GW gates, so that the
+// blocks times the column slices about fill the SMs.
+static int ks_tiled_gw(size_t count, int sms, int slices)
+{
+    const size_t blocks_target = std::max<size_t>(1, (size_t)sms / slices);
+    const size_t G = (count + blocks_target - 1) / blocks_target;
+    return (int)std::min<size_t>(8, std::max<size_t>(1, (G + dev::kKsTileWarps - 1) / dev::kKsTileWarps));
+}
+
+// Scratch bytes the tiled key switch of `count` gates needs for its digits.
+static size_t ks_tiled_digit_bytes(const Context &c, size_t count, int sms)
+{
+    const int slices = (int)(c.dp.ks_row / dev::kKsTileCols);
+    const size_t G = (size_t)dev::kKsTileWarps * ks_tiled_gw(count, sms, std::max(slices, 1));
+    return (count + G - 1) / G * G * (size_t)c.p.N * c.p.digitKS;
+}
+
+static bool ks_tiled_applies(const Context &c, size_t count, int sms, size_t scratch_bytes)
+{
+    if (c.tune.ks_tiled == 0) return false;
+    if (c.dp.ks_row % dev::kKsTileCols != 0 || c.p.N % 32 != 0 || c.p.Bks > 255) return false;
+    if (ks_tiled_digit_bytes(c, count, sms) > scratch_bytes) return false;
+    if (c.tune.ks_tiled > 0) return true;
+    return count >= kKsTiledMinGates;
+}
+
+static int launch_ks_tiled(Context &c, const dev::KsArgs &A, void *scratch, int sms, cudaStream_t st)
+{
+    const int slices = (int)(c.dp.ks_row / dev::kKsTileCols);
+    const int GW = ks_tiled_gw(A.count, sms, slices);
+    const size_t G = (size_t)dev::kKsTileWarps * GW;
+    dev::KsTiledArgs T{};
+    T.k = A;
+    T.digits = (const uint8_t *)scratch;
+    T.gstride = (A.count + G - 1) / G * G;
+    T.slices = slices;
+    dim3 dgrid((unsigned)((T.gstride + 31) / 32), (unsigned)(c.p.N / 32));
+    dev::ks_digits_kernel<<<dgrid, 256, 0, st>>>(A.ext, A.count, (uint8_t *)scratch, T.gstride, A.digitKS, A.Bks);
+    c.launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return c.cuda_fail(e, "key-switch digits launch");
+    const size_t blocks = T.gstride / G * slices;
+    const size_t smem = (size_t)dev::kKsTileStages * ((size_t)c.p.Bks * dev::kKsTileCols + G / 4) * sizeof(uint32_t);
+    switch (GW) {
+    case 1: return launch_ks_tiled_gw<1>(c, T, blocks, smem, st);
+    case 2: return launch_ks_tiled_gw<2>(c, T, blocks, smem, st);
+    case 3: return launch_ks_tiled_gw<3>(c, T, blocks, smem, st);
+    case 4: return launch_ks_tiled_gw<4>(c, T, blocks, smem, st);
+    case 5: return launch_ks_tiled_gw<5>(c, T, blocks, smem, st);
+    case 6: return launch_ks_tiled_gw<6>(c, T, blocks, smem, st);
+    case 7: return launch_ks_tiled_gw<7>(c, T, blocks, smem, st);
+    default: return launch_ks_tiled_gw<8>(c, T, blocks, smem, st);
+    }
+}
+
 int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
-                           cudaStream_t st, uint64_t *d_partials)
+                           cudaStream_t st, void *d_scratch, size_t scratch_bytes)
 {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
-    // a few ciphertexts: split each one's rows over many CTAs
-    if (!d_partials || count == 0 || count >= 2 * (size_t)std::max(sms, 1) || !c.d_kskey ||
-        c.p.n + 1 > 4 * kKsMaxThreads)
-        return launch_lwe_keyswitch32_indexed(c, d_extract, count, modswitch, d_out, nullptr, st);
+    sms = std::max(sms, 1);
+    if (!count) return FHEACC_OK;
+    if (!c.d_kskey) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
+    if (c.p.n + 1 > 4 * kKsMaxThreads) return c.fail(FHEACC_EINVAL, "n too large for key switch");
     dev::KsArgs A{};
     A.ext = d_extract; A.count = count; A.kskey = c.d_kskey; A.out = d_out; A.out_idx = nullptr;
     A.n = c.p.n; A.N = c.p.N; A.digitKS = (int)c.p.digitKS; A.Bks = c.p.Bks; A.ks_row = c.dp.ks_row;
     A.q = c.p.q; A.modswitch = modswitch ? 1u : 0u; A.Q = c.p.Q;
+    if (d_scratch && ks_tiled_applies(c, count, sms, scratch_bytes)) return launch_ks_tiled(c, A, d_scratch, sms, st);
+    // a few ciphertexts: split each one's rows over many CTAs
+    if (!d_scratch || count >= 2 * (size_t)sms || count * c.dp.ks_row * sizeof(uint64_t) > scratch_bytes)
+        return launch_lwe_keyswitch32_indexed(c, d_extract, count, modswitch, d_out, nullptr, st);
+    uint64_t *d_partials = (uint64_t *)d_scratch;
     const int rows = c.p.N * (int)c.p.digitKS;
     // about 8 CTAs per SM, at least 48 rows each
     const int slices = (int)std::max<size_t>(1, std::min<size_t>((size_t)rows / 48, (size_t)sms * 8 / count));

@@ -94,7 +94,9 @@ extern "C" int fheacc_bootstrap_noalloc(fheacc_ctx *ctx, const uint64_t *d_c1, c
         if (prof) cudaEventRecord(c.prof[0], st);
         rc = launch_blind_rotate32_with(c, d_c1, d_c2, d_gates, count, flags, accs, ext, st);
         if (rc == FHEACC_OK && prof) cudaEventRecord(c.prof[1], st);
-        if (rc == FHEACC_OK) rc = launch_lwe_keyswitch32(c, ext, count, true, d_out, st, (uint64_t *)accs);
+        if (rc == FHEACC_OK)
+            rc = launch_lwe_keyswitch32(c, ext, count, true, d_out, st, accs,
+                                        (size_t)FHEACC_NOALLOC_MAX_GATES * 2048 * sizeof(uint32_t));
         if (rc == FHEACC_OK && prof) cudaEventRecord(c.prof[2], st);
         if (rc == FHEACC_OK) {
             cudaError_t e = cudaEventRecord(c.done, st);

@@ -44,6 +44,15 @@ extern "C" {
 #define FHEACC_FLAG_PROFILE     2u  /* record CUDA events around each kernel of
                                        the call, on the launching stream;
                                        read them with fheacc_kernel_times */
+#define FHEACC_FLAG_FPGA_X1     4u  /* the issue order of fpga_eval_bootstrap_x1
+                                       (myfpga.cpp:1031-1063): the first step
+                                       (i = 0, j = 0) is always applied, with
+                                       its residue's key even when the residue
+                                       is 0 (BOOTSTRAP_INIT carries the key
+                                       address), every later step only with a
+                                       non-zero residue. FHEACC_FLAG_FPGA_COMPAT,
+                                       which applies every step, takes
+                                       precedence. */
 
 enum fheacc_gate { FHEACC_OR = 0, FHEACC_AND, FHEACC_NOR, FHEACC_NAND, FHEACC_XOR, FHEACC_XNOR };
 
@@ -241,13 +250,34 @@ int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t cou
  *                             CTAs share the remainder step by step; 0 = off
  *                             (some CTAs take one ciphertext more), -1
  *                             (default) = on
- * Results never depend on the options. */
+ *  FHEACC_OPT_KS_TILED      : 32-bit LWE key switch of a batched bootstrap:
+ *                             1 = the tiled form (gate blocks sharing each
+ *                             key row group through shared memory) for any
+ *                             batch, 0 = one CTA per gate, -1 (default) =
+ *                             tiled from 1024 gates
+ *  FHEACC_OPT_DEBUG_WAIT_LIMIT: for tests of the error path only. The
+ *                             number of polls (64-bit workers, the step
+ *                             window) or idle periods (32-bit pipelines) a
+ *                             bounded wait may take before it gives up;
+ *                             -1 (default) = the built-in limits. With a
+ *                             small value the waits between the workers of a
+ *                             CTA expire: the kernel still returns, the
+ *                             launch's results are invalid,
+ *                             FHEACC_STATUS_WAIT_LIMIT is set and
+ *                             fheacc_sync / fheacc_bootstrap return
+ *                             FHEACC_EIO. Set it back to -1 afterwards.
+ * Results never depend on the other options. The 64-bit blind rotation is a
+ * cooperative launch whenever its CTAs wait on each other (the remainder
+ * pool, the step window), so a grid that cannot be co-resident fails to
+ * launch rather than waiting. */
 #define FHEACC_OPT_BR_REGS_FOR_3  1
 #define FHEACC_OPT_BR_CTAS_PER_SM 2
 #define FHEACC_OPT_BR_GROUP       3
 #define FHEACC_OPT_BR_WINDOW      4
 #define FHEACC_OPT_BR_PIPES       5
 #define FHEACC_OPT_BR_POOL        6
+#define FHEACC_OPT_DEBUG_WAIT_LIMIT 7
+#define FHEACC_OPT_KS_TILED       8
 int fheacc_set_option(fheacc_ctx *ctx, int option, int value);
 
 /* Per-kernel device times (ms) of the most recent call made with

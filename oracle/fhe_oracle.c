@@ -327,7 +327,11 @@ int ora_blind_rotate(const ora_params *p, const uint64_t *c1, const uint64_t *c2
         uint64_t nega = (q - c[i]) % q;
         for (uint64_t j = 0; j < p->digitR; j++) {
             uint64_t residu = nega % p->Br;
-            if (residu > 0 || fpga_compat) {
+            /* issue order: 0 the CPU path's (residue 0 skipped, RLWE.cpp:759);
+             * 1 fpga_eval_bootstrap_x4..x16 (every step, myfpga.cpp:1200-1210);
+             * 2 fpga_eval_bootstrap_x1 (step (0, 0) always, as BOOTSTRAP_INIT,
+             * residue 0 skipped elsewhere, myfpga.cpp:1037-1046) */
+            if (residu > 0 || fpga_compat == 1 || (fpga_compat == 2 && i == 0 && j == 0)) {
                 const uint64_t *key = btkey + ((residu * p->digitR + j) * (uint64_t)n + (uint64_t)i) * rw;
                 ora_rlwe_mult_rgsw(p, acc_out, key, tmp);
                 memcpy(acc_out, tmp, 2 * (size_t)N * sizeof(uint64_t));

@@ -95,9 +95,11 @@ void ora_lwe_evaluate(const ora_params *p, const uint64_t *c1, const uint64_t *c
 /* LWE_eval_NOT (LWE.cpp:224-231). */
 void ora_lwe_eval_not(const ora_params *p, const uint64_t *c, uint64_t *out);
 /* Blind rotation part of eval_bootstrap (RLWE.cpp:733-767): the NTT-domain
- * accumulator after all steps. fpga_compat != 0 also applies the residue-0
- * keys, as fpga_eval_bootstrap_x4..x16 do (myfpga.cpp:1200-1210). Returns
- * the number of RLWE x RGSW steps applied. */
+ * accumulator after all steps. fpga_compat = 1 also applies the residue-0
+ * keys, as fpga_eval_bootstrap_x4..x16 do (myfpga.cpp:1200-1210); 2 applies
+ * the first step (i = 0, j = 0) whatever its residue and skips residue 0
+ * elsewhere, the issue order of fpga_eval_bootstrap_x1 (myfpga.cpp:1037-1046).
+ * Returns the number of RLWE x RGSW steps applied. */
 int  ora_blind_rotate(const ora_params *p, const uint64_t *c1, const uint64_t *c2, int gate,
                       const uint64_t *btkey, int fpga_compat, uint64_t *acc_out);
 /* LWE_keyswitch (LWE.cpp:233-253): RLWE (NTT) -> LWE mod Q. */

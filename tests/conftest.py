@@ -29,9 +29,14 @@ def F():
 
 
 class KeySet:
-    def __init__(self, F, preset):
+    def __init__(self, F, preset, n=None):
+        """The shared key set of a preset; n: a reduced LWE dimension (the
+        per-step work is unchanged, key generation and the oracle are quick)."""
         self.P = F.params_preset(preset)
         P = self.P
+        if n is not None:
+            P.n = n
+            F.derive(P)
         self.lwe_sk = F.LWE_secretkey(P, SEEDS["lwe_sk"])
         self.rlwe_sk = F.RLWE_secretkey(P, SEEDS["rlwe_sk"])
         self.btkey = F.bootstrap_key(P, SEEDS["btkey"], self.lwe_sk, self.rlwe_sk)
@@ -100,3 +105,28 @@ def random_gate_batch(ks, count, seed, gates=None):
     g = rng.integers(0, 6, count).astype(np.int32) if gates is None else np.asarray(gates, dtype=np.int32)
     c = ks.encrypt(np.concatenate([x, y]), seed=1000 + seed)
     return x, y, g, c[:count].copy(), c[count:].copy()
+
+
+def first_residue(P, c1, c2, gates):
+    """Residue of the first blind-rotation step (i = 0, j = 0) of each gate:
+    (q - a_0) mod q mod Br, a = LWE_evaluate(c1, c2) (LWE.cpp:203-222)."""
+    q = int(P.q)
+    a1 = c1[:, 0].astype(np.int64)
+    a2 = c2[:, 0].astype(np.int64)
+    x2 = (gates == 4) | (gates == 5)
+    a = np.where(x2, 2 * (a1 - a2), a1 + a2) % q
+    return ((q - a) % q) % int(P.Br)
+
+
+def x1_gate_batch(ks, count, seed):
+    """count gates of which about half have residue 0 at the first step, the
+    case where the issue order of fpga_eval_bootstrap_x1 differs from the
+    CPU path's (it applies that step's key anyway); drawn from a larger pool
+    of random encryptions."""
+    x, y, g, c1, c2 = random_gate_batch(ks, 48 * count, seed)
+    r0 = first_residue(ks.P, c1, c2, g)
+    zero = np.flatnonzero(r0 == 0)[:(count + 1) // 2]
+    other = np.flatnonzero(r0 != 0)[:count - len(zero)]
+    idx = np.sort(np.concatenate([zero, other]))
+    assert len(zero) >= 1 and len(idx) == count
+    return x[idx], y[idx], g[idx], c1[idx].copy(), c2[idx].copy(), r0[idx] == 0

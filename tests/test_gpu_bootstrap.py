@@ -4,7 +4,7 @@ and by decryption (the truth tables of test::bootstrapping, test.cpp:496-625).
 import numpy as np
 import pytest
 
-from conftest import random_gate_batch
+from conftest import random_gate_batch, x1_gate_batch
 
 pytestmark = pytest.mark.gpu
 
@@ -69,6 +69,74 @@ def test_fpga_compat_mode(F, ctx0, keys0, pipes):
     assert np.array_equal(out, want)
     truth = np.array([F.gate_truth(int(a), b, c) for a, b, c in zip(g, x, y)], dtype=np.uint8)
     assert np.array_equal(keys0.decrypt(out), truth)
+
+
+@pytest.mark.parametrize("pipes", [0, 1, 3])
+def test_fpga_x1_mode(F, ctx0, keys0, pipes):
+    """The issue order of fpga_eval_bootstrap_x1 (myfpga.cpp:1037-1046: the
+    first step always, with residue 0's key when its residue is 0) against the
+    oracle run the same way; gates with a non-zero first residue equal the CPU
+    path's words."""
+    x, y, g, c1, c2, zero = x1_gate_batch(keys0, 6, seed=61)
+    ctx0.set_option(F.OPT_BR_PIPES, pipes)
+    try:
+        out = ctx0.eval_bootstrap_batch(c1, c2, g, flags=F.FLAG_FPGA_X1)
+        cpu_order = ctx0.eval_bootstrap_batch(c1, c2, g)
+    finally:
+        ctx0.set_option(F.OPT_BR_PIPES, 0)
+    want, failed = keys0.oracle.eval_bootstrap_batch(c1, c2, g, keys0.btkey, keys0.kskey, fpga_compat=2)
+    assert failed == 0
+    assert np.array_equal(out, want)
+    assert np.array_equal(out[~zero], cpu_order[~zero])
+    truth = np.array([F.gate_truth(int(a), b, c) for a, b, c in zip(g, x, y)], dtype=np.uint8)
+    assert np.array_equal(keys0.decrypt(out), truth)
+
+
+def test_gpu_fixed_width_calls(F, ctx0, keys0):
+    """The fixed-width counterparts of fpga_eval_bootstrap_x4/x8/x12/x16:
+    x16 takes exactly 10 gates (myfpga.cpp:1540-1544), other sizes give
+    rc = -1 and no result."""
+    x, y, g, c1, c2 = random_gate_batch(keys0, 12, seed=71)
+    for width, call in ((4, ctx0.gpu_eval_bootstrap_x4), (8, ctx0.gpu_eval_bootstrap_x8),
+                        (12, ctx0.gpu_eval_bootstrap_x12), (10, ctx0.gpu_eval_bootstrap_x16)):
+        out, rc = call(list(c1[:width]), list(c2[:width]), list(g[:width]))
+        assert rc == 0
+        assert np.array_equal(np.array(out), ctx0.eval_bootstrap_batch(c1[:width], c2[:width], g[:width]))
+        bad, rc = call(list(c1[:width - 1]), list(c2[:width - 1]), list(g[:width - 1]))
+        assert bad is None and rc == -1
+    out, rc = ctx0.gpu_eval_bootstrap_x16(list(c1[:12]), list(c2[:12]), list(g[:12]))
+    assert out is None and rc == -1
+
+
+@pytest.mark.parametrize("count", [40, 333, 1100])
+def test_tiled_keyswitch_equals_per_gate(F, ctx0, keys0, cuda_ok, count):
+    """The tiled LWE key switch (gate blocks sharing each key row group through
+    shared memory; batches from 1024 gates take it by default) against the
+    one-CTA-per-gate kernel on the same blind-rotation outputs: forced on small
+    batches, with a partial last gate block (40, 333: 16 gates per block) and
+    two gates per warp (1100); the first gates also against the oracle."""
+    torch = cuda_ok
+    x, y, g, c1, c2 = random_gate_batch(keys0, count, seed=81 + count)
+    d1 = torch.from_numpy(c1.view(np.int64)).cuda()
+    d2 = torch.from_numpy(c2.view(np.int64)).cuda()
+    dg = torch.from_numpy(g).cuda()
+    tiled, per_gate = torch.zeros_like(d1), torch.zeros_like(d1)
+    try:
+        ctx0.set_option(F.OPT_KS_TILED, 1)
+        ctx0.bootstrap_async(d1.data_ptr(), d2.data_ptr(), dg.data_ptr(), count, tiled.data_ptr())
+        ctx0.sync()
+        ctx0.set_option(F.OPT_KS_TILED, 0)
+        ctx0.bootstrap_async(d1.data_ptr(), d2.data_ptr(), dg.data_ptr(), count, per_gate.data_ptr())
+        ctx0.sync()
+    finally:
+        ctx0.set_option(F.OPT_KS_TILED, -1)
+    assert torch.equal(tiled, per_gate)
+    out = tiled.cpu().numpy().view(np.uint64)
+    truth = np.array([F.gate_truth(int(a), b, c) for a, b, c in zip(g, x, y)], dtype=np.uint8)
+    assert np.array_equal(keys0.decrypt(out), truth)
+    k = 6
+    want, failed = keys0.oracle.eval_bootstrap_batch(c1[:k], c2[:k], g[:k], keys0.btkey, keys0.kskey)
+    assert failed == 0 and np.array_equal(out[:k], want)
 
 
 def test_errors(F, ctx0, keys0):

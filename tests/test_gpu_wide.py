@@ -1,9 +1,12 @@
 """The 64-bit path (N=2048, Q=18014398509404161 < 2^54, BG=2^9 x 6, n=630)
 against the oracle, bit-exact."""
+import os
+import sys
+
 import numpy as np
 import pytest
 
-from conftest import random_gate_batch
+from conftest import random_gate_batch, x1_gate_batch
 
 pytestmark = pytest.mark.gpu
 
@@ -141,6 +144,21 @@ def test_wide_fpga_compat_mode(F, ctx1, keys1, pipes):
     assert np.array_equal(out, want)
 
 
+@pytest.mark.parametrize("pipes", [1, 2])
+def test_wide_fpga_x1_mode(F, ctx1, keys1, pipes):
+    """The issue order of fpga_eval_bootstrap_x1 (myfpga.cpp:1037-1046) on the
+    64-bit path with one and two workers per CTA, against the oracle."""
+    x, y, g, c1, c2, zero = x1_gate_batch(keys1, 4, seed=43)
+    ctx1.set_option(F.OPT_BR_PIPES, pipes)
+    try:
+        out = ctx1.eval_bootstrap_batch(c1, c2, g, flags=F.FLAG_FPGA_X1)
+    finally:
+        ctx1.set_option(F.OPT_BR_PIPES, 0)
+    want, failed = keys1.oracle.eval_bootstrap_batch(c1, c2, g, keys1.btkey, keys1.kskey, fpga_compat=2)
+    assert failed == 0
+    assert np.array_equal(out, want)
+
+
 @pytest.mark.parametrize("count", [20, 60])
 def test_wide_rlwe_mult_rgsw_batch(F, ctx1, keys1, cuda_ok, count):
     """One RGSW per product. 20 products (120 product-digit CTAs, at most two
@@ -221,3 +239,44 @@ def test_wide_remainder_pool_full_grid(F, ctx1, keys1, cuda_ok):
     assert np.array_equal(accs[0], accs[1])
     want_acc, steps = keys1.oracle.blind_rotate(c1[count - 1], c2[count - 1], int(g[count - 1]), keys1.btkey)
     assert np.array_equal(accs[0][count - 1], want_acc)
+
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_reference_fixture_wide(F, ctx1, keys1, cuda_ok):
+    """The 64-bit GPU path word for word against the reference's own outputs
+    at N = 2048, Q = 18014398509404161 (ref_bootstrap_p1.npz, made by running
+    the reference's RLWE::eval_bootstrap, LWE::LWE_keyswitch and
+    LWE::LWE_modswitch, RLWE.cpp:726-786, LWE.cpp:233-269): the truth tables of
+    all six gates at n = 32, the key switch on random and edge-word RLWEs, the
+    modulus switch on random and edge words, and four gates at n = 630."""
+    torch = cuda_ok
+    sys.path.insert(0, GOLD)
+    from make_ref_fixtures import digest, full_inputs, truth_table_inputs
+    from conftest import KeySet
+    fx = np.load(os.path.join(GOLD, "ref_bootstrap_p1.npz"))
+    small = KeySet(F, 1, n=int(fx["n_small"]))
+    x, y, g, c1, c2 = truth_table_inputs(small)
+    assert digest(c1, c2) == fx["inputs_sha256"].item().decode()
+    with F.Context(small.P, 0) as ctx:
+        ctx.upload_bootstrap_key(small.btkey)
+        ctx.upload_keyswitch_key(small.kskey)
+        out = ctx.eval_bootstrap_batch(c1, c2, g)
+        assert np.array_equal(out, fx["out"].astype(np.uint64))
+        rl = fx["ks_in"]
+        dr = dev(torch, rl)
+        ks = torch.zeros((rl.shape[0], small.P.n + 1), dtype=torch.int64, device="cuda")
+        ctx.lwe_keyswitch_async(dr.data_ptr(), rl.shape[0], ks.data_ptr())
+        ctx.sync()
+        assert np.array_equal(host(ks), fx["ks_out"])
+        lw = fx["ms_in"]
+        dl = dev(torch, lw)
+        ms = torch.zeros_like(dl)
+        ctx.lwe_modswitch_async(dl.data_ptr(), lw.shape[0], ms.data_ptr())
+        ctx.sync()
+        assert np.array_equal(host(ms), fx["ms_out"])
+    fx_, fy, fg, f1, f2 = full_inputs(keys1)
+    assert digest(f1, f2) == fx["full_inputs_sha256"].item().decode()
+    fout = ctx1.eval_bootstrap_batch(f1, f2, fg)
+    assert np.array_equal(fout, fx["full_out"].astype(np.uint64))

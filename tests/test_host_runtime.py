@@ -129,6 +129,38 @@ def test_oracle_equals_reference_outputs(F, keys0):
     assert np.array_equal(keys0.decrypt(out), truth)
 
 
+def test_oracle_equals_reference_outputs_wide(F, keys1):
+    """The 64-bit set (N = 2048, Q < 2^54, BG 2^9 x 6, Bks 25 x 12): the
+    oracle's eval_bootstrap, LWE_keyswitch and LWE_modswitch give exactly the
+    reference's words (ref_bootstrap_p1.npz, tests/golden/make_ref_fixtures.py):
+    the truth tables at n = 32 and four gates at the full n = 630."""
+    import sys
+    sys.path.insert(0, GOLD)
+    from make_ref_fixtures import digest, full_inputs, keys_digest, truth_table_inputs
+    from conftest import KeySet
+    fx = np.load(os.path.join(GOLD, "ref_bootstrap_p1.npz"))
+    small = KeySet(F, 1, n=int(fx["n_small"]))
+    assert keys_digest(small) == fx["keys_sha256"].item().decode()
+    x, y, g, c1, c2 = truth_table_inputs(small)
+    assert digest(c1, c2) == fx["inputs_sha256"].item().decode()
+    out, failed = small.oracle.eval_bootstrap_batch(c1, c2, g, small.btkey, small.kskey)
+    assert failed == 0
+    assert np.array_equal(out, fx["out"].astype(np.uint64))
+    truth = np.array([F.gate_truth(int(a), b, c) for a, b, c in zip(g, x, y)], dtype=np.uint8)
+    assert np.array_equal(small.decrypt(out), truth)
+    ks_out = np.stack([small.oracle.lwe_keyswitch(r, small.kskey) for r in fx["ks_in"]])
+    assert np.array_equal(ks_out, fx["ks_out"])
+    ms_out = np.stack([small.oracle.lwe_modswitch(v) for v in fx["ms_in"]])
+    assert np.array_equal(ms_out, fx["ms_out"])
+    # the full dimension
+    assert keys_digest(keys1) == fx["full_keys_sha256"].item().decode()
+    fx_, fy, fg, f1, f2 = full_inputs(keys1)
+    assert digest(f1, f2) == fx["full_inputs_sha256"].item().decode()
+    fout, failed = keys1.oracle.eval_bootstrap_batch(f1, f2, fg, keys1.btkey, keys1.kskey)
+    assert failed == 0
+    assert np.array_equal(fout, fx["full_out"].astype(np.uint64))
+
+
 def test_wide_preset_oracle_bootstrap(F, keys1):
     """Preset 1 keys from the host generator bootstrap correctly in the oracle
     (N=2048, Q < 2^54, BG 2^9 x 6)."""
