@@ -1,0 +1,98 @@
+// gpu_backend.h -- namespace GPU: the FHE_ACC_runtime's device backend calls
+// with the FPGA backend's exact signatures (FHE_ACC_runtime/include/myfpga.h:
+// 128-404), implemented over the C ABI of libfheacc.so (include/fheacc.h).
+//
+// A maintainer adds gpu_backend.cpp to the runtime in place of myfpga.cpp,
+// includes this header instead of myfpga.h, and calls GPU:: where the code
+// called FPGA::. The slot id becomes a CUDA device index; the PCIe BAR handle
+// and the DMA file descriptors are accepted and ignored. Link with -lfheacc
+// -lcudart (the expand calls stage through device buffers).
+//
+// Results: bit-exact with RLWE::eval_bootstrap (RLWE.cpp:726-786), the CPU
+// path, which skips residue-0 steps. set_issue_flags(FHEACC_FLAG_FPGA_X1) or
+// (FHEACC_FLAG_FPGA_COMPAT) reproduces the FPGA calls' issue orders instead
+// (myfpga.cpp:1037-1046 for x1, 1200-1210 for x4..x16).
+#ifndef FHEACC_GPU_BACKEND_H
+#define FHEACC_GPU_BACKEND_H
+#include <cstdint>
+#include <memory>
+#include <vector>
+
+#include "LWE.h"
+#include "RLWE.h"
+#include "app.h"
+#include "params.h"
+#include "fheacc.h"
+
+// The AWS SDK's handle type (fpga_pci.h); a repeated identical typedef is
+// harmless where the SDK header is also included.
+typedef int pci_bar_handle_t;
+
+namespace GPU {
+
+// Creates the device context of `slot_id` (a CUDA device index) from the
+// runtime's global parameters (params.h). Replaces OCL_config_wr_rd
+// (myfpga.cpp:82-326). 0 on success, -1 on failure.
+int OCL_config_wr_rd(const int slot_id);
+// The twiddle tables are built when the context is created: these return 0
+// (BAR1_ROU_table_{2k,1k}_wr, myfpga.cpp:399-594).
+int BAR1_ROU_table_2k_wr(const int slot_id);
+int BAR1_ROU_table_1k_wr(const int slot_id);
+// Key uploads (dma_write_bootstrap_key, dma_write_subs_key,
+// dma_write_RGSW_enc_sk; myfpga.cpp:596-770). 0 on success, -1 on failure.
+int dma_write_bootstrap_key(const int slot_id, const RLWE::bootstrap_key &bt_key);
+int dma_write_subs_key(const int slot_id, const application::substitute_key &subs_key);
+int dma_write_RGSW_enc_sk(const int slot_id, const RLWE::RGSW_ciphertext &enc_sec);
+
+// Gate bootstrapping (myfpga.cpp:1003-1660). The FPGA runtime key-switches
+// on the host and passes the key each call; here the key switch runs on the
+// device: the key is uploaded at its first use on a slot, and again whenever
+// a different keyswitch_key object is passed. Widths are checked as the
+// FPGA calls check them (x4: 4, x8: 8, x12: 12, x16: exactly 10); a width
+// mismatch or c1 == c2 gives *rc = -1, a failed allocation -ENOMEM.
+LWE::LWE_ciphertext fpga_eval_bootstrap_x1(const LWE::LWE_ciphertext &c1, const LWE::LWE_ciphertext &c2,
+                                           const LWE::keyswitch_key &kskey, const GATES gate,
+                                           const pci_bar_handle_t ocl_bar_handle, int *rc, int read_fd);
+std::vector<LWE::LWE_ciphertext> fpga_eval_bootstrap_x4(const std::vector<LWE::LWE_ciphertext> &c1,
+                                                        const std::vector<LWE::LWE_ciphertext> &c2,
+                                                        const LWE::keyswitch_key &kskey,
+                                                        const std::vector<GATES> gate,
+                                                        const pci_bar_handle_t ocl_bar_handle, int *rc, int read_fd);
+std::vector<LWE::LWE_ciphertext> fpga_eval_bootstrap_x8(const std::vector<LWE::LWE_ciphertext> &c1,
+                                                        const std::vector<LWE::LWE_ciphertext> &c2,
+                                                        const LWE::keyswitch_key &kskey,
+                                                        const std::vector<GATES> gate,
+                                                        const pci_bar_handle_t ocl_bar_handle, int *rc, int read_fd);
+std::vector<LWE::LWE_ciphertext> fpga_eval_bootstrap_x12(const std::vector<LWE::LWE_ciphertext> &c1,
+                                                         const std::vector<LWE::LWE_ciphertext> &c2,
+                                                         const LWE::keyswitch_key &kskey,
+                                                         const std::vector<GATES> gate,
+                                                         const pci_bar_handle_t ocl_bar_handle, int *rc, int read_fd);
+std::vector<LWE::LWE_ciphertext> fpga_eval_bootstrap_x16(const std::vector<LWE::LWE_ciphertext> &c1,
+                                                         const std::vector<LWE::LWE_ciphertext> &c2,
+                                                         const LWE::keyswitch_key &kskey,
+                                                         const std::vector<GATES> gate,
+                                                         const pci_bar_handle_t ocl_bar_handle, int *rc, int read_fd);
+
+// expand_RLWE on the device (myfpga.cpp:1662-1790): N RLWEs, result[i] =
+// RLWE(N b_i X^i) for the input RLWE(sum b_i X^i) in the NTT domain. Needs
+// dma_write_subs_key. NULL and *rc != 0 on failure.
+std::unique_ptr<std::vector<RLWE::RLWE_ciphertext>> fpga_expand_RLWE(const RLWE::RLWE_ciphertext &c1,
+                                                                     const pci_bar_handle_t ocl_bar_handle, int *rc,
+                                                                     int read_fd, int write_fd);
+// homo_expand on the device (myfpga.cpp:2278-2452): digitG packed RLWEs to N
+// RGSWs. Needs dma_write_subs_key and dma_write_RGSW_enc_sk.
+std::shared_ptr<std::vector<RLWE::RGSW_ciphertext>> fpga_homo_expand(
+    const std::unique_ptr<std::vector<RLWE::RLWE_ciphertext>> &packed_bits, const pci_bar_handle_t ocl_bar_handle,
+    int *rc, int read_fd, int write_fd);
+
+// Not in the FPGA API: the issue order of the bootstrap calls (0, the
+// default: the CPU path's; FHEACC_FLAG_FPGA_X1 or FHEACC_FLAG_FPGA_COMPAT),
+// the context of a slot for direct use of the C ABI, and its release.
+void set_issue_flags(uint32_t flags);
+fheacc_ctx *context(const int slot_id);
+int release(const int slot_id);
+
+}  // namespace GPU
+
+#endif
