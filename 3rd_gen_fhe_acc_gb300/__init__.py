@@ -75,7 +75,8 @@ class RequestDone(ctypes.Structure):
 
 class ServerStats(ctypes.Structure):
     _fields_ = [("rounds", ctypes.c_uint64), ("gates", ctypes.c_uint64), ("busy_s", ctypes.c_double),
-                ("waiting", ctypes.c_uint64), ("active", ctypes.c_uint64), ("free_slots", ctypes.c_uint64)]
+                ("waiting", ctypes.c_uint64), ("active", ctypes.c_uint64), ("free_slots", ctypes.c_uint64),
+                ("pool_slots", ctypes.c_uint64), ("lanes", ctypes.c_uint64)]
 
 
 class TuneTrial(ctypes.Structure):
@@ -592,10 +593,11 @@ class Graph:
 # ------------------------------------------------------------------ serving
 class Server:
     """Continuous-batching request loop (fheacc_server_*): requests are gate
-    circuits over LWE ciphertexts; all ready gates of all admitted requests run
-    in one batched launch per round; admission by free pool slots."""
+    circuits over LWE ciphertexts; the ready gates of all admitted requests run
+    in batched launches, up to two rounds in flight; admission by free room in
+    a device pool (pool_ciphertexts=0: sized from the free device memory)."""
 
-    def __init__(self, ctx, max_batch=4096, pool_ciphertexts=1 << 18):
+    def __init__(self, ctx, max_batch=4096, pool_ciphertexts=0):
         h = ctypes.c_void_p()
         ctx.check(lib().fheacc_server_create(ctx.handle, max_batch, pool_ciphertexts, ctypes.byref(h)))
         self._h = h

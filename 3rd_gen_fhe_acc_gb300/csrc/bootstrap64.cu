@@ -273,6 +273,7 @@ __global__ void rlwe_split_sum64_kernel(const uint64_t *__restrict__ partial, ui
 
 struct Br64Args {
     const uint64_t *c1, *c2;
+    const uint32_t *idx1, *idx2;   // optional: gate g reads c1 + idx1[g] * (n+1) (else g)
     const int32_t *gates;
     size_t count;
     const ulonglong2 *btkey;   // [(i*digitR + j)*Br + r][digitG][2][2][2048] Shoup pairs
@@ -311,7 +312,8 @@ __device__ __forceinline__ void br64_residues(const Br64Args &A, size_t gid, uin
     const uint32_t q = A.q, qmask = q - 1;
     const int g = A.gates[gid];
     const bool x2 = (g == 4 || g == 5);
-    const uint64_t *c1 = A.c1 + gid * (size_t)(n + 1), *c2 = A.c2 + gid * (size_t)(n + 1);
+    const uint64_t *c1 = A.c1 + (A.idx1 ? (size_t)A.idx1[gid] : gid) * (size_t)(n + 1);
+    const uint64_t *c2 = A.c2 + (A.idx2 ? (size_t)A.idx2[gid] : gid) * (size_t)(n + 1);
     for (int i = t0; i <= n; i += nt) {
         const uint64_t v = x2 ? 2 * (c1[i] - c2[i]) : c1[i] + c2[i];
         if (i < n) {
@@ -656,6 +658,7 @@ struct Ks64Args {
     size_t count;
     const uint64_t *kskey;   // [(d*digitKS + j)*N + i][ks_row]
     uint64_t *out;
+    const uint32_t *out_idx;   // optional: ciphertext ci is written to out + out_idx[ci] * (n+1)
     int n, N, digitKS;
     uint32_t Bks, ks_row, q, modswitch;
     int fold;   // rows between mod-Q folds of the 64-bit sums, a multiple of 8
@@ -723,7 +726,7 @@ __global__ void __launch_bounds__(512) lwe_ks64_kernel(const __grid_constant__ K
         }
         const uint64_t b0 = ext[N];
         const uint64_t Q8 = Q / 8 + 1;
-        uint64_t *out = A.out + ci * (size_t)(n + 1);
+        uint64_t *out = A.out + (A.out_idx ? (size_t)A.out_idx[ci] : ci) * (size_t)(n + 1);
         const uint64_t sums[2] = {s0, s1};
 #pragma unroll
         for (int c2 = 0; c2 < 2; c2++) {
@@ -916,8 +919,12 @@ static int launch_br64_shape(Context &c, dev::Br64Args A, int max_ctas, cudaStre
         e = cudaGetLastError();
         if (e != cudaSuccess) return c.cuda_fail(e, "br64 pool launch");
     }
-    // the window's per-bucket targets assume one round of claims
-    int rc = rounds == 1 ? prepare_window(c, (int)steps, st, A.win) : FHEACC_OK;
+    // the window's per-bucket targets assume one round of claims, and its
+    // counters are the context's own (A.win.steps < 0: a launch that may run
+    // beside another of the same context takes none)
+    const bool window_ok = A.win.steps >= 0;
+    A.win = dev::StepWindow{};
+    int rc = rounds == 1 && window_ok ? prepare_window(c, (int)steps, st, A.win) : FHEACC_OK;
     if (rc) return rc;
     // CTAs that wait on other CTAs (the remainder pool's done words, the step
     // window) need the whole grid resident: a cooperative launch, which fails
@@ -943,10 +950,20 @@ int launch_blind_rotate64_with(Context &c, const uint64_t *d_c1, const uint64_t 
                                size_t count, uint32_t flags, uint64_t *accs, uint64_t *d_acc_out,
                                uint64_t *d_extract, int max_ctas, cudaStream_t st)
 {
+    return launch_blind_rotate64_indexed(c, d_c1, d_c2, nullptr, nullptr, d_gates, count, flags, accs, d_acc_out,
+                                         d_extract, max_ctas, true, st);
+}
+
+int launch_blind_rotate64_indexed(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const uint32_t *d_idx1,
+                                  const uint32_t *d_idx2, const int32_t *d_gates, size_t count, uint32_t flags,
+                                  uint64_t *accs, uint64_t *d_acc_out, uint64_t *d_extract, int max_ctas,
+                                  bool window, cudaStream_t st)
+{
     if (!count) return FHEACC_OK;
     if (!c.d_btkey64) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
     dev::Br64Args A{};
-    A.c1 = d_c1; A.c2 = d_c2; A.gates = d_gates; A.count = count;
+    A.c1 = d_c1; A.c2 = d_c2; A.idx1 = d_idx1; A.idx2 = d_idx2; A.gates = d_gates; A.count = count;
+    A.win.steps = window ? 0 : -1;
     A.btkey = c.d_btkey64; A.accs = accs; A.acc_out = d_acc_out; A.extract = d_extract;
     A.n = c.p.n; A.DG = (int)c.p.digitG; A.q = c.p.q; A.embed = c.dp.embed; A.Br = c.p.Br; A.digitR = c.p.digitR;
     A.bg_bits = c.p.BG_bits; A.flags = flags; A.derive_last = (int)c.dp.last_digit_from_acc;
@@ -976,13 +993,13 @@ int launch_extract64(Context &c, const uint64_t *d_rlwe, size_t count, uint64_t 
 }
 
 int launch_lwe_keyswitch64(Context &c, const uint64_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
-                           cudaStream_t st)
+                           cudaStream_t st, const uint32_t *d_out_idx)
 {
     if (!count) return FHEACC_OK;
     if (!c.d_kskey64) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
     if (c.dp.ks_row > 1024) return c.fail(FHEACC_EINVAL, "n too large for key switch");
     dev::Ks64Args A{};
-    A.ext = d_extract; A.count = count; A.kskey = c.d_kskey64; A.out = d_out;
+    A.ext = d_extract; A.count = count; A.kskey = c.d_kskey64; A.out = d_out; A.out_idx = d_out_idx;
     A.n = c.p.n; A.N = c.p.N; A.digitKS = (int)c.p.digitKS; A.Bks = c.p.Bks; A.ks_row = c.dp.ks_row;
     A.q = c.p.q; A.modswitch = modswitch ? 1u : 0u; A.Q = c.p.Q;
     // key words are < Q: (fold + 1) Q must stay below 2^64

@@ -203,7 +203,8 @@ int launch_lwe_keyswitch32_indexed(Context &c, const uint32_t *d_extract, size_t
 // partial sums) and large batches take the tiled form (their digits,
 // N * digitKS bytes per gate).
 int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
-                           cudaStream_t st, void *d_scratch = nullptr, size_t scratch_bytes = 0);
+                           cudaStream_t st, void *d_scratch = nullptr, size_t scratch_bytes = 0,
+                           const uint32_t *d_out_idx = nullptr);
 // Batches from this many gates take the tiled key switch.
 constexpr size_t kKsTiledMinGates = 1024;
 int launch_extract_from_ntt32(Context &c, const uint64_t *d_rlwe, size_t count, uint32_t *d_extract,
@@ -229,7 +230,15 @@ int launch_blind_rotate64_with(Context &c, const uint64_t *d_c1, const uint64_t 
                                uint64_t *d_extract, int max_ctas, cudaStream_t st);
 int launch_extract64(Context &c, const uint64_t *d_rlwe, size_t count, uint64_t *d_extract, cudaStream_t st);
 int launch_lwe_keyswitch64(Context &c, const uint64_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
-                           cudaStream_t st);
+                           cudaStream_t st, const uint32_t *d_out_idx = nullptr);
+// The 64-bit blind rotation reading gate g's inputs at c1 + idx1[g] * (n+1)
+// and c2 + idx2[g] * (n+1) (index arrays optional), caller-supplied
+// accumulator scratch (bootstrap_accs_bytes); window = false takes no step
+// window (for launches that may overlap another launch of the context).
+int launch_blind_rotate64_indexed(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, const uint32_t *d_idx1,
+                                  const uint32_t *d_idx2, const int32_t *d_gates, size_t count, uint32_t flags,
+                                  uint64_t *accs, uint64_t *d_acc_out, uint64_t *d_extract, int max_ctas,
+                                  bool window, cudaStream_t st);
 // automorphism / key switch / expand (expand.cu); mode: 0 SUBS, 1 KS,
 // 2 SUBS_KS, 3 EXPAND (one level f, in place on d_out, for `batches` r
 // arrays bstride words apart)

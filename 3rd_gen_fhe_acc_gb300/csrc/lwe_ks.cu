@@ -164,7 +164,7 @@ __global__ void ks_final_kernel(const __grid_constant__ KsArgs A, const unsigned
         uint64_t v;
         if (k < A.n) v = sm ? Q - sm : 0;
         else v = ((uint64_t)(A.ext[ci * kExtractStride + A.N] + Q8) % Q + Q - sm) % Q;
-        A.out[x] = A.modswitch ? scale_round_dev(v, A.q, A.Q) : v;
+        A.out[(A.out_idx ? (size_t)A.out_idx[ci] : ci) * w + k] = A.modswitch ? scale_round_dev(v, A.q, A.Q) : v;
     }
 }
 
@@ -172,7 +172,8 @@ __global__ void ks_final_kernel(const __grid_constant__ KsArgs A, const unsigned
 
 constexpr int kKsTileWarps = 16;   // warps of a tiled CTA
 constexpr int kKsTileCols = 128;   // key-row words per CTA (4 per lane)
-constexpr int kKsTileStages = 4;   // row groups in flight (cp.async ring)
+constexpr int kKsTileStages = 4;   // stages in flight (cp.async ring)
+constexpr int kKsTileGroups = 2;   // row groups per stage (one barrier per stage)
 
 struct KsTiledArgs {
     KsArgs k;
@@ -221,76 +222,149 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int PENDING>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory"); }
 
+// Digits of a warp's GW gates (GW = 1, 2, 4 or 8 bytes, naturally aligned) in
+// one shared-memory load.
+template <int GW>
+__device__ __forceinline__ uint64_t load_digits(const uint8_t *p)
+{
+    if (GW == 8) return *reinterpret_cast<const uint64_t *>(p);
+    if (GW == 4) return *reinterpret_cast<const uint32_t *>(p);
+    if (GW == 2) return *reinterpret_cast<const uint16_t *>(p);
+    return *p;
+}
+
 // CTA (gate block b, column slice s): gates [b G, b G + G), G = 16 GW, key
-// words [s 128, s 128 + 128). Stage t of the ring holds row group t's Bks row
-// slices ([Bks][128] words) and the block's G digits of that group. Warp w
-// owns gates w GW .. w GW + GW - 1 and lane l the words 4 l .. 4 l + 3 of the
-// slice: per row group it adds, for each of its gates, the row slice the
-// gate's digit selects (one 128-bit shared load; all lanes read one row, so a
-// warp's load is 512 contiguous bytes). Sums stay below 32 Q < 2^32 with a
-// conditional subtraction of 16 Q every 16 row groups (rows are canonical,
-// Q < 2^27).
+// words [s 128, s 128 + 128). The row groups are walked kKsTileGroups at a
+// time: a stage of the ring holds that many groups' Bks row slices ([Bks][128]
+// words each) and the block's G digits of each group. Every thread copies the
+// same chunks of every stage, so their offsets are worked out once; only the
+// stage's base addresses move. Warp w owns gates w GW .. w GW + GW - 1 and
+// lane l the words 4 l .. 4 l + 3 of the slice: per row group it reads its
+// gates' digits in one load and adds, for each gate, the row slice the digit
+// selects (one 128-bit shared load; all lanes read one row, so a warp's load
+// is 512 contiguous bytes, free of bank conflicts). Sums stay below 32 Q <
+// 2^32 with a conditional subtraction of 16 Q every 16 row groups (rows are
+// canonical, Q < 2^27).
 template <int GW>
 __global__ void __launch_bounds__(kKsTileWarps * 32, 1) lwe_ks32_tiled_kernel(const __grid_constant__ KsTiledArgs T)
 {
     extern __shared__ __align__(16) uint32_t ring[];
-    constexpr int G = kKsTileWarps * GW;
+    constexpr int G = kKsTileWarps * GW, R = kKsTileGroups;
+    constexpr int kMaxChunks = 4;   // chunks of a stage per thread (checked by the launcher)
     const KsArgs &A = T.k;
     const int N = A.N, D = A.digitKS, Bks = (int)A.Bks, n = A.n;
-    const int rows_words = Bks * kKsTileCols;           // row slices of one stage
-    const int stage_words = rows_words + G / 4;         // then the digits
-    const int rows_chunks = rows_words / 4, chunks = stage_words / 4;
+    const int group_words = Bks * kKsTileCols + G / 4;   // row slices, then digits
+    const int group_chunks = group_words / 4, rows_chunks = Bks * (kKsTileCols / 4);
+    const int stage_words = R * group_words;
     const int slice = blockIdx.x % T.slices;
-    const size_t gb = blockIdx.x / T.slices;
-    const size_t g0 = gb * G;
+    const size_t g0 = (size_t)(blockIdx.x / T.slices) * G;
     const int c0 = slice * kKsTileCols;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t Q = (uint32_t)A.Q, Q16 = 16 * Q;
     const int total = N * D;
     const size_t row_stride = (size_t)D * N * A.ks_row;   // words between digits d and d + 1
 
-    auto issue = [&](int rg) {
-        uint32_t *dst = ring + (rg % kKsTileStages) * stage_words;
-        const int i = rg / D, j = rg - i * D;
-        const uint32_t *rows = A.kskey + ((size_t)j * N + i) * A.ks_row + c0;
-        for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
-            if (c < rows_chunks) {
-                const int d = c >> 5, part = c & 31;
-                cp_async16(dst + 4 * c, rows + d * row_stride + 4 * part);
+    // this thread's chunks: group r of the stage, source offset from that
+    // group's base (rows: kskey row (d, j, i) slice; digits: the block's bytes),
+    // destination word in the stage
+    int ch_group[kMaxChunks], ch_dst[kMaxChunks];
+    size_t ch_off[kMaxChunks];
+    bool ch_digit[kMaxChunks];
+    int nch = 0;
+#pragma unroll
+    for (int u = 0; u < kMaxChunks; u++) {
+        const int c = threadIdx.x + u * (int)blockDim.x;
+        ch_group[u] = -1;
+        ch_off[u] = 0;
+        ch_dst[u] = 0;
+        ch_digit[u] = false;
+        if (c < R * group_chunks) {
+            const int r = c / group_chunks, cc = c - r * group_chunks;
+            ch_group[u] = r;
+            ch_dst[u] = r * group_words + 4 * cc;
+            if (cc < rows_chunks) {
+                ch_off[u] = (size_t)(cc >> 5) * row_stride + 4 * (cc & 31);
             } else {
-                const int part = c - rows_chunks;
-                cp_async16(dst + 4 * c, T.digits + (size_t)rg * T.gstride + g0 + 16 * part);
+                ch_digit[u] = true;
+                ch_off[u] = g0 + 16 * (size_t)(cc - rows_chunks);
+            }
+            nch = u + 1;
+        }
+    }
+    // coefficient and digit of the next group to fetch
+    int fi = 0, fj = 0, fetched = 0;
+    auto issue_stage = [&]() {
+        uint32_t *dst = ring + ((fetched / R) % kKsTileStages) * stage_words;
+        size_t rows_base[R], dig_base[R];
+        bool valid[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            valid[r] = fetched + r < total;
+            rows_base[r] = ((size_t)fj * N + fi) * A.ks_row + c0;
+            dig_base[r] = (size_t)(fetched + r) * T.gstride;
+            if (++fj == D) {
+                fj = 0;
+                ++fi;
             }
         }
+#pragma unroll
+        for (int u = 0; u < kMaxChunks; u++) {
+            if (u < nch) {
+                // the chunk's group (selects, not an indexed local array)
+                size_t rb = rows_base[0], db = dig_base[0];
+                bool v = valid[0];
+#pragma unroll
+                for (int r = 1; r < R; r++)
+                    if (ch_group[u] == r) {
+                        rb = rows_base[r];
+                        db = dig_base[r];
+                        v = valid[r];
+                    }
+                if (v) {
+                    const void *src = ch_digit[u] ? (const void *)(T.digits + db + ch_off[u])
+                                                  : (const void *)(A.kskey + rb + ch_off[u]);
+                    cp_async16(dst + ch_dst[u], src);
+                }
+            }
+        }
+        fetched += R;
     };
 
 #pragma unroll
     for (int s = 0; s < kKsTileStages - 1; s++) {
-        if (s < total) issue(s);
+        if (fetched < total) issue_stage();
         cp_async_commit();
     }
     uint32_t acc[GW][4];
 #pragma unroll
     for (int k = 0; k < GW; k++) acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = 0;
 
-    for (int rg = 0; rg < total; rg++) {
+    for (int rg = 0; rg < total; rg += R) {
         cp_async_wait<kKsTileStages - 2>();
         __syncthreads();
         // the stage read in the previous iteration is free: fetch ahead into it
-        if (rg + kKsTileStages - 1 < total) issue(rg + kKsTileStages - 1);
+        if (fetched < total) issue_stage();
         cp_async_commit();
-        const uint32_t *st = ring + (rg % kKsTileStages) * stage_words;
-        const uint8_t *dg = reinterpret_cast<const uint8_t *>(st + rows_words) + warp * GW;
-        const uint4 *rows4 = reinterpret_cast<const uint4 *>(st);
+        const uint32_t *st = ring + ((rg / R) % kKsTileStages) * stage_words;
 #pragma unroll
-        for (int k = 0; k < GW; k++) {
-            const uint4 v = rows4[(int)dg[k] * (kKsTileCols / 4) + lane];
-            acc[k][0] += v.x;
-            acc[k][1] += v.y;
-            acc[k][2] += v.z;
-            acc[k][3] += v.w;
+        for (int r = 0; r < R; r++) {
+            if (rg + r < total) {
+                const uint32_t *grp = st + r * group_words;
+                const uint64_t dg =
+                    load_digits<GW>(reinterpret_cast<const uint8_t *>(grp + Bks * kKsTileCols) + warp * GW);
+                const uint4 *rows4 = reinterpret_cast<const uint4 *>(grp);
+#pragma unroll
+                for (int k = 0; k < GW; k++) {
+                    const uint32_t d = (uint32_t)(dg >> (8 * k)) & 0xFFu;
+                    const uint4 v = rows4[d * (kKsTileCols / 4) + lane];
+                    acc[k][0] += v.x;
+                    acc[k][1] += v.y;
+                    acc[k][2] += v.z;
+                    acc[k][3] += v.w;
+                }
+            }
         }
-        if ((rg & 15) == 15) {
+        if (((rg / R) & (16 / R - 1)) == 16 / R - 1) {
 #pragma unroll
             for (int k = 0; k < GW; k++)
 #pragma unroll
@@ -340,13 +414,16 @@ static int launch_ks_tiled_gw(Context &c, const dev::KsTiledArgs &T, size_t bloc
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "tiled key switch launch");
 }
 
-// Gates per warp of the tiled form: gate blocks of 16 GW gates, so that the
-// blocks times the column slices about fill the SMs.
+// Gates per warp of the tiled form (1, 2, 4 or 8: a warp's digits are one
+// aligned load): gate blocks of 16 GW gates, the smallest GW with which the
+// blocks times the column slices fit on the SMs.
 static int ks_tiled_gw(size_t count, int sms, int slices)
 {
     const size_t blocks_target = std::max<size_t>(1, (size_t)sms / slices);
-    const size_t G = (count + blocks_target - 1) / blocks_target;
-    return (int)std::min<size_t>(8, std::max<size_t>(1, (G + dev::kKsTileWarps - 1) / dev::kKsTileWarps));
+    const size_t per_warp = ((count + blocks_target - 1) / blocks_target + dev::kKsTileWarps - 1) / dev::kKsTileWarps;
+    int gw = 1;
+    while (gw < 8 && (size_t)gw < per_warp) gw *= 2;
+    return gw;
 }
 
 // Scratch bytes the tiled key switch of `count` gates needs for its digits.
@@ -361,6 +438,9 @@ static bool ks_tiled_applies(const Context &c, size_t count, int sms, size_t scr
 {
     if (c.tune.ks_tiled == 0) return false;
     if (c.dp.ks_row % dev::kKsTileCols != 0 || c.p.N % 32 != 0 || c.p.Bks > 255) return false;
+    // a thread copies at most 4 chunks of a stage
+    if ((size_t)dev::kKsTileGroups * (c.p.Bks * (dev::kKsTileCols / 4) + 8) > 4 * 32 * (size_t)dev::kKsTileWarps)
+        return false;
     if (ks_tiled_digit_bytes(c, count, sms) > scratch_bytes) return false;
     if (c.tune.ks_tiled > 0) return true;
     return count >= kKsTiledMinGates;
@@ -382,21 +462,18 @@ static int launch_ks_tiled(Context &c, const dev::KsArgs &A, void *scratch, int 
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return c.cuda_fail(e, "key-switch digits launch");
     const size_t blocks = T.gstride / G * slices;
-    const size_t smem = (size_t)dev::kKsTileStages * ((size_t)c.p.Bks * dev::kKsTileCols + G / 4) * sizeof(uint32_t);
+    const size_t smem = (size_t)dev::kKsTileStages * dev::kKsTileGroups *
+                        ((size_t)c.p.Bks * dev::kKsTileCols + G / 4) * sizeof(uint32_t);
     switch (GW) {
     case 1: return launch_ks_tiled_gw<1>(c, T, blocks, smem, st);
     case 2: return launch_ks_tiled_gw<2>(c, T, blocks, smem, st);
-    case 3: return launch_ks_tiled_gw<3>(c, T, blocks, smem, st);
     case 4: return launch_ks_tiled_gw<4>(c, T, blocks, smem, st);
-    case 5: return launch_ks_tiled_gw<5>(c, T, blocks, smem, st);
-    case 6: return launch_ks_tiled_gw<6>(c, T, blocks, smem, st);
-    case 7: return launch_ks_tiled_gw<7>(c, T, blocks, smem, st);
     default: return launch_ks_tiled_gw<8>(c, T, blocks, smem, st);
     }
 }
 
 int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
-                           cudaStream_t st, void *d_scratch, size_t scratch_bytes)
+                           cudaStream_t st, void *d_scratch, size_t scratch_bytes, const uint32_t *d_out_idx)
 {
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
@@ -405,13 +482,13 @@ int launch_lwe_keyswitch32(Context &c, const uint32_t *d_extract, size_t count, 
     if (!c.d_kskey) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
     if (c.p.n + 1 > 4 * kKsMaxThreads) return c.fail(FHEACC_EINVAL, "n too large for key switch");
     dev::KsArgs A{};
-    A.ext = d_extract; A.count = count; A.kskey = c.d_kskey; A.out = d_out; A.out_idx = nullptr;
+    A.ext = d_extract; A.count = count; A.kskey = c.d_kskey; A.out = d_out; A.out_idx = d_out_idx;
     A.n = c.p.n; A.N = c.p.N; A.digitKS = (int)c.p.digitKS; A.Bks = c.p.Bks; A.ks_row = c.dp.ks_row;
     A.q = c.p.q; A.modswitch = modswitch ? 1u : 0u; A.Q = c.p.Q;
     if (d_scratch && ks_tiled_applies(c, count, sms, scratch_bytes)) return launch_ks_tiled(c, A, d_scratch, sms, st);
     // a few ciphertexts: split each one's rows over many CTAs
     if (!d_scratch || count >= 2 * (size_t)sms || count * c.dp.ks_row * sizeof(uint64_t) > scratch_bytes)
-        return launch_lwe_keyswitch32_indexed(c, d_extract, count, modswitch, d_out, nullptr, st);
+        return launch_lwe_keyswitch32_indexed(c, d_extract, count, modswitch, d_out, d_out_idx, st);
     uint64_t *d_partials = (uint64_t *)d_scratch;
     const int rows = c.p.N * (int)c.p.digitKS;
     // about 8 CTAs per SM, at least 48 rows each

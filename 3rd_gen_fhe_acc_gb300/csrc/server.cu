@@ -56,17 +56,30 @@ struct Request {
 
 }  // namespace
 
+// One in-flight round: its stream, event, index arrays and kernel scratch.
+struct Lane {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    uint32_t *d_idx = nullptr;          // [4][max_batch]: idx1, idx2, out slot, gate
+    uint32_t *h_idx = nullptr;          // pinned staging
+    void *d_accs = nullptr, *d_ext = nullptr;
+    size_t accs_bytes = 0;
+    std::vector<std::pair<Request *, uint32_t>> batch;
+    bool busy = false;
+    double t0 = 0;
+};
+
+constexpr int kLanes = 2;
+
 struct Server {
     Context *c = nullptr;
     size_t max_batch = 0;
     uint32_t slots = 0;
     size_t W = 0;                       // words per ciphertext (n + 1)
     uint64_t *d_pool = nullptr;
-    uint32_t *d_idx = nullptr;          // [4][max_batch]: idx1, idx2, out slot, gate
-    uint32_t *h_idx = nullptr;          // pinned staging
-    uint32_t *d_accs = nullptr, *d_ext = nullptr;
-    cudaStream_t st = nullptr;
-    cudaEvent_t ev = nullptr;
+    cudaStream_t up = nullptr;          // input uploads and output reads
+    cudaEvent_t ev_up = nullptr;        // after the latest input upload
+    Lane lane[kLanes];
     std::map<uint32_t, uint32_t> free_ranges;   // start -> length
 
     std::mutex mu;
@@ -81,7 +94,8 @@ struct Server {
 
     // statistics
     uint64_t rounds = 0, gates_run = 0;
-    double busy_s = 0;
+    double busy_s = 0, busy_since = 0;  // union of the lanes' busy intervals
+    int lanes_busy = 0;
 
     bool alloc_range(uint32_t need, uint32_t *base)
     {
@@ -132,14 +146,17 @@ struct Server {
         return fresh;
     }
 
+    // Copies the inputs of newly admitted requests into the pool; every
+    // round launched afterwards waits for them (ev_up).
     int upload_inputs(const std::vector<Request *> &fresh)
     {
+        if (fresh.empty()) return FHEACC_OK;
         for (Request *r : fresh) {
             cudaError_t e = cudaMemcpyAsync(d_pool + (size_t)r->base * W, r->inputs.data(),
-                                            r->inputs.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
+                                            r->inputs.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, up);
             if (e != cudaSuccess) return c->cuda_fail(e, "server input copy");
         }
-        return FHEACC_OK;
+        return cudaEventRecord(ev_up, up) == cudaSuccess ? FHEACC_OK : FHEACC_EIO;
     }
 
     bool node_ready(const Request *r, uint32_t node) const
@@ -147,121 +164,191 @@ struct Server {
         return node < r->num_inputs || r->state[node - r->num_inputs] == 2;
     }
 
+    // Ready gates, oldest request first, up to max_batch (caller holds mu).
+    void gather_locked(std::vector<std::pair<Request *, uint32_t>> &batch)
+    {
+        batch.clear();
+        for (Request *r : active) {
+            bool blocked = false;
+            for (uint32_t g = r->next_scan; g < r->num_gates && batch.size() < max_batch; g++) {
+                if (r->state[g] == 0) {
+                    if (node_ready(r, r->in1[g]) && node_ready(r, r->in2[g])) {
+                        r->state[g] = 1;
+                        batch.emplace_back(r, g);
+                    } else {
+                        blocked = true;
+                    }
+                }
+                if (!blocked) r->next_scan = g + 1;   // everything below is issued or done
+            }
+            if (batch.size() >= max_batch) break;
+        }
+    }
+
+    // One batched bootstrap of the lane's gates, reading and writing the pool
+    // through the lane's index arrays.
+    int launch(Lane &L)
+    {
+        const size_t k = L.batch.size();
+        for (size_t i = 0; i < k; i++) {
+            Request *r = L.batch[i].first;
+            const uint32_t g = L.batch[i].second;
+            L.h_idx[i] = r->base + r->in1[g];
+            L.h_idx[max_batch + i] = r->base + r->in2[g];
+            L.h_idx[2 * max_batch + i] = r->base + r->num_inputs + g;
+            L.h_idx[3 * max_batch + i] = (uint32_t)r->type[g];
+        }
+        cudaError_t e = cudaStreamWaitEvent(L.st, ev_up, 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(L.d_idx, L.h_idx, 4 * max_batch * sizeof(uint32_t), cudaMemcpyHostToDevice, L.st);
+        if (e != cudaSuccess) return c->cuda_fail(e, "server index copy");
+        const uint32_t *i1 = L.d_idx, *i2 = L.d_idx + max_batch, *io = L.d_idx + 2 * max_batch;
+        const int32_t *gt = reinterpret_cast<const int32_t *>(L.d_idx + 3 * max_batch);
+        int rc;
+        if (c->wide) {
+            rc = launch_blind_rotate64_indexed(*c, d_pool, d_pool, i1, i2, gt, k, 0, (uint64_t *)L.d_accs, nullptr,
+                                               (uint64_t *)L.d_ext, 0, false, L.st);
+            if (!rc) rc = launch_lwe_keyswitch64(*c, (const uint64_t *)L.d_ext, k, true, d_pool, L.st, io);
+        } else {
+            rc = launch_blind_rotate32_indexed(*c, d_pool, d_pool, i1, i2, gt, k, 0, (uint32_t *)L.d_accs,
+                                               (uint32_t *)L.d_ext, L.st);
+            if (!rc)
+                rc = launch_lwe_keyswitch32(*c, (const uint32_t *)L.d_ext, k, true, d_pool, L.st, L.d_accs,
+                                            L.accs_bytes, io);
+        }
+        if (!rc && cudaEventRecord(L.ev, L.st) != cudaSuccess) rc = FHEACC_EIO;
+        return rc;
+    }
+
+    // Marks a finished lane's gates done and completes the requests whose
+    // last gate it ran (their outputs are read back here).
+    int retire(Lane &L)
+    {
+        const double t1 = now_s();
+        std::vector<Request *> complete;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            rounds++;
+            gates_run += L.batch.size();
+            if (--lanes_busy == 0) busy_s += t1 - busy_since;
+            for (auto &bg : L.batch) {
+                bg.first->state[bg.second] = 2;
+                if (++bg.first->done == bg.first->num_gates) complete.push_back(bg.first);
+            }
+        }
+        L.busy = false;
+        L.batch.clear();
+        for (Request *r : complete) {
+            const size_t first = (size_t)r->base + r->num_inputs + r->num_gates - r->num_outputs;
+            cudaError_t e = cudaMemcpyAsync(r->out_host, d_pool + first * W,
+                                            (size_t)r->num_outputs * W * sizeof(uint64_t), cudaMemcpyDeviceToHost, up);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(up);
+            if (e != cudaSuccess) r->status = c->cuda_fail(e, "server output copy");
+        }
+        if (!complete.empty()) {
+            std::lock_guard<std::mutex> lk(mu);
+            const double t = now_s();
+            for (Request *r : complete) {
+                r->t_done = t;
+                active.erase(std::find(active.begin(), active.end(), r));
+                free_range(r->base, r->num_inputs + r->num_gates);
+                finished.push_back(r);
+            }
+            cv_done.notify_all();
+        }
+        return FHEACC_OK;
+    }
+
+    // The worker: keeps up to kLanes rounds in flight. A lane whose round has
+    // finished is retired (its gates done, finished requests completed); a
+    // free lane takes every gate that is ready and not in flight. Requests
+    // arriving meanwhile are admitted and uploaded at once, so their first
+    // gates go out on the next free lane while older rounds still run.
     void run()
     {
         cudaSetDevice(c->device);
-        std::vector<std::pair<Request *, uint32_t>> batch;
+        int next_lane = 0;
         for (;;) {
             std::vector<Request *> fresh;
+            bool any_active = false;
             {
                 std::unique_lock<std::mutex> lk(mu);
                 for (;;) {
                     fresh = admit_locked();
-                    if (stop || !active.empty()) break;
+                    bool busy = false;
+                    for (auto &L : lane) busy |= L.busy;
+                    if (stop || !active.empty() || busy) break;
                     cv_work.wait(lk);
                 }
                 if (stop) return;
+                any_active = !active.empty();
             }
             if (int rc = upload_inputs(fresh)) {
                 fail_all(rc);
                 return;
             }
-            // gather ready gates, oldest request first
-            batch.clear();
-            {
-                std::lock_guard<std::mutex> lk(mu);
-                for (Request *r : active) {
-                    bool blocked = false;
-                    for (uint32_t g = r->next_scan; g < r->num_gates && batch.size() < max_batch; g++) {
-                        if (r->state[g] == 0) {
-                            if (node_ready(r, r->in1[g]) && node_ready(r, r->in2[g])) {
-                                r->state[g] = 1;
-                                batch.emplace_back(r, g);
-                            } else {
-                                blocked = true;
-                            }
-                        }
-                        if (!blocked) r->next_scan = g + 1;   // everything below is issued or done
-                    }
-                    if (batch.size() >= max_batch) break;
-                }
-            }
-            if (batch.empty()) {
-                // every gate of every admitted request is waiting on a gate
-                // that is not in flight: impossible for a well-formed DAG
-                fail_all(c->fail(FHEACC_EINVAL, "server: request circuit has a cycle or a dangling input"));
-                return;
-            }
-            const size_t k = batch.size();
-            for (size_t i = 0; i < k; i++) {
-                Request *r = batch[i].first;
-                const uint32_t g = batch[i].second;
-                h_idx[i] = r->base + r->in1[g];
-                h_idx[max_batch + i] = r->base + r->in2[g];
-                h_idx[2 * max_batch + i] = r->base + r->num_inputs + g;
-                h_idx[3 * max_batch + i] = (uint32_t)r->type[g];
-            }
-            const double t0 = now_s();
-            cudaError_t e = cudaMemcpyAsync(d_idx, h_idx, 4 * max_batch * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
-            if (e != cudaSuccess) {
-                fail_all(c->cuda_fail(e, "server index copy"));
-                return;
-            }
-            int rc = launch_blind_rotate32_indexed(*c, d_pool, d_pool, d_idx, d_idx + max_batch,
-                                                   reinterpret_cast<const int32_t *>(d_idx + 3 * max_batch), k, 0,
-                                                   d_accs, d_ext, st);
-            if (!rc) rc = launch_lwe_keyswitch32_indexed(*c, d_ext, k, true, d_pool, d_idx + 2 * max_batch, st);
-            if (!rc && cudaEventRecord(ev, st) != cudaSuccess) rc = FHEACC_EIO;
-            if (rc) {
-                fail_all(rc);
-                return;
-            }
-            // admit and upload new arrivals while the round runs
-            {
-                std::vector<Request *> more;
-                {
-                    std::lock_guard<std::mutex> lk(mu);
-                    more = admit_locked();
-                }
-                if (int rc2 = upload_inputs(more)) {
-                    fail_all(rc2);
+            bool progressed = false;
+            for (auto &L : lane) {
+                if (!L.busy) continue;
+                cudaError_t e = cudaEventQuery(L.ev);
+                if (e == cudaErrorNotReady) continue;
+                if (e != cudaSuccess) {
+                    fail_all(c->cuda_fail(e, "server round"));
                     return;
                 }
+                retire(L);
+                progressed = true;
             }
-            e = cudaEventSynchronize(ev);
-            if (e != cudaSuccess) {
-                fail_all(c->cuda_fail(e, "server round"));
-                return;
-            }
-            const double t1 = now_s();
-            std::vector<Request *> complete;
-            {
-                std::lock_guard<std::mutex> lk(mu);
-                rounds++;
-                gates_run += k;
-                busy_s += t1 - t0;
-                for (auto &bg : batch) {
-                    bg.first->state[bg.second] = 2;
-                    if (++bg.first->done == bg.first->num_gates) complete.push_back(bg.first);
+            for (int li = 0; li < kLanes && any_active; li++) {
+                Lane &L = lane[(next_lane + li) % kLanes];
+                if (L.busy) continue;
+                {
+                    std::lock_guard<std::mutex> lk(mu);
+                    gather_locked(L.batch);
+                    if (L.batch.empty()) break;
+                    L.t0 = now_s();
+                    if (lanes_busy++ == 0) busy_since = L.t0;
                 }
-            }
-            for (Request *r : complete) {
-                const size_t first = (size_t)r->base + r->num_inputs + r->num_gates - r->num_outputs;
-                e = cudaMemcpyAsync(r->out_host, d_pool + first * W, (size_t)r->num_outputs * W * sizeof(uint64_t),
-                                    cudaMemcpyDeviceToHost, st);
-                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-                if (e != cudaSuccess) r->status = c->cuda_fail(e, "server output copy");
-            }
-            if (!complete.empty()) {
-                std::lock_guard<std::mutex> lk(mu);
-                const double t = now_s();
-                for (Request *r : complete) {
-                    r->t_done = t;
-                    active.erase(std::find(active.begin(), active.end(), r));
-                    free_range(r->base, r->num_inputs + r->num_gates);
-                    finished.push_back(r);
+                L.busy = true;
+                if (int rc = launch(L)) {
+                    fail_all(rc);
+                    return;
                 }
-                cv_done.notify_all();
+                next_lane = (next_lane + li + 1) % kLanes;
+                progressed = true;
+            }
+            if (progressed) continue;
+            int busy = 0;
+            for (auto &L : lane) busy += L.busy;
+            if (!busy) {
+                // every gate of every admitted request waits on a gate that
+                // is neither in flight nor done: impossible for a DAG
+                bool stuck;
+                {
+                    std::lock_guard<std::mutex> lk(mu);
+                    stuck = !active.empty();
+                }
+                if (stuck) {
+                    fail_all(c->fail(FHEACC_EINVAL, "server: request circuit has a cycle or a dangling input"));
+                    return;
+                }
+                continue;
+            }
+            if (busy == kLanes) {
+                // both lanes full: block on the older round
+                Lane *old = nullptr;
+                for (auto &L : lane)
+                    if (L.busy && (!old || L.t0 < old->t0)) old = &L;
+                cudaError_t e = cudaEventSynchronize(old->ev);
+                if (e != cudaSuccess) {
+                    fail_all(c->cuda_fail(e, "server round"));
+                    return;
+                }
+            } else {
+                // a lane is free but nothing is ready: wait for a round to end
+                // or a request to arrive
+                std::unique_lock<std::mutex> lk(mu);
+                cv_work.wait_for(lk, std::chrono::microseconds(100));
             }
         }
     }
@@ -287,6 +374,29 @@ struct Server {
     }
 };
 
+// Frees everything a server holds (its worker has stopped); the device is current.
+static void server_release(Server *s)
+{
+    for (auto &L : s->lane)
+        if (L.st) cudaStreamSynchronize(L.st);
+    if (s->up) cudaStreamSynchronize(s->up);
+    for (Request *r : s->waiting) delete r;
+    for (Request *r : s->active) delete r;
+    for (Request *r : s->finished) delete r;
+    for (auto &L : s->lane) {
+        cudaFree(L.d_idx);
+        cudaFreeHost(L.h_idx);
+        cudaFree(L.d_accs);
+        cudaFree(L.d_ext);
+        if (L.ev) cudaEventDestroy(L.ev);
+        if (L.st) cudaStreamDestroy(L.st);
+    }
+    cudaFree(s->d_pool);
+    if (s->ev_up) cudaEventDestroy(s->ev_up);
+    if (s->up) cudaStreamDestroy(s->up);
+    delete s;
+}
+
 }  // namespace fheacc
 
 using namespace fheacc;
@@ -295,31 +405,52 @@ extern "C" {
 
 int fheacc_server_create(fheacc_ctx *ctx, size_t max_batch, size_t pool_ciphertexts, fheacc_server **out)
 {
-    if (!ctx || !out || max_batch == 0 || pool_ciphertexts == 0 || pool_ciphertexts > 0xFFFFFFF0u) return FHEACC_EINVAL;
+    if (!ctx || !out || max_batch == 0 || max_batch > (1u << 24) || pool_ciphertexts > 0xFFFFFFF0u)
+        return FHEACC_EINVAL;
     Context &c = *reinterpret_cast<Context *>(ctx);
-    if (c.wide) return c.fail(FHEACC_EINVAL, "server: runs the N = 1024 parameter sets");
-    if (!c.d_btkey || !c.d_kskey) return c.fail(FHEACC_ENOKEY, "server: keys must be uploaded first");
-    int prev = -1;
-    cudaGetDevice(&prev);
-    if (prev != c.device) cudaSetDevice(c.device);
+    if (c.wide ? (!c.d_btkey64 || !c.d_kskey64) : (!c.d_btkey || !c.d_kskey))
+        return c.fail(FHEACC_ENOKEY, "server: keys must be uploaded first");
+    DeviceGuard guard(c.device);
     Server *s = new Server();
     s->c = &c;
     s->max_batch = max_batch;
-    s->slots = (uint32_t)pool_ciphertexts;
     s->W = (size_t)c.p.n + 1;
-    cudaError_t e = cudaMalloc(&s->d_pool, (size_t)s->slots * s->W * sizeof(uint64_t));
-    if (e == cudaSuccess) e = cudaMalloc(&s->d_idx, 4 * max_batch * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMallocHost(&s->h_idx, 4 * max_batch * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&s->d_accs, (max_batch * 2048 + kClaimWords) * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&s->d_ext, max_batch * kExtractStride * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev, cudaEventDisableTiming);
-    if (prev >= 0 && prev != c.device) cudaSetDevice(prev);
+    const size_t ct_bytes = s->W * sizeof(uint64_t);
+    const size_t lane_bytes = 4 * max_batch * sizeof(uint32_t) + bootstrap_accs_bytes(c, max_batch) +
+                              bootstrap_extract_bytes(c, max_batch);
+    if (pool_ciphertexts == 0) {
+        // a quarter of the device memory free now (after the lanes' scratch),
+        // at most 32 GiB
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || free_b < kLanes * lane_bytes) {
+            cudaGetLastError();
+            delete s;
+            return c.fail(FHEACC_ENOMEM, "server: no free device memory for the pool");
+        }
+        const size_t pool_b = std::min<size_t>((free_b - kLanes * lane_bytes) / 4, (size_t)32 << 30);
+        pool_ciphertexts = std::min<size_t>(pool_b / ct_bytes, 0xFFFFFFF0u);
+        if (pool_ciphertexts == 0) {
+            delete s;
+            return c.fail(FHEACC_ENOMEM, "server: no free device memory for the pool");
+        }
+    }
+    s->slots = (uint32_t)pool_ciphertexts;
+    cudaError_t e = cudaMalloc(&s->d_pool, (size_t)s->slots * ct_bytes);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->up, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->ev_up, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(s->ev_up, s->up);
+    for (auto &L : s->lane) {
+        L.accs_bytes = bootstrap_accs_bytes(c, max_batch);
+        if (e == cudaSuccess) e = cudaMalloc(&L.d_idx, 4 * max_batch * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMallocHost(&L.h_idx, 4 * max_batch * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc(&L.d_accs, L.accs_bytes);
+        if (e == cudaSuccess) e = cudaMalloc(&L.d_ext, bootstrap_extract_bytes(c, max_batch));
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L.st, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L.ev, cudaEventDisableTiming);
+    }
     if (e != cudaSuccess) {
         cudaGetLastError();
-        cudaFree(s->d_pool); cudaFree(s->d_idx); cudaFreeHost(s->h_idx); cudaFree(s->d_accs); cudaFree(s->d_ext);
-        if (s->st) cudaStreamDestroy(s->st);
-        delete s;
+        server_release(s);
         return c.fail(FHEACC_ENOMEM, std::string("server allocation: ") + cudaGetErrorString(e));
     }
     s->free_ranges[0] = s->slots;
@@ -402,6 +533,8 @@ int fheacc_server_stats(fheacc_server *srv, fheacc_server_stats_t *st)
     uint64_t free_slots = 0;
     for (auto &kv : s.free_ranges) free_slots += kv.second;
     st->free_slots = free_slots;
+    st->pool_slots = s.slots;
+    st->lanes = kLanes;
     return FHEACC_OK;
 }
 
@@ -415,22 +548,8 @@ int fheacc_server_destroy(fheacc_server *srv)
     }
     s->cv_work.notify_all();
     if (s->worker.joinable()) s->worker.join();
-    int prev = -1;
-    cudaGetDevice(&prev);
-    if (prev != s->c->device) cudaSetDevice(s->c->device);
-    cudaStreamSynchronize(s->st);
-    for (Request *r : s->waiting) delete r;
-    for (Request *r : s->active) delete r;
-    for (Request *r : s->finished) delete r;
-    cudaFree(s->d_pool);
-    cudaFree(s->d_idx);
-    cudaFreeHost(s->h_idx);
-    cudaFree(s->d_accs);
-    cudaFree(s->d_ext);
-    cudaEventDestroy(s->ev);
-    cudaStreamDestroy(s->st);
-    if (prev >= 0 && prev != s->c->device) cudaSetDevice(prev);
-    delete s;
+    DeviceGuard guard(s->c->device);
+    server_release(s);
     return FHEACC_OK;
 }
 

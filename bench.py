@@ -140,6 +140,33 @@ def steps_of(c1, c2, gates, P):
     return steps
 
 
+class KeyCache:
+    """One key set (secret keys, bootstrap and key-switch keys, a context with
+    both uploaded) per preset, made once and shared by the blocks of a run."""
+
+    def __init__(self, F, device=0):
+        self.F, self.device, self.sets = F, device, {}
+
+    def get(self, preset):
+        if preset not in self.sets:
+            F = self.F
+            P = F.params_preset(preset)
+            lsk = F.LWE_secretkey(P, SEEDS["lwe_sk"])
+            rsk = F.RLWE_secretkey(P, SEEDS["rlwe_sk"])
+            bt = F.bootstrap_key(P, SEEDS["btkey"], lsk, rsk)
+            ks = F.keyswitch_key(P, SEEDS["kskey"], rsk, lsk)
+            ctx = F.Context(P, self.device)
+            ctx.upload_bootstrap_key(bt)
+            ctx.upload_keyswitch_key(ks)
+            self.sets[preset] = dict(P=P, lsk=lsk, rsk=rsk, bt=bt, ks=ks, ctx=ctx)
+        return self.sets[preset]
+
+    def close(self):
+        for s in self.sets.values():
+            s["ctx"].close()
+        self.sets = {}
+
+
 def make_inputs(F, P, batch, rank):
     lsk = F.LWE_secretkey(P, SEEDS["lwe_sk"])
     rsk = F.RLWE_secretkey(P, SEEDS["rlwe_sk"])
@@ -194,7 +221,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "bootstraps/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": config_of(param_view(P), args),
+        "config": config_of(param_view(P), args.batch),
         "cpu_baseline": {"value": value, "unit": "bootstraps/s", "cores": cores, "kind": "port",
                          "sample": "%d gates per step of the %d-gate batch, oracle eval_bootstrap "
                                    "(C restatement of RLWE.cpp:726-786) on %d threads; keys from the oracle's own "
@@ -309,17 +336,19 @@ def run_serving(F, ctx, P, lsk, rate, duration, kmax=256, seed=7, max_batch=4096
             "queue_ms_p99": float(np.percentile(queue, 99)), "gpu_busy_frac": st["busy_s"] / elapsed}
 
 
-def run_mixed(args):
+def run_mixed(args, cache=None):
     """Uneven batching (one CUDA-graph launch per step): requests of geometric
     size (mean 64, from a seed) until 3000 N=1024 and 700 N=2048 gates, the two
     parameter sets as two contexts, each autotuned for its batch, both batches
-    captured into one graph."""
+    captured into one graph. Returns the line (printed when run alone)."""
     import torch
     import __graft_entry__
     __graft_entry__.build_product()
     import importlib
     F = importlib.import_module("3rd_gen_fhe_acc_gb300")
     torch.cuda.set_device(0)
+    own = cache is None
+    cache = cache or KeyCache(F)
     rng = np.random.default_rng(args.mixed_seed)
     sets = []
     for preset, total in ((0, args.mixed_narrow), (1, args.mixed_wide)):
@@ -341,20 +370,15 @@ def run_mixed(args):
             offs[ri] = off
             off += S["counts"][ri]
         S["offsets"] = offs
-        lsk = F.LWE_secretkey(P, SEEDS["lwe_sk"])
-        rsk = F.RLWE_secretkey(P, SEEDS["rlwe_sk"])
+        K = cache.get(S["preset"])
+        lsk = K["lsk"]
         x = rng.integers(0, 2, B).astype(np.uint8)
         y = rng.integers(0, 2, B).astype(np.uint8)
         g = rng.integers(0, 6, B).astype(np.int32)
         c = F.LWE_encrypt(P, SEEDS["enc"] + 31 * si, lsk, np.concatenate([x, y]))
         S.update(lsk=lsk, x=x, y=y, g=g, c1=c[:B].copy(), c2=c[B:].copy(),
                  truth=np.array([F.gate_truth(int(a), b, d) for a, b, d in zip(g, x, y)], dtype=np.uint8))
-        S["bt"] = F.bootstrap_key(P, SEEDS["btkey"], lsk, rsk)
-        S["ks"] = F.keyswitch_key(P, SEEDS["kskey"], rsk, lsk)
-        ctx = F.Context(P, 0)
-        ctx.upload_bootstrap_key(S["bt"])
-        ctx.upload_keyswitch_key(S["ks"])
-        S["ctx"] = ctx
+        S["bt"], S["ks"], S["ctx"] = K["bt"], K["ks"], K["ctx"]
         S["d1"] = torch.from_numpy(S["c1"].view(np.int64)).cuda()
         S["d2"] = torch.from_numpy(S["c2"].view(np.int64)).cuda()
         S["dg"] = torch.from_numpy(g).cuda()
@@ -515,13 +539,17 @@ def run_mixed(args):
                    "tuned_equals_untuned": all(S["tuned_same"] for S in sets),
                    "every_request_decrypts": bool(per_request_ok), "setup_s": setup_s},
     }
-    print(json.dumps(line))
-    for S in sets:
-        S["ctx"].close()
-    return 0
+    for S in sets:   # the contexts go back to their defaults
+        for opt, v in ((F.OPT_BR_REGS_FOR_3, -1), (F.OPT_BR_CTAS_PER_SM, 0), (F.OPT_BR_GROUP, 0),
+                       (F.OPT_BR_WINDOW, -1), (F.OPT_BR_PIPES, 0)):
+            S["ctx"].set_option(opt, v)
+    if own:
+        print(json.dumps(line))
+        cache.close()
+    return line
 
 
-def run_psi(args):
+def run_psi(args, cache=None):
     """One PSI query of the reference's PSI test (test.cpp:1510-1606) per step,
     at N = 2048 (the 64-bit set): homo_expand of digitG packed RLWEs into N
     RGSWs (app.cpp:78-96), a CMUX tree selecting one of 2^(18 - log2 N) = 128
@@ -540,9 +568,14 @@ def run_psi(args):
     N, Q, dG, logN = P.N, P.Q, P.digitG, 11
     rw, gw = 2 * N, dG * 4 * N
     t_setup = time.perf_counter()
-    rsk = F.RLWE_secretkey(P, 12)
+    own = cache is None
+    if own:
+        rsk = F.RLWE_secretkey(P, 12)
+        ctx = F.Context(P, 0)
+    else:
+        K = cache.get(1)
+        rsk, ctx = K["rsk"], K["ctx"]
     subs = F.substitute_key(P, 15, rsk)
-    ctx = F.Context(P, 0)
     ctx.upload_subs_key(subs)
     stream = torch.cuda.current_stream()
     st = stream.cuda_stream
@@ -705,9 +738,10 @@ def run_psi(args):
         "checks": {"result_decodes": bool(decodes(first_out)), "e2e_decodes": bool(e2e_ok),
                    "steps_repeatable": bool(repeat_ok), "setup_s": setup_s},
     }
-    print(json.dumps(line))
-    ctx.close()
-    return 0
+    if own:
+        print(json.dumps(line))
+        ctx.close()
+    return line
 
 
 def fheacc_key_bytes(P):
@@ -717,16 +751,47 @@ def fheacc_key_bytes(P):
     return P.Br * P.digitR * P.n * P.digitG * 4 * P.N * 16 + P.Bks * P.digitKS * P.N * ((P.n + 32) // 32 * 32) * 8
 
 
-def config_of(P, args):
+def config_of(P, batch):
     word = "uint32" if P.N == 1024 else "uint64"
     return {"workload": ("%d independent NAND-gate bootstraps: n=%d, N=%d, Q=%d (%s words), BG=2^%d x%d, "
                          "Br=%d x%d, Bks=%d x%d, q=%d; keys and input bits from fixed seeds") % (
-                            args.batch, P.n, P.N, P.Q, word, P.BG_bits, P.digitG, P.Br, P.digitR, P.Bks, P.digitKS,
+                            batch, P.n, P.N, P.Q, word, P.BG_bits, P.digitG, P.Br, P.digitR, P.Bks, P.digitKS,
                             P.q),
-            "batch": args.batch, "gate": "NAND", "n": P.n, "N": P.N, "Q": P.Q,
+            "batch": batch, "gate": "NAND", "n": P.n, "N": P.N, "Q": P.Q,
             "l2": "flushed between timed steps (write of a 512 MiB buffer); keys (%.1f GB) exceed L2" % (
                 (fheacc_key_bytes(P)) / 1e9),
             "parallelism": "one batch per GPU (independent gates, no collective)"}
+
+
+def extra_blocks(F, D, cache, args, dev_id):
+    """The other measured configurations, each with its own CUDA-event
+    timing, rooflines and CPU sample, reported inside the default line:
+    cfg2, 2048 gates at N = 2048 (64-bit words); mixed, the uneven N = 1024 +
+    N = 2048 batch in one CUDA-graph launch; psi, the reference's PSI query at
+    N = 2048. Their steps are capped at 3 to keep the whole run within a few
+    minutes (the warm-up stays at 3 or more)."""
+    import copy
+    out = {}
+    sub = copy.copy(args)
+    sub.steps = min(args.steps, 3)
+
+    def keep(line, keys):
+        return {k: line[k] for k in keys if k in line}
+    common = ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "dtype", "config", "e2e", "roofline",
+              "cpu_baseline", "clocks", "gpu_launches", "checks")
+    t0 = time.perf_counter()
+    w = measure_batch(F, D, cache, 1, args.wide_batch, sub, dev_id, sub.steps, 2, False)
+    out["cfg2"] = keep(w, common + ("roofline_hbm", "plain"))
+    out["cfg2"]["wall_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    m = run_mixed(sub, cache)
+    out["mixed"] = keep(m, common + ("per_set", "graph_vs_sum_of_alone", "concurrent_branches"))
+    out["mixed"]["wall_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    p = run_psi(args, cache)
+    out["psi"] = keep(p, common + ("phases_ms",))
+    out["psi"]["wall_s"] = time.perf_counter() - t0
+    return out
 
 
 def main():
@@ -740,6 +805,9 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=48)
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="only the headline configuration (4096 gates, N=1024): skip the cfg2 / mixed / psi blocks")
+    ap.add_argument("--wide-batch", type=int, default=2048, help="gates of the N=2048 block (cfg2)")
     ap.add_argument("--serve", action="store_true",
                     help="sweep serving rates (PSI queries through the continuous-batching server) and exit")
     ap.add_argument("--serve-rate", type=float, default=20000.0, help="offered bootstraps/s of the serving sample")
@@ -760,9 +828,11 @@ def main():
     if args.profile_case:
         return profile_case(args.preset)
     if args.mixed:
-        return run_mixed(args)
+        run_mixed(args)
+        return 0
     if args.psi:
-        return run_psi(args)
+        run_psi(args)
+        return 0
 
     import torch
     import __graft_entry__
@@ -772,14 +842,25 @@ def main():
     D = Dist(use_cuda=True)
     dev_id = D.local if D.ws > 1 else 0
     torch.cuda.set_device(dev_id)
-    P = F.params_preset(args.preset)
-    B = args.batch
+    cache = KeyCache(F, dev_id)
+    line = measure_batch(F, D, cache, args.preset, args.batch, args, dev_id, args.steps, args.plain_sample, True)
+    if D.ws == 1 and not args.no_extra:
+        line["configs"] = extra_blocks(F, D, cache, args, dev_id)
+    if D.rank == 0:
+        print(json.dumps(line))
+    cache.close()
+    D.close()
+    return 0
+
+
+def measure_batch(F, D, cache, preset, B, args, dev_id, steps, plain_sample, serve):
+    """One batched configuration: K timed steps on device-resident inputs, the
+    e2e steps through the host-buffer C ABI, the plain form, the rooflines, a
+    CPU sample and (serve) the serving sample; returns the JSON line."""
+    import torch
+    K = cache.get(preset)
+    P, ctx, bt, ks = K["P"], K["ctx"], K["bt"], K["ks"]
     lsk, rsk, x, y, c1, c2, gates = make_inputs(F, P, B, D.rank)
-    bt = F.bootstrap_key(P, SEEDS["btkey"], lsk, rsk)
-    ks = F.keyswitch_key(P, SEEDS["kskey"], rsk, lsk)
-    ctx = F.Context(P, dev_id)
-    ctx.upload_bootstrap_key(bt)
-    ctx.upload_keyswitch_key(ks)
     W = P.n + 1
     stream = torch.cuda.current_stream()
     st = stream.cuda_stream
@@ -816,7 +897,7 @@ def main():
     D.barrier()
     torch.cuda.synchronize()
     n0 = ctx.kernel_launches()
-    for _ in range(args.steps):
+    for _ in range(steps):
         flush.fill_(1)
         e0, e1 = step_device(True)
         torch.cuda.synchronize()
@@ -829,7 +910,7 @@ def main():
     D.barrier()
     clk = clocks.stop()
     total_s = D.max(sum(step_ms) / 1e3)
-    value = D.ws * B * args.steps / total_s
+    value = D.ws * B * steps / total_s
     same = np.array_equal(dout.cpu().numpy().view(np.uint64), out0)
 
     # e2e: host buffers through the C ABI (pinned host memory)
@@ -839,7 +920,7 @@ def main():
     ho = torch.zeros_like(h1).pin_memory()
     n1, n2, ng, no = (t.numpy() for t in (h1, h2, hg, ho))
     e2e_s = []
-    for s in range(args.warmup + args.steps):
+    for s in range(args.warmup + steps):
         flush.fill_(1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -851,11 +932,11 @@ def main():
             e2e_s.append(dt)
     D.barrier()
     e2e_total = D.max(sum(e2e_s))
-    e2e_value = D.ws * B * args.steps / e2e_total
+    e2e_value = D.ws * B * steps / e2e_total
     e2e_same = np.array_equal(no.view(np.uint64), out0)
 
     # plain form: one launch sequence per gate
-    Pn = min(args.plain_sample, B)
+    Pn = min(plain_sample, B)
     ctx.bootstrap_plain_async(d1.data_ptr(), d2.data_ptr(), dg.data_ptr(), 4, dout.data_ptr(), 0, st)
     torch.cuda.synchronize()
     lat = []
@@ -894,7 +975,7 @@ def main():
     if os.path.exists(TRAFFIC_FILE):
         with open(TRAFFIC_FILE) as f:
             tj = json.load(f)
-        if args.batch == 4096 and args.preset == 0:
+        if B == 4096 and preset == 0:
             traffic = tj.get("br32_pipe", {}).get("bytes_per_launch_4096")
     hbm_peak = None
     peaks_src = "fallback 6800 GB/s"
@@ -971,17 +1052,17 @@ def main():
                "bitexact_vs_gpu": "%d/%d" % (int((co == out0[:nsample]).all(axis=1).sum()), nsample)}
 
     serving = None
-    if D.ws == 1 and args.serve_seconds > 0 and P.N == 1024:   # the server runs the 32-bit sets
+    if serve and D.ws == 1 and args.serve_seconds > 0 and P.N == 1024:   # the server runs the 32-bit sets
         serving = run_serving(F, ctx, P, lsk, args.serve_rate, args.serve_seconds)
-    if args.serve and P.N == 1024:
+    if serve and args.serve and P.N == 1024:
         sweep = [run_serving(F, ctx, P, lsk, r, 10.0) for r in (1e3, 5e3, 1e4, 2e4, 3e4, 4e4, 6e4, 1e5)]
         print(json.dumps({"serving_sweep": sweep}))
 
     line = {
-        "metric": METRIC, "value": value, "unit": "bootstraps/s", "n_gpus": D.ws, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": "bootstraps/s", "n_gpus": D.ws, "steps": steps,
         "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32" if P.N == 1024 else "u64", "data": "synthetic",
-        "config": config_of(P, args),
+        "config": config_of(P, B),
         "e2e": {"value": e2e_value, "unit": "bootstraps/s",
                 "h2d_bytes_per_step": int(2 * B * W * 8 + B * 4), "d2h_bytes_per_step": int(B * W * 8),
                 "ms_per_step": 1e3 * statistics.mean(e2e_s)},
@@ -997,11 +1078,7 @@ def main():
                    "plain_equal": bool(plain_ok), "kernel_ms": {"blind_rotate": statistics.mean(br_ms),
                                                                 "keyswitch": statistics.mean(ks_ms)}},
     }
-    if D.rank == 0:
-        print(json.dumps(line))
-    ctx.close()
-    D.close()
-    return 0
+    return line
 
 
 if __name__ == "__main__":

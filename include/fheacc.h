@@ -393,12 +393,18 @@ int fheacc_graph_destroy(fheacc_graph *g);
  * gate_types[g]) with in1[g] != in2[g] < num_inputs + g. The last num_outputs
  * nodes are written to `out` ([num_outputs][n+1]) when the request completes.
  * All nodes of an admitted request live in a device pool of pool_ciphertexts
- * slots; a request is admitted when the pool has room for all its nodes, in
- * arrival order. A worker thread runs rounds: every gate of every admitted
- * request whose inputs are ready (up to max_batch) goes into one batched
- * launch; requests arriving meanwhile join the next round. Keys must be
- * uploaded before fheacc_server_create; the context must outlive the server
- * and not be used for other work while the server runs. */
+ * slots (0: sized at creation from the device memory then free, a quarter of
+ * it up to 32 GiB); a request is admitted when the pool has room for all its
+ * nodes, in arrival order, and a request larger than the whole pool is
+ * refused with FHEACC_EINVAL. A worker thread keeps up to two rounds in
+ * flight on two streams, each with its own scratch: whenever a round ends or
+ * a lane is free, every gate of every admitted request whose inputs are ready
+ * and that is not already in flight (up to max_batch) goes into one batched
+ * launch, so requests arriving while a round runs start on the other lane
+ * without waiting for it. Both parameter widths are served (N = 1024 and
+ * N = 2048 contexts). Keys must be uploaded before fheacc_server_create; the
+ * context must outlive the server and not be used for other work while the
+ * server runs. */
 typedef struct fheacc_server fheacc_server;
 typedef struct fheacc_request_done {
     uint64_t request_id;
@@ -408,8 +414,10 @@ typedef struct fheacc_request_done {
 } fheacc_request_done;
 typedef struct fheacc_server_stats_t {
     uint64_t rounds, gates;  /* batched launches and gates run so far */
-    double busy_s;           /* wall time of the rounds */
+    double busy_s;           /* wall time during which at least one round was on the GPU */
     uint64_t waiting, active, free_slots;
+    uint64_t pool_slots;     /* ciphertexts the pool holds */
+    uint64_t lanes;          /* rounds the server keeps in flight at once */
 } fheacc_server_stats_t;
 int fheacc_server_create(fheacc_ctx *ctx, size_t max_batch, size_t pool_ciphertexts, fheacc_server **out);
 int fheacc_server_submit(fheacc_server *srv, const uint64_t *inputs, uint32_t num_inputs, const int32_t *gate_types,

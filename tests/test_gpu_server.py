@@ -109,3 +109,50 @@ def test_server_rejects_bad_circuits(F, ctx0, keys0):
             srv.submit(ct, [9], [0], [1], 1)          # bad gate code
     finally:
         srv.close()
+
+
+def test_server_pool_sized_from_free_memory(F, ctx0, keys0):
+    """pool_ciphertexts = 0: the pool is sized at creation from the device
+    memory then free (a quarter, at most 32 GiB), and serves requests."""
+    import torch
+    free_b, _ = torch.cuda.mem_get_info()
+    srv = F.Server(ctx0, max_batch=256, pool_ciphertexts=0)
+    try:
+        st = srv.stats()
+        ct_bytes = (keys0.P.n + 1) * 8
+        assert st["pool_slots"] > 0 and st["lanes"] == 2
+        assert st["pool_slots"] * ct_bytes <= min(free_b // 4, 32 << 30)
+        assert st["free_slots"] == st["pool_slots"]
+        ct, want = make_query(F, keys0, 2, match_at=0, seed=301)
+        rid, _ = srv.submit(ct, *F.psi_equality_circuit(2))
+        got = wait_all(srv, [rid])
+        assert got[rid][0] == F.OK
+        assert np.array_equal(keys0.decrypt(got[rid][1]), want)
+    finally:
+        srv.close()
+
+
+def test_server_wide_parameter_set(F, ctx1, keys1):
+    """The N = 2048, 64-bit set through the server: a small circuit (three
+    gates in two levels), each request's words equal to the batched call on the
+    same gate inputs, mixed with other requests on both lanes."""
+    rng = np.random.default_rng(77)
+    reqs = []
+    for k in range(4):
+        bits = rng.integers(0, 2, 3).astype(np.uint8)
+        ct = keys1.encrypt(bits, seed=500 + k)
+        # node 3 = NAND(0, 1), node 4 = XOR(3, 2)
+        reqs.append((ct, bits))
+    srv = F.Server(ctx1, max_batch=64, pool_ciphertexts=256)
+    try:
+        ids = [srv.submit(ct, [F.NAND, F.XOR], [0, 3], [1, 2], 1)[0] for ct, _ in reqs]
+        got = wait_all(srv, ids, timeout_s=300)
+        for rid, (ct, bits) in zip(ids, reqs):
+            assert got[rid][0] == F.OK
+            want = (1 - (bits[0] & bits[1])) ^ bits[2]
+            assert keys1.decrypt(got[rid][1])[0] == want
+            first = ctx1.eval_bootstrap_batch(ct[0:1], ct[1:2], [F.NAND])
+            direct = ctx1.eval_bootstrap_batch(first, ct[2:3], [F.XOR])
+            assert np.array_equal(got[rid][1], direct)
+    finally:
+        srv.close()
