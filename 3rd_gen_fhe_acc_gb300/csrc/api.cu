@@ -79,7 +79,8 @@ int bootstrap_device_with(Context &c, const uint64_t *d_c1, const uint64_t *d_c2
         if (!c.d_kskey64) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
         int rc = launch_blind_rotate64_with(c, d_c1, d_c2, d_gates, count, flags, (uint64_t *)accs, nullptr,
                                             (uint64_t *)extract, 0, st);
-        return rc ? rc : launch_lwe_keyswitch64(c, (const uint64_t *)extract, count, true, d_out, st);
+        return rc ? rc : launch_lwe_keyswitch64(c, (const uint64_t *)extract, count, true, d_out, st, nullptr, accs,
+                                                bootstrap_accs_bytes(c, count));
     }
     if (!c.d_btkey) return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
     if (!c.d_kskey) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
@@ -104,7 +105,7 @@ int bootstrap_device(Context &c, const uint64_t *d_c1, const uint64_t *d_c2, con
         rc = launch_blind_rotate64(c, d_c1, d_c2, d_gates, count, flags, nullptr, ext, max_ctas, st);
         if (rc) return rc;
         if (prof) cudaEventRecord(c.prof[1], st);
-        rc = launch_lwe_keyswitch64(c, ext, count, true, d_out, st);
+        rc = launch_lwe_keyswitch64(c, ext, count, true, d_out, st, nullptr, c.accs.ptr, c.accs.bytes);
         if (prof && rc == FHEACC_OK) cudaEventRecord(c.prof[2], st);
         return rc;
     }

@@ -102,11 +102,12 @@ struct PipeSmem {
 };
 
 // Bytes of dynamic shared memory before the digit tables: one PipeSmem per
-// pipeline, then the residue table [group][n * digitR], rounded up to 16.
+// pipeline, then the residue table [group][n * digitR] and the issue order
+// [n * digitR][group], each rounded up to 16.
 template <int NB, int NP>
 __host__ __device__ constexpr size_t pipe_tables_offset(int group, size_t steps)
 {
-    return NP * sizeof(PipeSmem<NB>) + ((size_t)group * steps + 15) / 16 * 16;
+    return NP * sizeof(PipeSmem<NB>) + 2 * (((size_t)group * steps + 15) / 16 * 16);
 }
 
 __device__ __forceinline__ void load_btile(uint32_t (&x)[32], const uint32_t *src, int lane)
@@ -154,7 +155,8 @@ __device__ __forceinline__ void store_btile(uint32_t *dst, const uint32_t (&x)[3
 // none) and the step its ciphertext must have finished; [11] periods idled in
 // a row waiting for it. done[k]: last finished step of ciphertext k.
 __device__ __noinline__ void pipe_plan(const int *C, int *Nx, volatile int *done, int *cursor, const uint8_t *res,
-                                       int m, int S, int mode, unsigned *status, int idle_limit)
+                                       const uint8_t *order, int m, int S, int mode, unsigned *status,
+                                       int idle_limit)
 {
     // period t's inverse-NTT item moves to the digit warps
     Nx[2] = C[6] ? C[0] : -1;
@@ -170,7 +172,7 @@ __device__ __noinline__ void pipe_plan(const int *C, int *Nx, volatile int *done
                 Nx[5] = 1;
                 break;
             }
-            const int st = idx / m, k = idx - st * m;
+            const int st = idx / m, k = order[idx];
             if (step_issued(res + k * S, st, mode)) {
                 int prev = st - 1;
                 while (prev >= 0 && !step_issued(res + k * S, prev, mode)) prev--;
@@ -304,6 +306,8 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PipeSmem<GW> *pipes = reinterpret_cast<PipeSmem<GW> *>(smem_raw);
     uint8_t *res = smem_raw + NP * sizeof(PipeSmem<GW>);   // [group][n * digitR] residues
+    // [n * digitR][group]: the group's ciphertexts of each step, by residue
+    uint8_t *order = res + ((size_t)A.group * (A.n * A.digitR) + 15) / 16 * 16;
     __shared__ int done[kMaxGroup * NP];
     __shared__ int cursor;
     __shared__ unsigned long long claim_first;
@@ -357,11 +361,23 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
             c0[11] = 0;                   // idle periods in a row
         }
         __syncthreads();
+        // issue order of each step: the group's ciphertexts by residue, so that
+        // items applying the same RGSW key follow one another and the later
+        // ones read it from L1 (the order within a step is free: every
+        // ciphertext still takes its own steps in the reference's order)
+        for (int st = threadIdx.x; st < S; st += blockDim.x) {
+            uint8_t *o = order + st * m;
+            int pos = 0;
+            for (uint32_t r = 0; r < A.Br; r++)
+                for (int k = 0; k < m; k++)
+                    if (res[k * S + st] == r) o[pos++] = (uint8_t)k;
+        }
+        __syncthreads();
 
         // ---- NP pipelines over the (step, ciphertext) items of the group. One
         // thread of each plans the pipeline's next period after each period
         // and publishes the plan in shared memory.
-        if (pw == 0 && lane == 0) pipe_plan(s.ctl[1], s.ctl[0], done, &cursor, res, m, S, mode, A.status, A.idle_limit);
+        if (pw == 0 && lane == 0) pipe_plan(s.ctl[1], s.ctl[0], done, &cursor, res, order, m, S, mode, A.status, A.idle_limit);
         pipe_barrier(1 + pl, PT);
         for (int t = 0;; t ^= 1) {
             const int *ctl = s.ctl[t];
@@ -391,7 +407,7 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
             // item once its digit NTTs are in shared memory; one thread first
             // plans the next period
             pipe_barrier(1 + pl, PT);
-            if (pw == 0 && lane == 0) pipe_plan(ctl, s.ctl[t ^ 1], done, &cursor, res, m, S, mode, A.status, A.idle_limit);
+            if (pw == 0 && lane == 0) pipe_plan(ctl, s.ctl[t ^ 1], done, &cursor, res, order, m, S, mode, A.status, A.idle_limit);
             if (ctl[3] >= 0) {
                 const int gk = ctl[3], gs = ctl[2];
                 const uint32_t rr = res[gk * S + gs];
@@ -436,9 +452,9 @@ static int launch_pipe_dg(Context &c, dev::PipeArgs A, int max_ctas, cudaStream_
     const size_t steps = (size_t)c.p.n * c.p.digitR, tables = A.digit_tables ? 20 * ((size_t)1 << c.p.BG_bits) : 0;
     // group cap: kMaxGroup (or the tuned cap) per pipeline, within the shared memory of one CTA
     int cap = NP * (c.tune.br_group > 0 ? std::min(c.tune.br_group, dev::kMaxGroup) : dev::kMaxGroup);
-    const size_t fixed = dev::pipe_tables_offset<GW, NP>(0, steps) + tables + 16;
-    if (fixed + (size_t)cap * steps > kPipeSmemBudget)
-        cap = fixed < kPipeSmemBudget ? (int)((kPipeSmemBudget - fixed) / steps) : 0;
+    const size_t fixed = dev::pipe_tables_offset<GW, NP>(0, steps) + tables + 32;
+    if (fixed + 2 * (size_t)cap * steps > kPipeSmemBudget)
+        cap = fixed < kPipeSmemBudget ? (int)((kPipeSmemBudget - fixed) / (2 * steps)) : 0;
     if (cap < 1) return c.fail(FHEACC_EINVAL, "n * digitR too large for the blind rotation's residue table");
     // residency with the largest group allowed; the group is then fitted to the batch
     size_t smem = dev::pipe_tables_offset<GW, NP>(cap, steps) + tables;

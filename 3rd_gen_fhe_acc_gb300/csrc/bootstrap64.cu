@@ -743,6 +743,53 @@ __global__ void __launch_bounds__(512) lwe_ks64_kernel(const __grid_constant__ K
     }
 }
 
+// Split form for a few ciphertexts (a lone gate's key switch would otherwise
+// run on one CTA): CTA (ci, slice) sums rows [slice * per, ...) of
+// ciphertext ci (per <= fold rows, so its 64-bit sums cannot overflow),
+// reduces them mod Q and adds them into part[ci][ks_row] (zeroed before;
+// slices * Q < 2^64); ks64_final_kernel reduces and writes the outputs.
+__global__ void __launch_bounds__(512) ks64_partial_kernel(const __grid_constant__ Ks64Args A,
+                                                           unsigned long long *part, int slices)
+{
+    const int N = A.N, D = A.digitKS, t = threadIdx.x;
+    const uint64_t Q = A.Q;
+    const size_t rs2 = A.ks_row / 2;
+    const ulonglong2 *key2 = reinterpret_cast<const ulonglong2 *>(A.kskey);
+    const int total = N * D, per = (total + slices - 1) / slices;
+    const size_t ci = blockIdx.x / slices;
+    const int r0 = (int)(blockIdx.x % slices) * per, r1 = min(total, r0 + per);
+    if (ci >= A.count) return;
+    const uint64_t *ext = A.ext + ci * kExtract64;
+    uint64_t s0 = 0, s1 = 0;
+    for (int r = r0; r < r1; r++) {
+        const int i = r / D, j = r - i * D;
+        uint64_t a = ext[i];
+        for (int jj = 0; jj < j; jj++) a /= A.Bks;
+        const uint32_t d = (uint32_t)(a % A.Bks);
+        const ulonglong2 v = __ldg(key2 + ((size_t)(d * D + j) * N + i) * rs2 + t);
+        s0 += v.x;
+        s1 += v.y;
+    }
+    unsigned long long *p = part + ci * A.ks_row + 2 * (size_t)t;
+    atomicAdd(p + 0, (unsigned long long)(s0 % Q));
+    atomicAdd(p + 1, (unsigned long long)(s1 % Q));
+}
+
+__global__ void ks64_final_kernel(const __grid_constant__ Ks64Args A, const unsigned long long *part)
+{
+    const uint64_t Q = A.Q, Q8 = Q / 8 + 1;
+    const size_t w = (size_t)A.n + 1;
+    for (size_t x = (size_t)blockIdx.x * blockDim.x + threadIdx.x; x < A.count * w; x += (size_t)gridDim.x * blockDim.x) {
+        const size_t ci = x / w;
+        const int k = (int)(x - ci * w);
+        const uint64_t sm = part[ci * A.ks_row + k] % Q;
+        uint64_t v;
+        if (k < A.n) v = sm ? Q - sm : 0;
+        else v = ((A.ext[ci * kExtract64 + A.N] + Q8) % Q + Q - sm) % Q;
+        A.out[(A.out_idx ? (size_t)A.out_idx[ci] : ci) * w + k] = A.modswitch ? scale_round64(v, A.q, Q) : v;
+    }
+}
+
 }  // namespace dev
 
 static int sms_of(Context &c)
@@ -993,7 +1040,7 @@ int launch_extract64(Context &c, const uint64_t *d_rlwe, size_t count, uint64_t 
 }
 
 int launch_lwe_keyswitch64(Context &c, const uint64_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
-                           cudaStream_t st, const uint32_t *d_out_idx)
+                           cudaStream_t st, const uint32_t *d_out_idx, void *d_scratch, size_t scratch_bytes)
 {
     if (!count) return FHEACC_OK;
     if (!c.d_kskey64) return c.fail(FHEACC_ENOKEY, "LWE key-switch key not uploaded");
@@ -1005,9 +1052,31 @@ int launch_lwe_keyswitch64(Context &c, const uint64_t *d_extract, size_t count, 
     // key words are < Q: (fold + 1) Q must stay below 2^64
     const uint64_t fold = std::min<uint64_t>(256, UINT64_MAX / c.p.Q - 1);
     A.fold = (int)std::max<uint64_t>(8, fold & ~(uint64_t)7);
-    const size_t smem = (size_t)c.p.N * c.p.digitKS;
     const unsigned threads = c.dp.ks_row / 2;   // ks_row: a multiple of 32 words, > n
-    size_t blocks = std::min<size_t>(count, (size_t)sms_of(c) * 6);
+    const size_t sms = (size_t)sms_of(c);
+    // a few ciphertexts: each one's rows split over many CTAs, with at most
+    // `fold` rows per CTA and slices * Q < 2^64
+    const int rows = c.p.N * (int)c.p.digitKS;
+    const size_t max_slices = std::min<uint64_t>(UINT64_MAX / c.p.Q, 4096);
+    const size_t slices = std::min<size_t>(max_slices, std::max<size_t>((size_t)(rows + A.fold - 1) / A.fold,
+                                                                         sms * 8 / std::max<size_t>(count, 1)));
+    if (d_scratch && count < 2 * sms && count * c.dp.ks_row * sizeof(uint64_t) <= scratch_bytes &&
+        (size_t)(rows + slices - 1) / slices <= (size_t)A.fold) {
+        unsigned long long *part = reinterpret_cast<unsigned long long *>(d_scratch);
+        cudaError_t e = cudaMemsetAsync(part, 0, count * c.dp.ks_row * sizeof(uint64_t), st);
+        if (e != cudaSuccess) return c.cuda_fail(e, "key switch partials reset");
+        dev::ks64_partial_kernel<<<(unsigned)(count * slices), threads, 0, st>>>(A, part, (int)slices);
+        c.launches++;
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return c.cuda_fail(e, "key switch partial launch");
+        const size_t words = count * ((size_t)c.p.n + 1);
+        dev::ks64_final_kernel<<<(unsigned)std::min<size_t>((words + 255) / 256, 1024), 256, 0, st>>>(A, part);
+        c.launches++;
+        e = cudaGetLastError();
+        return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "key switch final launch");
+    }
+    const size_t smem = (size_t)c.p.N * c.p.digitKS;
+    size_t blocks = std::min<size_t>(count, sms * 6);
     dev::lwe_ks64_kernel<<<(unsigned)blocks, threads, smem, st>>>(A);
     c.launches++;
     cudaError_t e = cudaGetLastError();

@@ -229,8 +229,11 @@ int launch_blind_rotate64_with(Context &c, const uint64_t *d_c1, const uint64_t 
                                size_t count, uint32_t flags, uint64_t *accs, uint64_t *d_acc_out,
                                uint64_t *d_extract, int max_ctas, cudaStream_t st);
 int launch_extract64(Context &c, const uint64_t *d_rlwe, size_t count, uint64_t *d_extract, cudaStream_t st);
+// d_scratch (optional, scratch_bytes of free device memory): lets a few
+// ciphertexts' rows be split over many CTAs (count * ks_row u64 partial sums).
 int launch_lwe_keyswitch64(Context &c, const uint64_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
-                           cudaStream_t st, const uint32_t *d_out_idx = nullptr);
+                           cudaStream_t st, const uint32_t *d_out_idx = nullptr, void *d_scratch = nullptr,
+                           size_t scratch_bytes = 0);
 // The 64-bit blind rotation reading gate g's inputs at c1 + idx1[g] * (n+1)
 // and c2 + idx2[g] * (n+1) (index arrays optional), caller-supplied
 // accumulator scratch (bootstrap_accs_bytes); window = false takes no step

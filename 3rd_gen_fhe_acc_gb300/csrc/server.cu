@@ -208,7 +208,9 @@ struct Server {
         if (c->wide) {
             rc = launch_blind_rotate64_indexed(*c, d_pool, d_pool, i1, i2, gt, k, 0, (uint64_t *)L.d_accs, nullptr,
                                                (uint64_t *)L.d_ext, 0, false, L.st);
-            if (!rc) rc = launch_lwe_keyswitch64(*c, (const uint64_t *)L.d_ext, k, true, d_pool, L.st, io);
+            if (!rc)
+                rc = launch_lwe_keyswitch64(*c, (const uint64_t *)L.d_ext, k, true, d_pool, L.st, io, L.d_accs,
+                                            L.accs_bytes);
         } else {
             rc = launch_blind_rotate32_indexed(*c, d_pool, d_pool, i1, i2, gt, k, 0, (uint32_t *)L.d_accs,
                                                (uint32_t *)L.d_ext, L.st);

@@ -853,7 +853,7 @@ def main():
     return 0
 
 
-def measure_batch(F, D, cache, preset, B, args, dev_id, steps, plain_sample, serve):
+def measure_batch(F, D, cache, preset, B, args, dev_id, n_steps, plain_sample, serve):
     """One batched configuration: K timed steps on device-resident inputs, the
     e2e steps through the host-buffer C ABI, the plain form, the rooflines, a
     CPU sample and (serve) the serving sample; returns the JSON line."""
@@ -897,7 +897,7 @@ def measure_batch(F, D, cache, preset, B, args, dev_id, steps, plain_sample, ser
     D.barrier()
     torch.cuda.synchronize()
     n0 = ctx.kernel_launches()
-    for _ in range(steps):
+    for _ in range(n_steps):
         flush.fill_(1)
         e0, e1 = step_device(True)
         torch.cuda.synchronize()
@@ -910,7 +910,7 @@ def measure_batch(F, D, cache, preset, B, args, dev_id, steps, plain_sample, ser
     D.barrier()
     clk = clocks.stop()
     total_s = D.max(sum(step_ms) / 1e3)
-    value = D.ws * B * steps / total_s
+    value = D.ws * B * n_steps / total_s
     same = np.array_equal(dout.cpu().numpy().view(np.uint64), out0)
 
     # e2e: host buffers through the C ABI (pinned host memory)
@@ -920,7 +920,7 @@ def measure_batch(F, D, cache, preset, B, args, dev_id, steps, plain_sample, ser
     ho = torch.zeros_like(h1).pin_memory()
     n1, n2, ng, no = (t.numpy() for t in (h1, h2, hg, ho))
     e2e_s = []
-    for s in range(args.warmup + steps):
+    for s in range(args.warmup + n_steps):
         flush.fill_(1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -932,7 +932,7 @@ def measure_batch(F, D, cache, preset, B, args, dev_id, steps, plain_sample, ser
             e2e_s.append(dt)
     D.barrier()
     e2e_total = D.max(sum(e2e_s))
-    e2e_value = D.ws * B * steps / e2e_total
+    e2e_value = D.ws * B * n_steps / e2e_total
     e2e_same = np.array_equal(no.view(np.uint64), out0)
 
     # plain form: one launch sequence per gate
@@ -1059,7 +1059,7 @@ def measure_batch(F, D, cache, preset, B, args, dev_id, steps, plain_sample, ser
         print(json.dumps({"serving_sweep": sweep}))
 
     line = {
-        "metric": METRIC, "value": value, "unit": "bootstraps/s", "n_gpus": D.ws, "steps": steps,
+        "metric": METRIC, "value": value, "unit": "bootstraps/s", "n_gpus": D.ws, "steps": n_steps,
         "warmup": args.warmup, "ms_per_step": statistics.mean(step_ms), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32" if P.N == 1024 else "u64", "data": "synthetic",
         "config": config_of(P, B),

@@ -159,6 +159,23 @@ def test_wide_fpga_x1_mode(F, ctx1, keys1, pipes):
     assert np.array_equal(out, want)
 
 
+def test_wide_plain_equals_batched(F, ctx1, keys1, cuda_ok):
+    """The plain form at N = 2048 (one launch sequence per gate; each lone
+    gate's key switch split over many CTAs, 64-bit partial sums reduced mod
+    Q per CTA) gives the batched call's words."""
+    torch = cuda_ok
+    x, y, g, c1, c2 = random_gate_batch(keys1, 3, seed=51)
+    d1, d2 = dev(torch, c1), dev(torch, c2)
+    dg = torch.from_numpy(g).cuda()
+    ob, op = torch.zeros_like(d1), torch.zeros_like(d1)
+    ctx1.bootstrap_async(d1.data_ptr(), d2.data_ptr(), dg.data_ptr(), 3, ob.data_ptr())
+    ctx1.bootstrap_plain_async(d1.data_ptr(), d2.data_ptr(), dg.data_ptr(), 3, op.data_ptr())
+    ctx1.sync()
+    assert torch.equal(ob, op)
+    truth = np.array([F.gate_truth(int(a), b, c) for a, b, c in zip(g, x, y)], dtype=np.uint8)
+    assert np.array_equal(keys1.decrypt(host(op)), truth)
+
+
 @pytest.mark.parametrize("count", [20, 60])
 def test_wide_rlwe_mult_rgsw_batch(F, ctx1, keys1, cuda_ok, count):
     """One RGSW per product. 20 products (120 product-digit CTAs, at most two
