@@ -102,12 +102,11 @@ struct PipeSmem {
 };
 
 // Bytes of dynamic shared memory before the digit tables: one PipeSmem per
-// pipeline, then the residue table [group][n * digitR] and the issue order
-// [n * digitR][group], each rounded up to 16.
+// pipeline, then the residue table [group][n * digitR], rounded up to 16.
 template <int NB, int NP>
 __host__ __device__ constexpr size_t pipe_tables_offset(int group, size_t steps)
 {
-    return NP * sizeof(PipeSmem<NB>) + 2 * (((size_t)group * steps + 15) / 16 * 16);
+    return NP * sizeof(PipeSmem<NB>) + ((size_t)group * steps + 15) / 16 * 16;
 }
 
 __device__ __forceinline__ void load_btile(uint32_t (&x)[32], const uint32_t *src, int lane)
@@ -155,8 +154,7 @@ __device__ __forceinline__ void store_btile(uint32_t *dst, const uint32_t (&x)[3
 // none) and the step its ciphertext must have finished; [11] periods idled in
 // a row waiting for it. done[k]: last finished step of ciphertext k.
 __device__ __noinline__ void pipe_plan(const int *C, int *Nx, volatile int *done, int *cursor, const uint8_t *res,
-                                       const uint8_t *order, int m, int S, int mode, unsigned *status,
-                                       int idle_limit)
+                                       int m, int S, int mode, unsigned *status, int idle_limit)
 {
     // period t's inverse-NTT item moves to the digit warps
     Nx[2] = C[6] ? C[0] : -1;
@@ -172,7 +170,7 @@ __device__ __noinline__ void pipe_plan(const int *C, int *Nx, volatile int *done
                 Nx[5] = 1;
                 break;
             }
-            const int st = idx / m, k = order[idx];
+            const int st = idx / m, k = idx - st * m;
             if (step_issued(res + k * S, st, mode)) {
                 int prev = st - 1;
                 while (prev >= 0 && !step_issued(res + k * S, prev, mode)) prev--;
@@ -306,8 +304,6 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PipeSmem<GW> *pipes = reinterpret_cast<PipeSmem<GW> *>(smem_raw);
     uint8_t *res = smem_raw + NP * sizeof(PipeSmem<GW>);   // [group][n * digitR] residues
-    // [n * digitR][group]: the group's ciphertexts of each step, by residue
-    uint8_t *order = res + ((size_t)A.group * (A.n * A.digitR) + 15) / 16 * 16;
     __shared__ int done[kMaxGroup * NP];
     __shared__ int cursor;
     __shared__ unsigned long long claim_first;
@@ -319,17 +315,18 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
     const size_t rgsw_words = (size_t)DG * 4 * 1024;
     const int mode = issue_mode(A.flags);
 
-    // digit tables (ntt_fwd_1024_digit): t1 [BG], t23 [BG], t123 [BG]
-    const int BG = A.digit_tables ? 1 << A.bg_bits : 0;
+    // digit tables (ntt_fwd_1024_digit): t1, t23, t123, each [BG][copies]
+    const int cl = digit_table_copies_log2((int)A.bg_bits);
+    const int BGC = A.digit_tables ? (1 << A.bg_bits) << cl : 0;
     uint32_t *t1 = reinterpret_cast<uint32_t *>(smem_raw + pipe_tables_offset<GW, NP>(A.group, S));
-    uint2 *t23 = reinterpret_cast<uint2 *>(t1 + BG), *t123 = t23 + BG;
-    for (int y = threadIdx.x; y < BG; y += blockDim.x) {
-        const uint64_t Q = c.Q;
-        t1[y] = (uint32_t)((uint64_t)y * c.fw[1] % Q);
-        t23[y] = make_uint2((uint32_t)((uint64_t)y * c.fw[2] % Q), (uint32_t)((uint64_t)y * c.fw[3] % Q));
-        t123[y] = make_uint2((uint32_t)((uint64_t)y * A.w21 % Q), (uint32_t)((uint64_t)y * A.w31 % Q));
+    uint2 *t23 = reinterpret_cast<uint2 *>(t1 + BGC), *t123 = t23 + BGC;
+    for (int i = threadIdx.x; i < BGC; i += blockDim.x) {
+        const uint64_t Q = c.Q, y = (uint64_t)(i >> cl);
+        t1[i] = (uint32_t)(y * c.fw[1] % Q);
+        t23[i] = make_uint2((uint32_t)(y * c.fw[2] % Q), (uint32_t)(y * c.fw[3] % Q));
+        t123[i] = make_uint2((uint32_t)(y * A.w21 % Q), (uint32_t)(y * A.w31 % Q));
     }
-    const DigitTables dt{t1, t23, t123};
+    const DigitTables dt{t1, t23, t123, cl};
     __syncthreads();
 
     // each CTA claims A.group consecutive ciphertexts at a time until none are left
@@ -361,23 +358,11 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
             c0[11] = 0;                   // idle periods in a row
         }
         __syncthreads();
-        // issue order of each step: the group's ciphertexts by residue, so that
-        // items applying the same RGSW key follow one another and the later
-        // ones read it from L1 (the order within a step is free: every
-        // ciphertext still takes its own steps in the reference's order)
-        for (int st = threadIdx.x; st < S; st += blockDim.x) {
-            uint8_t *o = order + st * m;
-            int pos = 0;
-            for (uint32_t r = 0; r < A.Br; r++)
-                for (int k = 0; k < m; k++)
-                    if (res[k * S + st] == r) o[pos++] = (uint8_t)k;
-        }
-        __syncthreads();
 
         // ---- NP pipelines over the (step, ciphertext) items of the group. One
         // thread of each plans the pipeline's next period after each period
         // and publishes the plan in shared memory.
-        if (pw == 0 && lane == 0) pipe_plan(s.ctl[1], s.ctl[0], done, &cursor, res, order, m, S, mode, A.status, A.idle_limit);
+        if (pw == 0 && lane == 0) pipe_plan(s.ctl[1], s.ctl[0], done, &cursor, res, m, S, mode, A.status, A.idle_limit);
         pipe_barrier(1 + pl, PT);
         for (int t = 0;; t ^= 1) {
             const int *ctl = s.ctl[t];
@@ -407,7 +392,7 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
             // item once its digit NTTs are in shared memory; one thread first
             // plans the next period
             pipe_barrier(1 + pl, PT);
-            if (pw == 0 && lane == 0) pipe_plan(ctl, s.ctl[t ^ 1], done, &cursor, res, order, m, S, mode, A.status, A.idle_limit);
+            if (pw == 0 && lane == 0) pipe_plan(ctl, s.ctl[t ^ 1], done, &cursor, res, m, S, mode, A.status, A.idle_limit);
             if (ctl[3] >= 0) {
                 const int gk = ctl[3], gs = ctl[2];
                 const uint32_t rr = res[gk * S + gs];
@@ -449,12 +434,13 @@ static int launch_pipe_dg(Context &c, dev::PipeArgs A, int max_ctas, cudaStream_
     constexpr int GW = 2 * (DG - 1);
     constexpr int threads = NP * 32 * (GW + 2);
     auto kern = dev::br32_pipe_kernel<DG, NP, MINB>;
-    const size_t steps = (size_t)c.p.n * c.p.digitR, tables = A.digit_tables ? 20 * ((size_t)1 << c.p.BG_bits) : 0;
+    const size_t steps = (size_t)c.p.n * c.p.digitR;
+    const size_t tables = A.digit_tables ? (20 * ((size_t)1 << c.p.BG_bits)) << dev::digit_table_copies_log2((int)c.p.BG_bits) : 0;
     // group cap: kMaxGroup (or the tuned cap) per pipeline, within the shared memory of one CTA
     int cap = NP * (c.tune.br_group > 0 ? std::min(c.tune.br_group, dev::kMaxGroup) : dev::kMaxGroup);
-    const size_t fixed = dev::pipe_tables_offset<GW, NP>(0, steps) + tables + 32;
-    if (fixed + 2 * (size_t)cap * steps > kPipeSmemBudget)
-        cap = fixed < kPipeSmemBudget ? (int)((kPipeSmemBudget - fixed) / (2 * steps)) : 0;
+    const size_t fixed = dev::pipe_tables_offset<GW, NP>(0, steps) + tables + 16;
+    if (fixed + (size_t)cap * steps > kPipeSmemBudget)
+        cap = fixed < kPipeSmemBudget ? (int)((kPipeSmemBudget - fixed) / steps) : 0;
     if (cap < 1) return c.fail(FHEACC_EINVAL, "n * digitR too large for the blind rotation's residue table");
     // residency with the largest group allowed; the group is then fitted to the batch
     size_t smem = dev::pipe_tables_offset<GW, NP>(cap, steps) + tables;

@@ -177,18 +177,29 @@ constexpr int kKsTileGroups = 2;   // row groups per stage (one barrier per stag
 
 struct KsTiledArgs {
     KsArgs k;
-    const uint8_t *digits;   // [(i * digitKS + j)][gstride]: digit j of a[i] of each gate
-    size_t gstride;          // gates per digit row (a multiple of the gate block, padded with zeros)
+    const uint8_t *digits;   // [(i * digitKS + j)][gstride]: digit j of a[i] of each gate (ks_digit_slot)
+    size_t gstride;          // bytes per digit row: 128 per gate block
     int slices;              // column slices of kKsTileCols words
 };
 
-// digits[(i * D + j) * gstride + g] = (a_i / Bks^j) mod Bks of gate g (0 for
-// gates >= count). A CTA of 32 x 8 threads handles 32 gates x 32
-// coefficients: the extracted words are read row-wise (coalesced), transposed
-// in shared memory, and each digit row is written 32 gates at a time.
+// The digits of a gate block as the tiled kernel reads them: warp w of the
+// block owns gates w GW .. w GW + GW - 1 and their digits of one row group sit
+// in the warp's 8-byte slot, so a block's digits of a row group are 128 bytes
+// (16 warps x 8) and a warp reads its own in one aligned 64-bit load.
+__host__ __device__ __forceinline__ size_t ks_digit_slot(size_t g, int GW)
+{
+    const size_t G = (size_t)kKsTileWarps * GW, b = g / G, r = g - b * G;
+    return b * (kKsTileWarps * 8) + (r / GW) * 8 + r % GW;
+}
+
+// digits[(i * D + j) * gstride + slot(g)] = (a_i / Bks^j) mod Bks of gate g
+// (0 for the gates >= count of the last block). A CTA of 32 x 8 threads
+// handles 32 gates x 32 coefficients: the extracted words are read row-wise
+// (coalesced), transposed in shared memory, and each digit row is written 32
+// gates at a time.
 __global__ void __launch_bounds__(256) ks_digits_kernel(const uint32_t *__restrict__ ext, size_t count,
-                                                        uint8_t *__restrict__ digits, size_t gstride, int D,
-                                                        uint32_t Bks)
+                                                        size_t padded, uint8_t *__restrict__ digits, size_t gstride,
+                                                        int D, uint32_t Bks, int GW)
 {
     __shared__ uint32_t tile[32][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
@@ -200,12 +211,14 @@ __global__ void __launch_bounds__(256) ks_digits_kernel(const uint32_t *__restri
         tile[ty + 8 * r][tx] = g < count ? ext[g * kExtractStride + i0 + tx] : 0u;
     }
     __syncthreads();
-    if (g0 + tx >= gstride) return;
+    const size_t g = g0 + tx;
+    if (g >= padded) return;
+    const size_t slot = ks_digit_slot(g, GW);
 #pragma unroll
     for (int r = 0; r < 4; r++) {
         const int ci = ty + 8 * r;
         uint32_t a = tile[tx][ci];
-        uint8_t *dst = digits + (size_t)(i0 + ci) * D * gstride + g0 + tx;
+        uint8_t *dst = digits + (size_t)(i0 + ci) * D * gstride + slot;
         for (int j = 0; j < D; j++) {
             dst[(size_t)j * gstride] = (uint8_t)(a % Bks);
             a /= Bks;
@@ -222,110 +235,101 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int PENDING>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory"); }
 
-// Digits of a warp's GW gates (GW = 1, 2, 4 or 8 bytes, naturally aligned) in
-// one shared-memory load.
-template <int GW>
-__device__ __forceinline__ uint64_t load_digits(const uint8_t *p)
-{
-    if (GW == 8) return *reinterpret_cast<const uint64_t *>(p);
-    if (GW == 4) return *reinterpret_cast<const uint32_t *>(p);
-    if (GW == 2) return *reinterpret_cast<const uint16_t *>(p);
-    return *p;
-}
-
-// CTA (gate block b, column slice s): gates [b G, b G + G), G = 16 GW, key
-// words [s 128, s 128 + 128). The row groups are walked kKsTileGroups at a
-// time: a stage of the ring holds that many groups' Bks row slices ([Bks][128]
-// words each) and the block's G digits of each group. Every thread copies the
-// same chunks of every stage, so their offsets are worked out once; only the
-// stage's base addresses move. Warp w owns gates w GW .. w GW + GW - 1 and
-// lane l the words 4 l .. 4 l + 3 of the slice: per row group it reads its
-// gates' digits in one load and adds, for each gate, the row slice the digit
-// selects (one 128-bit shared load; all lanes read one row, so a warp's load
-// is 512 contiguous bytes, free of bank conflicts). Sums stay below 32 Q <
-// 2^32 with a conditional subtraction of 16 Q every 16 row groups (rows are
-// canonical, Q < 2^27).
+// CTA (gate block b, column slice s): gates [b G, b G + G), G = 16 GW (GW <=
+// 8), key words [s 128, s 128 + 128). The row groups are walked kKsTileGroups
+// at a time: a stage of the ring holds that many groups' Bks row slices
+// ([Bks][128] words each) and the block's 128 digit bytes of each group. Every
+// thread copies the same chunks of every stage; their source addresses move
+// by a per-group offset that is advanced, not recomputed. Warp w owns gates
+// w GW .. w GW + GW - 1 and lane l the words 4 l .. 4 l + 3 of the slice: per
+// row group it reads its digit slot in one 64-bit load and adds, for each of
+// its gates, the row slice the digit selects (one 128-bit shared load; all
+// lanes read one row, so a warp's load is 512 contiguous bytes, free of bank
+// conflicts). Sums stay below 32 Q < 2^32 with a conditional subtraction of
+// 16 Q every 16 row groups (rows are canonical, Q < 2^27).
 template <int GW>
 __global__ void __launch_bounds__(kKsTileWarps * 32, 1) lwe_ks32_tiled_kernel(const __grid_constant__ KsTiledArgs T)
 {
     extern __shared__ __align__(16) uint32_t ring[];
-    constexpr int G = kKsTileWarps * GW, R = kKsTileGroups;
+    constexpr int R = kKsTileGroups;
     constexpr int kMaxChunks = 4;   // chunks of a stage per thread (checked by the launcher)
+    constexpr int kDigitWords = kKsTileWarps * 8 / 4;
     const KsArgs &A = T.k;
     const int N = A.N, D = A.digitKS, Bks = (int)A.Bks, n = A.n;
-    const int group_words = Bks * kKsTileCols + G / 4;   // row slices, then digits
+    const int group_words = Bks * kKsTileCols + kDigitWords;   // row slices, then digit slots
     const int group_chunks = group_words / 4, rows_chunks = Bks * (kKsTileCols / 4);
     const int stage_words = R * group_words;
     const int slice = blockIdx.x % T.slices;
-    const size_t g0 = (size_t)(blockIdx.x / T.slices) * G;
+    const size_t gb = blockIdx.x / T.slices;
+    const size_t g0 = gb * (kKsTileWarps * GW);
     const int c0 = slice * kKsTileCols;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t Q = (uint32_t)A.Q, Q16 = 16 * Q;
     const int total = N * D;
     const size_t row_stride = (size_t)D * N * A.ks_row;   // words between digits d and d + 1
 
-    // this thread's chunks: group r of the stage, source offset from that
-    // group's base (rows: kskey row (d, j, i) slice; digits: the block's bytes),
+    // this thread's chunks: their group of the stage, source pointer for stage
+    // 0 (rows: kskey row (d, j, i) slice; digits: the block's slots) and
     // destination word in the stage
-    int ch_group[kMaxChunks], ch_dst[kMaxChunks];
-    size_t ch_off[kMaxChunks];
-    bool ch_digit[kMaxChunks];
-    int nch = 0;
+    const char *src[kMaxChunks];
+    int dst[kMaxChunks], grp[kMaxChunks];
+    bool dig[kMaxChunks];
 #pragma unroll
     for (int u = 0; u < kMaxChunks; u++) {
         const int c = threadIdx.x + u * (int)blockDim.x;
-        ch_group[u] = -1;
-        ch_off[u] = 0;
-        ch_dst[u] = 0;
-        ch_digit[u] = false;
+        src[u] = nullptr;
+        dst[u] = 0;
+        grp[u] = -1;
+        dig[u] = false;
         if (c < R * group_chunks) {
             const int r = c / group_chunks, cc = c - r * group_chunks;
-            ch_group[u] = r;
-            ch_dst[u] = r * group_words + 4 * cc;
+            grp[u] = r;
+            dst[u] = r * group_words + 4 * cc;
+            // row group r of stage 0: (i, j) = (r / D, r % D)
+            const int i = r / D, j = r - (r / D) * D;
             if (cc < rows_chunks) {
-                ch_off[u] = (size_t)(cc >> 5) * row_stride + 4 * (cc & 31);
+                src[u] = reinterpret_cast<const char *>(A.kskey + ((size_t)j * N + i) * A.ks_row + c0 +
+                                                        (size_t)(cc >> 5) * row_stride + 4 * (cc & 31));
             } else {
-                ch_digit[u] = true;
-                ch_off[u] = g0 + 16 * (size_t)(cc - rows_chunks);
+                dig[u] = true;
+                src[u] = reinterpret_cast<const char *>(T.digits + (size_t)r * T.gstride + gb * (kKsTileWarps * 8) +
+                                                        16 * (cc - rows_chunks));
             }
-            nch = u + 1;
         }
     }
-    // coefficient and digit of the next group to fetch
-    int fi = 0, fj = 0, fetched = 0;
+    // per group of the next stage to fetch: its (i, j), to advance the row offsets
+    int gi[R], gj[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+        gi[r] = r / D;
+        gj[r] = r - gi[r] * D;
+    }
+    int fetched = 0;   // row groups issued so far
     auto issue_stage = [&]() {
-        uint32_t *dst = ring + ((fetched / R) % kKsTileStages) * stage_words;
-        size_t rows_base[R], dig_base[R];
-        bool valid[R];
+        uint32_t *ring_stage = ring + ((fetched / R) % kKsTileStages) * stage_words;
+#pragma unroll
+        for (int u = 0; u < kMaxChunks; u++)
+            if (grp[u] >= 0 && fetched + grp[u] < total) cp_async16(ring_stage + dst[u], src[u]);
+        // advance every group by R row groups: the rows by the change of (i, j),
+        // the digits by R rows of slots
+        long long drow[R];
 #pragma unroll
         for (int r = 0; r < R; r++) {
-            valid[r] = fetched + r < total;
-            rows_base[r] = ((size_t)fj * N + fi) * A.ks_row + c0;
-            dig_base[r] = (size_t)(fetched + r) * T.gstride;
-            if (++fj == D) {
-                fj = 0;
-                ++fi;
+            const long long before = (long long)gj[r] * N + gi[r];
+            gj[r] += R;
+            while (gj[r] >= D) {
+                gj[r] -= D;
+                gi[r]++;
             }
+            drow[r] = ((long long)gj[r] * N + gi[r] - before) * (long long)A.ks_row * 4;
         }
 #pragma unroll
         for (int u = 0; u < kMaxChunks; u++) {
-            if (u < nch) {
-                // the chunk's group (selects, not an indexed local array)
-                size_t rb = rows_base[0], db = dig_base[0];
-                bool v = valid[0];
+            long long d = dig[u] ? (long long)R * (long long)T.gstride : 0;
 #pragma unroll
-                for (int r = 1; r < R; r++)
-                    if (ch_group[u] == r) {
-                        rb = rows_base[r];
-                        db = dig_base[r];
-                        v = valid[r];
-                    }
-                if (v) {
-                    const void *src = ch_digit[u] ? (const void *)(T.digits + db + ch_off[u])
-                                                  : (const void *)(A.kskey + rb + ch_off[u]);
-                    cp_async16(dst + ch_dst[u], src);
-                }
-            }
+            for (int r = 0; r < R; r++)
+                if (!dig[u] && grp[u] == r) d = drow[r];
+            src[u] += d;
         }
         fetched += R;
     };
@@ -349,13 +353,12 @@ __global__ void __launch_bounds__(kKsTileWarps * 32, 1) lwe_ks32_tiled_kernel(co
 #pragma unroll
         for (int r = 0; r < R; r++) {
             if (rg + r < total) {
-                const uint32_t *grp = st + r * group_words;
-                const uint64_t dg =
-                    load_digits<GW>(reinterpret_cast<const uint8_t *>(grp + Bks * kKsTileCols) + warp * GW);
-                const uint4 *rows4 = reinterpret_cast<const uint4 *>(grp);
+                const uint32_t *grp_w = st + r * group_words;
+                const uint2 dg2 = reinterpret_cast<const uint2 *>(grp_w + Bks * kKsTileCols)[warp];
+                const uint4 *rows4 = reinterpret_cast<const uint4 *>(grp_w);
 #pragma unroll
                 for (int k = 0; k < GW; k++) {
-                    const uint32_t d = (uint32_t)(dg >> (8 * k)) & 0xFFu;
+                    const uint32_t d = ((k < 4 ? dg2.x : dg2.y) >> (8 * (k & 3))) & 0xFFu;
                     const uint4 v = rows4[d * (kKsTileCols / 4) + lane];
                     acc[k][0] += v.x;
                     acc[k][1] += v.y;
@@ -414,24 +417,23 @@ static int launch_ks_tiled_gw(Context &c, const dev::KsTiledArgs &T, size_t bloc
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "tiled key switch launch");
 }
 
-// Gates per warp of the tiled form (1, 2, 4 or 8: a warp's digits are one
-// aligned load): gate blocks of 16 GW gates, the smallest GW with which the
-// blocks times the column slices fit on the SMs.
+// Gates per warp of the tiled form (1..8, the bytes of a warp's digit slot):
+// gate blocks of 16 GW gates, the smallest GW with which the blocks times the
+// column slices fit on the SMs (4096 gates: 7, 37 blocks x 4 slices = 148 CTAs).
 static int ks_tiled_gw(size_t count, int sms, int slices)
 {
     const size_t blocks_target = std::max<size_t>(1, (size_t)sms / slices);
     const size_t per_warp = ((count + blocks_target - 1) / blocks_target + dev::kKsTileWarps - 1) / dev::kKsTileWarps;
-    int gw = 1;
-    while (gw < 8 && (size_t)gw < per_warp) gw *= 2;
-    return gw;
+    return (int)std::min<size_t>(8, std::max<size_t>(1, per_warp));
 }
 
-// Scratch bytes the tiled key switch of `count` gates needs for its digits.
+// Scratch bytes the tiled key switch of `count` gates needs for its digits:
+// 128 slot bytes per gate block and row group.
 static size_t ks_tiled_digit_bytes(const Context &c, size_t count, int sms)
 {
     const int slices = (int)(c.dp.ks_row / dev::kKsTileCols);
     const size_t G = (size_t)dev::kKsTileWarps * ks_tiled_gw(count, sms, std::max(slices, 1));
-    return (count + G - 1) / G * G * (size_t)c.p.N * c.p.digitKS;
+    return (count + G - 1) / G * (dev::kKsTileWarps * 8) * (size_t)c.p.N * c.p.digitKS;
 }
 
 static bool ks_tiled_applies(const Context &c, size_t count, int sms, size_t scratch_bytes)
@@ -450,24 +452,30 @@ static int launch_ks_tiled(Context &c, const dev::KsArgs &A, void *scratch, int 
 {
     const int slices = (int)(c.dp.ks_row / dev::kKsTileCols);
     const int GW = ks_tiled_gw(A.count, sms, slices);
-    const size_t G = (size_t)dev::kKsTileWarps * GW;
+    const size_t G = (size_t)dev::kKsTileWarps * GW, nblocks = (A.count + G - 1) / G;
     dev::KsTiledArgs T{};
     T.k = A;
     T.digits = (const uint8_t *)scratch;
-    T.gstride = (A.count + G - 1) / G * G;
+    T.gstride = nblocks * (dev::kKsTileWarps * 8);
     T.slices = slices;
-    dim3 dgrid((unsigned)((T.gstride + 31) / 32), (unsigned)(c.p.N / 32));
-    dev::ks_digits_kernel<<<dgrid, 256, 0, st>>>(A.ext, A.count, (uint8_t *)scratch, T.gstride, A.digitKS, A.Bks);
+    const size_t padded = nblocks * G;
+    dim3 dgrid((unsigned)((padded + 31) / 32), (unsigned)(c.p.N / 32));
+    dev::ks_digits_kernel<<<dgrid, 256, 0, st>>>(A.ext, A.count, padded, (uint8_t *)scratch, T.gstride,
+                                                 A.digitKS, A.Bks, GW);
     c.launches++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return c.cuda_fail(e, "key-switch digits launch");
-    const size_t blocks = T.gstride / G * slices;
+    const size_t blocks = nblocks * slices;
     const size_t smem = (size_t)dev::kKsTileStages * dev::kKsTileGroups *
-                        ((size_t)c.p.Bks * dev::kKsTileCols + G / 4) * sizeof(uint32_t);
+                        ((size_t)c.p.Bks * dev::kKsTileCols + dev::kKsTileWarps * 2) * sizeof(uint32_t);
     switch (GW) {
     case 1: return launch_ks_tiled_gw<1>(c, T, blocks, smem, st);
     case 2: return launch_ks_tiled_gw<2>(c, T, blocks, smem, st);
+    case 3: return launch_ks_tiled_gw<3>(c, T, blocks, smem, st);
     case 4: return launch_ks_tiled_gw<4>(c, T, blocks, smem, st);
+    case 5: return launch_ks_tiled_gw<5>(c, T, blocks, smem, st);
+    case 6: return launch_ks_tiled_gw<6>(c, T, blocks, smem, st);
+    case 7: return launch_ks_tiled_gw<7>(c, T, blocks, smem, st);
     default: return launch_ks_tiled_gw<8>(c, T, blocks, smem, st);
     }
 }

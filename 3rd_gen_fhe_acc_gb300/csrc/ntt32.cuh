@@ -221,11 +221,20 @@ __device__ __forceinline__ void ntt_fwd_1024(uint32_t (&x)[32], const Ntt32Const
 // forward stages, which are the same for every lane: w1 = rou[1] (stage t =
 // 512), w2 = rou[2] and w3 = rou[3] (stage t = 256). The tables hold, for
 // y < BG:  t1[y] = y w1,  t23[y] = (y w2, y w3),  t123[y] = (y w2 w1, y w3 w1),
-// all canonical mod Q.
+// all canonical mod Q. Each table is held in 2^copies_log2 copies, entry y of
+// copy k at [(y << copies_log2) + k], and lane l reads copy l mod 2^copies_log2:
+// with 16 copies the digits of a warp (random 7-bit values) hit distinct banks
+// in the 64-bit tables and at most two lanes share a bank in t1, instead of
+// several lanes per bank for a single copy.
 struct DigitTables {
     const uint32_t *t1;
     const uint2 *t23, *t123;
+    int copies_log2;
 };
+
+// Copies of the digit tables a gadget base of 2^bg_bits gets (shared memory
+// 20 BG bytes per copy: 16 copies up to BG = 128).
+__host__ __device__ constexpr int digit_table_copies_log2(int bg_bits) { return bg_bits <= 7 ? 4 : 0; }
 
 // Forward NTT of a digit polynomial: x in layout A with values < BG -> layout
 // B, values < 19Q + BG, same result mod Q as ntt_fwd_1024. The first two
@@ -241,11 +250,12 @@ __device__ __forceinline__ void ntt_fwd_1024_digit(uint32_t (&x)[32], const Ntt3
                                                    const uint2 *__restrict__ fwd_tw, uint32_t *buf,
                                                    const DigitTables &T, int lane)
 {
+    const int cl = T.copies_log2, cp = lane & ((1 << cl) - 1);
 #pragma unroll
     for (int r = 0; r < 8; r++) {
         const uint32_t x0 = x[r], x1 = x[r + 8], x2 = x[r + 16], x3 = x[r + 24];
-        const uint32_t a = T.t1[x2];
-        const uint2 bd = T.t23[x1], ce = T.t123[x3];
+        const uint32_t a = T.t1[(x2 << cl) + cp];
+        const uint2 bd = T.t23[(x1 << cl) + cp], ce = T.t123[(x3 << cl) + cp];
         x[r] = x0 + a + bd.x + ce.x;
         x[r + 8] = x0 + a + (c.twoQ - bd.x - ce.x);
         x[r + 16] = x0 + (c.twoQ - a - ce.y) + bd.y;

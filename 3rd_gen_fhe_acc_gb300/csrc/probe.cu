@@ -46,16 +46,17 @@ __global__ void __launch_bounds__(320, 2) ntt_rate_kernel(uint32_t *sink, int it
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     uint32_t *bufs = reinterpret_cast<uint32_t *>(smem_raw);   // [10][1024]
-    const int BG = 1 << bg_bits;
+    const int BG = 1 << bg_bits, cl = digit_table_copies_log2(bg_bits), BGC = BG << cl;
     uint32_t *t1 = bufs + 10 * kN32;
-    uint2 *t23 = reinterpret_cast<uint2 *>(t1 + BG), *t123 = t23 + BG;
-    for (int y = threadIdx.x; y < BG; y += blockDim.x) {
-        t1[y] = (uint32_t)((uint64_t)y * c.fw[1] % c.Q);
-        t23[y] = make_uint2((uint32_t)((uint64_t)y * c.fw[2] % c.Q), (uint32_t)((uint64_t)y * c.fw[3] % c.Q));
-        t123[y] = make_uint2(t1[y], t23[y].x);
+    uint2 *t23 = reinterpret_cast<uint2 *>(t1 + BGC), *t123 = t23 + BGC;
+    for (int i = threadIdx.x; i < BGC; i += blockDim.x) {
+        const uint64_t y = (uint64_t)(i >> cl);
+        t1[i] = (uint32_t)(y * c.fw[1] % c.Q);
+        t23[i] = make_uint2((uint32_t)(y * c.fw[2] % c.Q), (uint32_t)(y * c.fw[3] % c.Q));
+        t123[i] = make_uint2(t1[i], t23[i].x);
     }
     __syncthreads();
-    const DigitTables dt{t1, t23, t123};
+    const DigitTables dt{t1, t23, t123, cl};
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     uint32_t *buf = bufs + warp * kN32;
     uint32_t x[32];
@@ -234,7 +235,7 @@ int measure_components(Context &c, double ns[4])
     // blind rotation does); above that it is the plain forward NTT
     const bool tables = c.p.BG_bits <= 9;
     const int bg = tables ? (int)c.p.BG_bits : 1;
-    const size_t smem = 10 * dev::kN32 * sizeof(uint32_t) + 20 * ((size_t)1 << bg);
+    const size_t smem = 10 * dev::kN32 * sizeof(uint32_t) + ((20 * ((size_t)1 << bg)) << dev::digit_table_copies_log2(bg));
     float ms[4] = {0, 0, 0, 0};
     int rc = FHEACC_OK;
     auto k0 = dev::ntt_rate_kernel<0>, k1 = dev::ntt_rate_kernel<1>, k2 = dev::ntt_rate_kernel<2>;

@@ -108,13 +108,14 @@ def test_gpu_fixed_width_calls(F, ctx0, keys0):
     assert out is None and rc == -1
 
 
-@pytest.mark.parametrize("count", [40, 333, 1100])
+@pytest.mark.parametrize("count", [40, 333, 1100, 2600])
 def test_tiled_keyswitch_equals_per_gate(F, ctx0, keys0, cuda_ok, count):
     """The tiled LWE key switch (gate blocks sharing each key row group through
     shared memory; batches from 1024 gates take it by default) against the
     one-CTA-per-gate kernel on the same blind-rotation outputs: forced on small
     batches, with a partial last gate block (40, 333: 16 gates per block) and
-    two gates per warp (1100); the first gates also against the oracle."""
+    two and five gates per warp (1100, 2600); the first gates also against the
+    oracle."""
     torch = cuda_ok
     x, y, g, c1, c2 = random_gate_batch(keys0, count, seed=81 + count)
     d1 = torch.from_numpy(c1.view(np.int64)).cuda()
