@@ -53,8 +53,10 @@ __device__ __forceinline__ void mac_chunk(int u, const uint4 *__restrict__ key,
         const int pp = qi / DG, hh = qi % DG;
         const uint4 dv = (DERIVE && hh == DG - 1) ? __ldcg(acc_nd + pp * 256 + u)
                                                   : *reinterpret_cast<const uint4 *>(dbuf[pp * DT + hh] + pa);
-        const uint4 a4 = __ldg(key + ((hh * 2 + pp) * 2 + 0) * 256 + u);
-        const uint4 b4 = __ldg(key + ((hh * 2 + pp) * 2 + 1) * 256 + u);
+        // keys stream through L2 only: an item's 64 KB would otherwise evict
+        // the transforms' twiddle tables from the L1 left beside shared memory
+        const uint4 a4 = __ldcg(key + ((hh * 2 + pp) * 2 + 0) * 256 + u);
+        const uint4 b4 = __ldcg(key + ((hh * 2 + pp) * 2 + 1) * 256 + u);
         sa[0] += (uint64_t)dv.x * a4.x; sb[0] += (uint64_t)dv.x * b4.x;
         sa[1] += (uint64_t)dv.y * a4.y; sb[1] += (uint64_t)dv.y * b4.y;
         sa[2] += (uint64_t)dv.z * a4.z; sb[2] += (uint64_t)dv.z * b4.z;
