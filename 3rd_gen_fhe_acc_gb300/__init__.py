@@ -36,6 +36,7 @@ OPT_BR_PIPES = 5
 OPT_BR_POOL = 6
 OPT_DEBUG_WAIT_LIMIT = 7
 OPT_KS_TILED = 8
+OPT_BR_SOLO = 9
 GRAPH_CONCURRENT = 1
 STATUS_WAIT_LIMIT = 1
 KIND_LWE_SK, KIND_RLWE_SK, KIND_BOOTSTRAP_KEY, KIND_LWE_KS_KEY, KIND_SUBS_KEY, KIND_LWE_CT, KIND_RLWE_CT, \

@@ -757,6 +757,10 @@ int fheacc_set_option(fheacc_ctx *ctx, int option, int value)
     case FHEACC_OPT_KS_TILED:
         c.tune.ks_tiled = value < 0 ? -1 : value ? 1 : 0;
         return FHEACC_OK;
+    case FHEACC_OPT_BR_SOLO:
+        if (value < -1 || value > 64) return c.fail(FHEACC_EINVAL, "latency-form gates per SM must be -1..64");
+        c.tune.br_solo = value;
+        return FHEACC_OK;
     case FHEACC_OPT_DEBUG_WAIT_LIMIT:
         if (value < -1) return c.fail(FHEACC_EINVAL, "wait limit must be -1 (built-in) or >= 0");
         c.tune.debug_wait_limit = value;

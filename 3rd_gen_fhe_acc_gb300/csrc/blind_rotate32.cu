@@ -419,6 +419,272 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
     }
 }
 
+// ---- Latency form: one ciphertext per CTA, keys prefetched into shared memory.
+//
+// Below one ciphertext per SM the pipelines above have nothing to overlap: a
+// lone ciphertext's steps are a serial chain, and each step waits for its 64 KB
+// key from DRAM and for its accumulator's round trip through L2. This kernel
+// keeps the accumulator in shared memory and streams the keys of the next two
+// issued steps into two shared-memory buffers with bulk asynchronous copies
+// (cp.async.bulk, completion counted in bytes on an mbarrier), so a step is
+// the three transform phases and nothing else:
+//   inverse-NTT warps (2): acc (NTT domain) -> inverse NTT -> tslot
+//   digit warps (2 (digitG - 1)): digits of tslot -> digit NTTs -> dbuf
+//   all warps: wait for the step's key buffer, multiply-accumulate -> acc
+// The arithmetic is the pipelines' (same transforms, same 64-bit sums and
+// Montgomery reduction), so the outputs are identical word for word.
+
+// Polls of an mbarrier before a key wait gives up and flags the launch (the
+// copy of one key takes microseconds).
+constexpr int kSoloWaitLimit = 1 << 22;
+
+// Digit-table copies of the latency form (8 up to BG = 128: the twiddle
+// copies take the shared memory of the other 8).
+__host__ __device__ constexpr int solo_table_copies_log2(int bg_bits) { return bg_bits <= 7 ? 3 : 0; }
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bulk copy of `bytes` (a multiple of 16, both addresses 16-byte aligned) from
+// global to shared memory, counted on `bar`.
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(__cvta_generic_to_global(src)), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Waits for phase `parity` of `bar`; false if it did not complete within
+// `limit` polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity, int limit)
+{
+    for (int i = 0; i < limit; i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// Next issued step after step s (S if none).
+__device__ __forceinline__ int solo_next_step(const uint8_t *res, int s, int S, int mode)
+{
+    for (s++; s < S; s++)
+        if (step_issued(res, s, mode)) return s;
+    return S;
+}
+
+// Multiply-accumulate of chunk u (the elements of mac_chunk) from shared
+// memory: the key buffer keeps the global B-tiled order, the accumulator and
+// the digit NTTs are swizzled rows. Reads both accumulator chunks before
+// writing them.
+template <int DG>
+__device__ __forceinline__ void mac_chunk_solo(int u, const uint4 *key, const uint32_t (*dbuf)[kN32],
+                                               uint32_t (*acc)[kN32], uint32_t Q, uint32_t qinv_neg)
+{
+    constexpr int DT = DG - 1;
+    const int pa = sw_chunk(u & 31, u >> 5);
+    uint64_t sa[4] = {0, 0, 0, 0}, sb[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int qi = 0; qi < 2 * DG; qi++) {
+        const int pp = qi / DG, hh = qi % DG;
+        const uint4 dv = hh == DG - 1 ? *reinterpret_cast<const uint4 *>(acc[pp] + pa)
+                                      : *reinterpret_cast<const uint4 *>(dbuf[pp * DT + hh] + pa);
+        const uint4 a4 = key[((hh * 2 + pp) * 2 + 0) * 256 + u];
+        const uint4 b4 = key[((hh * 2 + pp) * 2 + 1) * 256 + u];
+        sa[0] += (uint64_t)dv.x * a4.x; sb[0] += (uint64_t)dv.x * b4.x;
+        sa[1] += (uint64_t)dv.y * a4.y; sb[1] += (uint64_t)dv.y * b4.y;
+        sa[2] += (uint64_t)dv.z * a4.z; sb[2] += (uint64_t)dv.z * b4.z;
+        sa[3] += (uint64_t)dv.w * a4.w; sb[3] += (uint64_t)dv.w * b4.w;
+    }
+    *reinterpret_cast<uint4 *>(acc[0] + pa) =
+        make_uint4(mont_reduce_2q(sa[0], Q, qinv_neg), mont_reduce_2q(sa[1], Q, qinv_neg),
+                   mont_reduce_2q(sa[2], Q, qinv_neg), mont_reduce_2q(sa[3], Q, qinv_neg));
+    *reinterpret_cast<uint4 *>(acc[1] + pa) =
+        make_uint4(mont_reduce_2q(sb[0], Q, qinv_neg), mont_reduce_2q(sb[1], Q, qinv_neg),
+                   mont_reduce_2q(sb[2], Q, qinv_neg), mont_reduce_2q(sb[3], Q, qinv_neg));
+}
+
+// Shared memory of a latency-form CTA: two key buffers, then the accumulator,
+// the time-domain polys, the digit NTTs, copies of the forward and inverse
+// twiddle tables, the digit tables and the residues. The twiddles are copied
+// because L1 does not keep them from one step to the next here: read through
+// L1, the first forward NTT of a step took 6000 cycles instead of 2300, each
+// of its five per-lane-twiddle stages waiting on L2.
+template <int DG>
+struct SoloLayout {
+    static constexpr int GW = 2 * (DG - 1);
+    static constexpr size_t key_bytes = (size_t)DG * 4 * kN32 * sizeof(uint32_t);
+    static constexpr size_t acc_off = 2 * key_bytes;
+    static constexpr size_t ts_off = acc_off + 2 * kN32 * sizeof(uint32_t);
+    static constexpr size_t dbuf_off = ts_off + 2 * kN32 * sizeof(uint32_t);
+    static constexpr size_t tw_off = dbuf_off + (size_t)GW * kN32 * sizeof(uint32_t);   // [fwd, inv][1024] uint2
+    static constexpr size_t tables_off = tw_off + 2 * kN32 * sizeof(uint2);
+    static size_t __host__ __device__ res_off(size_t tables) { return tables_off + (tables + 15) / 16 * 16; }
+    static size_t __host__ __device__ bytes(size_t tables, size_t steps) { return res_off(tables) + (steps + 15) / 16 * 16; }
+};
+
+template <int DG>
+__global__ void __launch_bounds__(32 * 2 * DG, 1)
+    br32_solo_kernel(const __grid_constant__ PipeArgs A, const __grid_constant__ Ntt32Consts c,
+                     const uint2 *__restrict__ fwd_tw, const uint2 *__restrict__ inv_tw, uint32_t mu32)
+{
+    using L = SoloLayout<DG>;
+    constexpr int DT = DG - 1, GW = L::GW, NW = GW + 2, PT = 32 * NW;
+    extern __shared__ __align__(16) unsigned char solo_smem[];
+    __shared__ __align__(8) uint64_t bars[2];
+    uint32_t(*acc)[kN32] = reinterpret_cast<uint32_t(*)[kN32]>(solo_smem + L::acc_off);
+    uint32_t(*ts)[kN32] = reinterpret_cast<uint32_t(*)[kN32]>(solo_smem + L::ts_off);
+    uint32_t(*dbuf)[kN32] = reinterpret_cast<uint32_t(*)[kN32]>(solo_smem + L::dbuf_off);
+    uint2 *ftw = reinterpret_cast<uint2 *>(solo_smem + L::tw_off), *itw = ftw + kN32;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int S = A.n * (int)A.digitR;
+    const int mode = issue_mode(A.flags);
+    const size_t rgsw_words = (size_t)DG * 4 * kN32;
+
+    for (int i = threadIdx.x; i < kN32; i += blockDim.x) {
+        ftw[i] = __ldg(fwd_tw + i);
+        itw[i] = __ldg(inv_tw + i);
+    }
+    const int cl = solo_table_copies_log2((int)A.bg_bits);
+    const int BGC = A.digit_tables ? (1 << A.bg_bits) << cl : 0;
+    uint32_t *t1 = reinterpret_cast<uint32_t *>(solo_smem + L::tables_off);
+    uint2 *t23 = reinterpret_cast<uint2 *>(t1 + BGC), *t123 = t23 + BGC;
+    uint8_t *res = solo_smem + L::res_off((size_t)(20 * BGC));
+    for (int i = threadIdx.x; i < BGC; i += blockDim.x) {
+        const uint64_t Q = c.Q, y = (uint64_t)(i >> cl);
+        t1[i] = (uint32_t)(y * c.fw[1] % Q);
+        t23[i] = make_uint2((uint32_t)(y * c.fw[2] % Q), (uint32_t)(y * c.fw[3] % Q));
+        t123[i] = make_uint2((uint32_t)(y * A.w21 % Q), (uint32_t)(y * A.w31 % Q));
+    }
+    const DigitTables dt{t1, t23, t123, cl};
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    // bit b of parity: phase of bars[b] the next wait expects; of pending: a
+    // copy into buffer b not yet waited for (thread 0, which issues the copies,
+    // keeps the authoritative view)
+    unsigned parity = 0, pending = 0;
+
+    // the key of step s (residue res[s]) into buffer b
+    auto fetch = [&](int s, int b) {
+        pending |= 1u << b;
+        const uint32_t *src = A.btkey + ((size_t)s * A.Br + res[s]) * rgsw_words;
+        mbar_expect_tx(&bars[b], (unsigned)L::key_bytes);
+#pragma unroll
+        for (int h = 0; h < DG; h++)
+            bulk_copy_g2s(solo_smem + b * L::key_bytes + h * (L::key_bytes / DG),
+                          src + h * (rgsw_words / DG), (unsigned)(L::key_bytes / DG), &bars[b]);
+    };
+
+    for (size_t gid = blockIdx.x; gid < A.count; gid += gridDim.x) {
+        // ---- LWE_evaluate, residues and the initial accumulator (global, B-tiled)
+        if (warp == 0) pipe_init_item(A, c, fwd_tw, dbuf[0], res, gid, lane, mu32);
+        __syncthreads();
+        const int s0 = solo_next_step(res, -1, S, mode), s1 = s0 < S ? solo_next_step(res, s0, S, mode) : S;
+        if (threadIdx.x == 0) {
+            if (s0 < S) fetch(s0, 0);
+            if (s1 < S) fetch(s1, 1);
+        }
+        {
+            const uint4 *g4 = reinterpret_cast<const uint4 *>(A.accs + gid * 2048);
+            for (int u = threadIdx.x; u < 512; u += PT) {
+                const int P = u >> 8, v = u & 255;
+                *reinterpret_cast<uint4 *>(acc[P] + sw_chunk(v & 31, v >> 5)) = __ldcg(g4 + u);
+            }
+        }
+        __syncthreads();
+
+        bool failed = false;
+        int next = s1;   // the step whose key the buffer being released receives
+        for (int s = s0, b = 0; s < S; b ^= 1) {
+            if (warp >= GW) {
+                const int hp = warp - GW;
+                uint32_t x[32];
+                load_row(x, acc[hp], lane);
+                ntt_inv_1024_noscale<true>(x, c, itw, ts[hp], lane);
+                store_row(ts[hp], lane, x);
+            }
+            __syncthreads();
+            if (warp < GW) {
+                const int p = warp / DT, h = warp % DT;
+                const uint32_t shift = A.bg_bits * h, mask = (1u << A.bg_bits) - 1;
+                uint32_t x[32];
+                load_row(x, ts[p], lane);
+#pragma unroll
+                for (int r = 0; r < 32; r++) x[r] = (x[r] >> shift) & mask;
+                if (A.digit_tables) ntt_fwd_1024_digit<true>(x, c, ftw, dbuf[warp], dt, lane);
+                else ntt_fwd_1024<true>(x, c, ftw, dbuf[warp], lane);
+                store_row(dbuf[warp], lane, x);
+            }
+            const bool ok = mbar_wait_bounded(&bars[b], (parity >> b) & 1u, kSoloWaitLimit);
+            if (ok) {
+                parity ^= 1u << b;
+                pending &= ~(1u << b);
+            }
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            const uint4 *key = reinterpret_cast<const uint4 *>(solo_smem + b * L::key_bytes);
+            for (int u = threadIdx.x; u < 256; u += PT) mac_chunk_solo<DG>(u, key, dbuf, acc, c.Q, A.qinv_neg);
+            __syncthreads();
+            // buffer b is free again: it receives the key after the one in flight
+            const int after = next < S ? solo_next_step(res, next, S, mode) : S;
+            if (threadIdx.x == 0 && after < S) fetch(after, b);
+            s = next;
+            next = after;
+        }
+        if (failed) {
+            // flag the launch, let the copies in flight land (the CTA's shared
+            // memory stays allocated while thread 0 waits), and stop
+            if (threadIdx.x == 0) {
+                atomicOr(A.status, kStatusWaitLimit);
+                for (int b = 0; b < 2; b++)
+                    if (pending & (1u << b)) mbar_wait_bounded(&bars[b], (parity >> b) & 1u, kSoloWaitLimit);
+            }
+            return;
+        }
+
+        // ---- accumulator back to global memory, then the outputs of the pipelines' epilogue
+        {
+            uint4 *g4 = reinterpret_cast<uint4 *>(A.accs + gid * 2048);
+            for (int u = threadIdx.x; u < 512; u += PT) {
+                const int P = u >> 8, v = u & 255;
+                __stcg(g4 + u, *reinterpret_cast<const uint4 *>(acc[P] + sw_chunk(v & 31, v >> 5)));
+            }
+        }
+        __syncthreads();
+        if (warp < 2) pipe_out_poly(A, c, inv_tw, dbuf[warp], gid, warp, lane);
+        __syncthreads();
+    }
+}
+
 }  // namespace dev
 
 static int sm_count(Context &c)
@@ -468,6 +734,32 @@ static int launch_pipe_dg(Context &c, dev::PipeArgs A, int max_ctas, cudaStream_
     return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "blind rotation launch");
 }
 
+// Latency form: one CTA per ciphertext on up to one CTA per SM, each CTA
+// taking every gridDim-th ciphertext.
+template <int DG>
+static int launch_solo_dg(Context &c, const dev::PipeArgs &A, int max_ctas, cudaStream_t st)
+{
+    using L = dev::SoloLayout<DG>;
+    constexpr int threads = 32 * 2 * DG;
+    auto kern = dev::br32_solo_kernel<DG>;
+    const size_t steps = (size_t)c.p.n * c.p.digitR;
+    const size_t tables = A.digit_tables ? (20 * ((size_t)1 << c.p.BG_bits)) << dev::solo_table_copies_log2((int)c.p.BG_bits) : 0;
+    const size_t smem = L::bytes(tables, steps);
+    if (smem > kPipeSmemBudget) return 1;   // does not fit: the caller takes the pipelines
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return c.cuda_fail(e, "blind rotation (latency form) smem attribute");
+    size_t blocks = std::min<size_t>(A.count, (size_t)sm_count(c));
+    if (max_ctas > 0) blocks = std::min<size_t>(blocks, (size_t)max_ctas);
+    kern<<<(unsigned)blocks, threads, smem, st>>>(A, c.nc, c.d_fwd_tw, c.d_inv_tw, (uint32_t)((1ULL << 32) / c.p.Q));
+    c.launches++;
+    e = cudaGetLastError();
+    return e == cudaSuccess ? FHEACC_OK : c.cuda_fail(e, "blind rotation (latency form) launch");
+}
+
+// Latency form up to this many gates per SM by default (one GB300, 4096-gate
+// key set); FHEACC_OPT_BR_SOLO overrides, 0 turns it off.
+constexpr int kSoloGatesPerSm = 1;
+
 // Pipelines per CTA. By default from the gates per SM (one GB300, 4096-gate
 // key set): up to 2 a single pipeline per SM is fastest (its items do not
 // wait on other pipelines), up to 5 two pipelines, beyond that three.
@@ -475,6 +767,12 @@ template <int DG>
 static int launch_pipe_shape(Context &c, const dev::PipeArgs &A, int max_ctas, cudaStream_t st)
 {
     const size_t sms = (size_t)sm_count(c);
+    // explicit pipeline shapes and the wait-limit tests keep the pipelines
+    const int solo = c.tune.br_solo >= 0 ? c.tune.br_solo : kSoloGatesPerSm;
+    if (solo > 0 && c.tune.br_pipes == 0 && c.tune.debug_wait_limit < 0 && A.count <= (size_t)solo * sms) {
+        const int rc = launch_solo_dg<DG>(c, A, max_ctas, st);
+        if (rc != 1) return rc;
+    }
     const int np = c.tune.br_pipes > 0 ? c.tune.br_pipes : A.count <= 2 * sms ? 1 : A.count <= 5 * sms ? 2 : 3;
     if (np == 3) return launch_pipe_dg<DG, 3, 1>(c, A, max_ctas, st);
     if (np == 2) return launch_pipe_dg<DG, 2, 1>(c, A, max_ctas, st);

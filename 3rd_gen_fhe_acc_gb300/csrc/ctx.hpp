@@ -45,6 +45,7 @@ struct Tuning {
     int br_pool = -1;         // 64-bit path: remainder gates shared by all CTAs (0: off; -1: on)
     int debug_wait_limit = -1;   // tests: polls / idle periods before a bounded wait gives up (-1: built-in)
     int ks_tiled = -1;        // 32-bit LWE key switch: tiled form 1 always (scratch allowing), 0 never, -1 by size
+    int br_solo = -1;         // 32-bit path: latency form up to this many gates per SM (0: off; -1: default)
 };
 
 constexpr size_t kPipeSmemBudget = 220 * 1024;   // dynamic shared memory of one blind-rotation CTA

@@ -89,16 +89,18 @@ __device__ __forceinline__ void fwd_stage_A(uint32_t (&x)[32], const Ntt32Consts
 // at (g / 2) * 64 + 2 * lane + g % 2, so each warp load reads 256 or 512
 // contiguous bytes. Forward stages s = 5..9 (G = 1..16) start at
 // 32 * (2^(s-5) - 1); inverse stages t = 1..16 (G = 16/t) at 32 * (32 - 32/t).
-template <int G, int OFF>
+// Both tables have 992 entries. SH: the table is a copy in shared memory
+// (plain loads) instead of global memory read through L1 (__ldg).
+template <int G, int OFF, bool SH = false>
 __device__ __forceinline__ void load_stage_twiddles(uint2 (&w)[G], const uint2 *__restrict__ tw, int lane)
 {
     if (G == 1) {
-        w[0] = __ldg(tw + OFF + lane);
+        w[0] = SH ? tw[OFF + lane] : __ldg(tw + OFF + lane);
     } else {
         const uint4 *t4 = reinterpret_cast<const uint4 *>(tw + OFF);
 #pragma unroll
         for (int gg = 0; gg < G / 2; gg++) {
-            const uint4 v = __ldg(t4 + gg * 32 + lane);
+            const uint4 v = SH ? t4[gg * 32 + lane] : __ldg(t4 + gg * 32 + lane);
             w[2 * gg] = make_uint2(v.x, v.y);
             w[2 * gg + 1] = make_uint2(v.z, v.w);
         }
@@ -106,13 +108,13 @@ __device__ __forceinline__ void load_stage_twiddles(uint2 (&w)[G], const uint2 *
 }
 
 // Forward stage s (5..9) in layout B.
-template <int S>
+template <int S, bool SH = false>
 __device__ __forceinline__ void fwd_stage_B(uint32_t (&x)[32], const uint2 *__restrict__ tw, int lane,
                                             uint32_t Q, uint32_t twoQ)
 {
     constexpr int t = 512 >> S, G = 16 / t;   // G twiddles per lane
     uint2 w[G];
-    load_stage_twiddles<G, 32 * ((1 << (S - 5)) - 1)>(w, tw, lane);
+    load_stage_twiddles<G, 32 * ((1 << (S - 5)) - 1), SH>(w, tw, lane);
 #pragma unroll
     for (int r = 0; r < 32; r++) {
         if (!(r & t)) {
@@ -123,13 +125,13 @@ __device__ __forceinline__ void fwd_stage_B(uint32_t (&x)[32], const uint2 *__re
 }
 
 // Inverse stage with butterfly distance t (1..16) in layout B.
-template <int T>
+template <int T, bool SH = false>
 __device__ __forceinline__ void inv_stage_B(uint32_t (&x)[32], const uint2 *__restrict__ tw, int lane,
                                             uint32_t Q, uint32_t twoQ)
 {
     constexpr int G = 16 / T;
     uint2 w[G];
-    load_stage_twiddles<G, 32 * (32 - 32 / T)>(w, tw, lane);
+    load_stage_twiddles<G, 32 * (32 - 32 / T), SH>(w, tw, lane);
 #pragma unroll
     for (int r = 0; r < 32; r++) {
         if (!(r & T)) {
@@ -200,7 +202,8 @@ __device__ __forceinline__ void transpose_B_to_A(uint32_t (&x)[32], uint32_t *bu
 
 // Forward NTT: x in layout A (values < Q) -> layout B, values < 21Q, in the
 // reference's bit-reversed output order. buf: 1024 words of 16-byte aligned
-// scratch.
+// scratch. SH: fwd_tw is a shared-memory copy of the table.
+template <bool SH = false>
 __device__ __forceinline__ void ntt_fwd_1024(uint32_t (&x)[32], const Ntt32Consts &c,
                                              const uint2 *__restrict__ fwd_tw, uint32_t *buf, int lane)
 {
@@ -210,11 +213,11 @@ __device__ __forceinline__ void ntt_fwd_1024(uint32_t (&x)[32], const Ntt32Const
     fwd_stage_A<3>(x, c);
     fwd_stage_A<4>(x, c);
     transpose_A_to_B(x, buf, lane);
-    fwd_stage_B<5>(x, fwd_tw, lane, c.Q, c.twoQ);
-    fwd_stage_B<6>(x, fwd_tw, lane, c.Q, c.twoQ);
-    fwd_stage_B<7>(x, fwd_tw, lane, c.Q, c.twoQ);
-    fwd_stage_B<8>(x, fwd_tw, lane, c.Q, c.twoQ);
-    fwd_stage_B<9>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<5, SH>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<6, SH>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<7, SH>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<8, SH>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<9, SH>(x, fwd_tw, lane, c.Q, c.twoQ);
 }
 
 // Products of a gadget digit (y < BG) with the three twiddles of the first two
@@ -246,6 +249,7 @@ __host__ __device__ constexpr int digit_table_copies_log2(int bg_bits) { return 
 //   x[r + 24] = x0 - w1 x2 - w3 x1 + w3 w1 x3
 // with the five products read from DigitTables (three shared-memory loads
 // instead of four Shoup multiplies), each output below 3Q + BG.
+template <bool SH = false>
 __device__ __forceinline__ void ntt_fwd_1024_digit(uint32_t (&x)[32], const Ntt32Consts &c,
                                                    const uint2 *__restrict__ fwd_tw, uint32_t *buf,
                                                    const DigitTables &T, int lane)
@@ -265,25 +269,26 @@ __device__ __forceinline__ void ntt_fwd_1024_digit(uint32_t (&x)[32], const Ntt3
     fwd_stage_A<3>(x, c);
     fwd_stage_A<4>(x, c);
     transpose_A_to_B(x, buf, lane);
-    fwd_stage_B<5>(x, fwd_tw, lane, c.Q, c.twoQ);
-    fwd_stage_B<6>(x, fwd_tw, lane, c.Q, c.twoQ);
-    fwd_stage_B<7>(x, fwd_tw, lane, c.Q, c.twoQ);
-    fwd_stage_B<8>(x, fwd_tw, lane, c.Q, c.twoQ);
-    fwd_stage_B<9>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<5, SH>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<6, SH>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<7, SH>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<8, SH>(x, fwd_tw, lane, c.Q, c.twoQ);
+    fwd_stage_B<9, SH>(x, fwd_tw, lane, c.Q, c.twoQ);
 }
 
 // Inverse NTT without the final N^-1: x in layout B (values < 2Q) -> layout
 // A, canonical, equal to N * (the reference's iNTT) mod Q. Used on
 // accumulators that already carry the factor N^-1 (bootstrap keys uploaded
-// times N^-1).
+// times N^-1). SH: inv_tw is a shared-memory copy of the table.
+template <bool SH = false>
 __device__ __forceinline__ void ntt_inv_1024_noscale(uint32_t (&x)[32], const Ntt32Consts &c,
                                                      const uint2 *__restrict__ inv_tw, uint32_t *buf, int lane)
 {
-    inv_stage_B<1>(x, inv_tw, lane, c.Q, c.twoQ);
-    inv_stage_B<2>(x, inv_tw, lane, c.Q, c.twoQ);
-    inv_stage_B<4>(x, inv_tw, lane, c.Q, c.twoQ);
-    inv_stage_B<8>(x, inv_tw, lane, c.Q, c.twoQ);
-    inv_stage_B<16>(x, inv_tw, lane, c.Q, c.twoQ);
+    inv_stage_B<1, SH>(x, inv_tw, lane, c.Q, c.twoQ);
+    inv_stage_B<2, SH>(x, inv_tw, lane, c.Q, c.twoQ);
+    inv_stage_B<4, SH>(x, inv_tw, lane, c.Q, c.twoQ);
+    inv_stage_B<8, SH>(x, inv_tw, lane, c.Q, c.twoQ);
+    inv_stage_B<16, SH>(x, inv_tw, lane, c.Q, c.twoQ);
     transpose_B_to_A(x, buf, lane);
     inv_stage_A<1>(x, c);
     inv_stage_A<2>(x, c);

@@ -255,6 +255,14 @@ int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t cou
  *                             key row group through shared memory) for any
  *                             batch, 0 = one CTA per gate, -1 (default) =
  *                             tiled from 1024 gates
+ *  FHEACC_OPT_BR_SOLO       : 32-bit words: the latency form of the blind
+ *                             rotation (one CTA per ciphertext, accumulator in
+ *                             shared memory, each step's key prefetched into
+ *                             shared memory by bulk asynchronous copies) up
+ *                             to this many gates per SM; 0 = off, -1
+ *                             (default) = 1. Not taken when
+ *                             FHEACC_OPT_BR_PIPES or
+ *                             FHEACC_OPT_DEBUG_WAIT_LIMIT is set.
  *  FHEACC_OPT_DEBUG_WAIT_LIMIT: for tests of the error path only. The
  *                             number of polls (64-bit workers, the step
  *                             window) or idle periods (32-bit pipelines) a
@@ -278,6 +286,7 @@ int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t cou
 #define FHEACC_OPT_BR_POOL        6
 #define FHEACC_OPT_DEBUG_WAIT_LIMIT 7
 #define FHEACC_OPT_KS_TILED       8
+#define FHEACC_OPT_BR_SOLO        9
 int fheacc_set_option(fheacc_ctx *ctx, int option, int value);
 
 /* Per-kernel device times (ms) of the most recent call made with
