@@ -242,25 +242,26 @@ def param_view(p):
     return v
 
 
-def profile_case(preset=0):
+def profile_case(preset=0, gates=912, n=64):
     """The case the committed ncu section captures use: the bench parameter
     set with n = 64 (same per-step work), 912 random gates (6 per SM: the
     3-pipeline shape of the 32-bit kernel, one wave of the 64-bit grid), two
-    batched launches, outputs checked by decryption."""
+    batched launches, outputs checked by decryption. gates = 1, n = 500: a
+    lone gate of the bench set (the latency form of the 32-bit kernel)."""
     import torch
     import __graft_entry__
     __graft_entry__.build_product()
     import importlib
     F = importlib.import_module("3rd_gen_fhe_acc_gb300")
     P = F.params_preset(preset)
-    P.n = 64
+    P.n = n
     F.derive(P)
     lsk = F.LWE_secretkey(P, 1)
     rsk = F.RLWE_secretkey(P, 2)
     ctx = F.Context(P, 0)
     ctx.upload_bootstrap_key(F.bootstrap_key(P, 3, lsk, rsk))
     ctx.upload_keyswitch_key(F.keyswitch_key(P, 4, rsk, lsk))
-    B = 912
+    B = gates
     rng = np.random.default_rng(0)
     bits = rng.integers(0, 2, 2 * B).astype(np.uint8)
     c = F.LWE_encrypt(P, 9, lsk, bits)
@@ -820,13 +821,15 @@ def main():
     ap.add_argument("--mixed-wide", type=int, default=700)
     ap.add_argument("--mixed-seed", type=int, default=2024)
     ap.add_argument("--profile-case", action="store_true",
-                    help="only run the small profiling case (n=64, 608 gates, 2 launches) and exit")
+                    help="only run the small profiling case (n=64, 912 gates, 2 launches) and exit")
+    ap.add_argument("--profile-gates", type=int, default=912, help="gates of the profiling case")
+    ap.add_argument("--profile-n", type=int, default=64, help="LWE dimension of the profiling case")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
     if args.profile_case:
-        return profile_case(args.preset)
+        return profile_case(args.preset, args.profile_gates, args.profile_n)
     if args.mixed:
         run_mixed(args)
         return 0

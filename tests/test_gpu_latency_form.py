@@ -84,3 +84,24 @@ def test_latency_form_bg9_against_oracle(F, keys2, cuda_ok):
         assert ctx.device_status() == 0
     finally:
         ctx.close()
+
+
+def test_empty_batches_launch_nothing(F, ctx0, cuda_ok):
+    """count = 0 through every bootstrap entry point: FHEACC_OK, no kernel
+    launched, no output touched (the reference's x-width calls reject a
+    wrong width; an any-count ABI takes zero as a no-op)."""
+    torch = cuda_ok
+    L = F.lib()
+    d = torch.full((4, 501), -1, dtype=torch.int64, device="cuda")
+    dg = torch.zeros(4, dtype=torch.int32, device="cuda")
+    before = ctx0.kernel_launches() if hasattr(ctx0, "kernel_launches") else None
+    ctx0.bootstrap_async(d.data_ptr(), d.data_ptr(), dg.data_ptr(), 0, d.data_ptr())
+    ctx0.bootstrap_plain_async(d.data_ptr(), d.data_ptr(), dg.data_ptr(), 0, d.data_ptr())
+    ctx0.blind_rotate_async(d.data_ptr(), d.data_ptr(), dg.data_ptr(), 0, d.data_ptr())
+    assert L.fheacc_bootstrap_noalloc(ctx0.handle, d.data_ptr(), d.data_ptr(), dg.data_ptr(), 0, d.data_ptr(), 0,
+                                      None) == F.OK
+    assert L.fheacc_bootstrap(ctx0.handle, None, None, None, 0, None, 0) == F.OK
+    ctx0.sync()
+    if before is not None:
+        assert ctx0.kernel_launches() == before
+    assert bool((d == -1).all())
