@@ -1054,6 +1054,10 @@ int launch_lwe_keyswitch64(Context &c, const uint64_t *d_extract, size_t count, 
     A.fold = (int)std::max<uint64_t>(8, fold & ~(uint64_t)7);
     const unsigned threads = c.dp.ks_row / 2;   // ks_row: a multiple of 32 words, > n
     const size_t sms = (size_t)sms_of(c);
+    // from two gates per SM: the tiled form (lwe_ks.cu), each row group read
+    // from L2 once per gate block
+    if (d_scratch && ks64_tiled_applies(c, count, (int)sms, scratch_bytes))
+        return launch_ks64_tiled(c, d_extract, count, modswitch, d_out, d_out_idx, d_scratch, (int)sms, st);
     // a few ciphertexts: each one's rows split over many CTAs, with at most
     // `fold` rows per CTA and slices * Q < 2^64
     const int rows = c.p.N * (int)c.p.digitKS;

@@ -230,8 +230,14 @@ int launch_blind_rotate64_with(Context &c, const uint64_t *d_c1, const uint64_t 
                                size_t count, uint32_t flags, uint64_t *accs, uint64_t *d_acc_out,
                                uint64_t *d_extract, int max_ctas, cudaStream_t st);
 int launch_extract64(Context &c, const uint64_t *d_rlwe, size_t count, uint64_t *d_extract, cudaStream_t st);
-// d_scratch (optional, scratch_bytes of free device memory): lets a few
-// ciphertexts' rows be split over many CTAs (count * ks_row u64 partial sums).
+// Tiled 64-bit LWE key switch (lwe_ks.cu): whether it applies to `count` gates
+// with `scratch_bytes` of scratch for the digits, and the launch.
+bool ks64_tiled_applies(const Context &c, size_t count, int sms, size_t scratch_bytes);
+int launch_ks64_tiled(Context &c, const uint64_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
+                      const uint32_t *d_out_idx, void *scratch, int sms, cudaStream_t st);
+// d_scratch (optional, scratch_bytes of free device memory): from two gates
+// per SM holds the tiled form's digits; below, lets a few ciphertexts' rows be
+// split over many CTAs (count * ks_row u64 partial sums).
 int launch_lwe_keyswitch64(Context &c, const uint64_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
                            cudaStream_t st, const uint32_t *d_out_idx = nullptr, void *d_scratch = nullptr,
                            size_t scratch_bytes = 0);

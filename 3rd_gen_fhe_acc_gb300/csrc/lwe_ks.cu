@@ -29,6 +29,7 @@
 // same epilogue.
 #include "ctx.hpp"
 #include <algorithm>
+#include <type_traits>
 
 namespace fheacc {
 namespace dev {
@@ -176,10 +177,11 @@ constexpr int kKsTileStages = 4;   // stages in flight (cp.async ring)
 constexpr int kKsTileGroups = 2;   // row groups per stage (one barrier per stage)
 
 struct KsTiledArgs {
-    KsArgs k;
+    KsArgs k;                // 64-bit words: kskey and ks_row in 32-bit units (a u64 row is 2 ks_row words)
     const uint8_t *digits;   // [(i * digitKS + j)][gstride]: digit j of a[i] of each gate (ks_digit_slot)
-    size_t gstride;          // bytes per digit row: 128 per gate block
-    int slices;              // column slices of kKsTileCols words
+    size_t gstride;          // bytes per digit row: 128 per gate block (64-bit words: 16 GW)
+    int slices;              // column slices of kKsTileCols 32-bit words
+    const uint64_t *ext64;   // 64-bit words: extracted RLWEs (kExtract64 words each)
 };
 
 // The digits of a gate block as the tiled kernel reads them: warp w of the
@@ -226,6 +228,40 @@ __global__ void __launch_bounds__(256) ks_digits_kernel(const uint32_t *__restri
     }
 }
 
+// 64-bit words: digits[(i * D + j) * gstride + g] = (a_i / Bks^j) mod Bks of
+// gate g, the gates of a block contiguous (16 GW bytes per block and row
+// group). Same 32 x 32 transpose as ks_digits_kernel. The quotients come from
+// magic = ceil(2^64 / Bks): floor(a magic / 2^64) = floor(a / Bks) for every
+// a below Q (the launcher checks Q (magic Bks - 2^64) < 2^64).
+__global__ void __launch_bounds__(256) ks_digits64_kernel(const uint64_t *__restrict__ ext, size_t count,
+                                                          size_t padded, uint8_t *__restrict__ digits, size_t gstride,
+                                                          int D, uint32_t Bks, uint64_t magic)
+{
+    __shared__ uint64_t tile[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const size_t g0 = (size_t)blockIdx.x * 32;
+    const int i0 = blockIdx.y * 32;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const size_t g = g0 + ty + 8 * r;
+        tile[ty + 8 * r][tx] = g < count ? ext[g * kExtract64 + i0 + tx] : 0ull;
+    }
+    __syncthreads();
+    const size_t g = g0 + tx;
+    if (g >= padded) return;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const int ci = ty + 8 * r;
+        uint64_t a = tile[tx][ci];
+        uint8_t *dst = digits + (size_t)(i0 + ci) * D * gstride + g;
+        for (int j = 0; j < D; j++) {
+            const uint64_t qt = __umul64hi(a, magic);
+            dst[(size_t)j * gstride] = (uint8_t)(a - qt * Bks);
+            a = qt;
+        }
+    }
+}
+
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -235,25 +271,31 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int PENDING>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(PENDING) : "memory"); }
 
-// CTA (gate block b, column slice s): gates [b G, b G + G), G = 16 GW (GW <=
-// 8), key words [s 128, s 128 + 128). The row groups are walked kKsTileGroups
-// at a time: a stage of the ring holds that many groups' Bks row slices
-// ([Bks][128] words each) and the block's 128 digit bytes of each group. Every
-// thread copies the same chunks of every stage; their source addresses move
-// by a per-group offset that is advanced, not recomputed. Warp w owns gates
-// w GW .. w GW + GW - 1 and lane l the words 4 l .. 4 l + 3 of the slice: per
-// row group it reads its digit slot in one 64-bit load and adds, for each of
-// its gates, the row slice the digit selects (one 128-bit shared load; all
-// lanes read one row, so a warp's load is 512 contiguous bytes, free of bank
-// conflicts). Sums stay below 32 Q < 2^32 with a conditional subtraction of
-// 16 Q every 16 row groups (rows are canonical, Q < 2^27).
-template <int GW>
-__global__ void __launch_bounds__(kKsTileWarps * 32, 1) lwe_ks32_tiled_kernel(const __grid_constant__ KsTiledArgs T)
+// CTA (gate block b, column slice s): gates [b G, b G + G), G = 16 GW, key
+// words [s 128, s 128 + 128) (32-bit units: 64 words of a 64-bit row). The row
+// groups are walked kKsTileGroups at a time: a stage of the ring holds that
+// many groups' Bks row slices ([Bks][512 bytes] each) and the block's digit
+// bytes of each group. Every thread copies the same chunks of every stage;
+// their source addresses move by a per-group offset that is advanced, not
+// recomputed. Warp w owns gates w GW .. w GW + GW - 1 and lane l the 16 bytes
+// 16 l .. 16 l + 15 of the slice: per row group it reads its gates' digits and
+// adds, for each gate, the row slice the digit selects (one 128-bit shared
+// load; all lanes read one row, so a warp's load is 512 contiguous bytes, free
+// of bank conflicts). Sums stay below 32 Q with a conditional subtraction of
+// 16 Q every 16 row groups (rows are canonical): 32-bit sums for Q < 2^27,
+// 64-bit sums for the 64-bit words.
+// 32-bit words: GW <= 8, the block's digits of a group in 8-byte slots per
+// warp (ks_digit_slot), read in one 64-bit load. 64-bit words (WIDE): GW <=
+// 16, the block's G digit bytes contiguous, read as bytes.
+template <int GW, bool WIDE>
+__device__ __forceinline__ void ks_tiled_body(const KsTiledArgs &T, uint32_t *ring)
 {
-    extern __shared__ __align__(16) uint32_t ring[];
     constexpr int R = kKsTileGroups;
     constexpr int kMaxChunks = 4;   // chunks of a stage per thread (checked by the launcher)
-    constexpr int kDigitWords = kKsTileWarps * 8 / 4;
+    constexpr int kDigitBytes = WIDE ? kKsTileWarps * GW : kKsTileWarps * 8;   // per block and row group
+    constexpr int kDigitWords = kDigitBytes / 4;
+    using Acc = typename std::conditional<WIDE, uint64_t, uint32_t>::type;
+    constexpr int AE = WIDE ? 2 : 4;   // sums per gate and lane
     const KsArgs &A = T.k;
     const int N = A.N, D = A.digitKS, Bks = (int)A.Bks, n = A.n;
     const int group_words = Bks * kKsTileCols + kDigitWords;   // row slices, then digit slots
@@ -264,7 +306,7 @@ __global__ void __launch_bounds__(kKsTileWarps * 32, 1) lwe_ks32_tiled_kernel(co
     const size_t g0 = gb * (kKsTileWarps * GW);
     const int c0 = slice * kKsTileCols;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t Q = (uint32_t)A.Q, Q16 = 16 * Q;
+    const Acc Q = (Acc)A.Q, Q16 = 16 * Q;
     const int total = N * D;
     const size_t row_stride = (size_t)D * N * A.ks_row;   // words between digits d and d + 1
 
@@ -292,7 +334,7 @@ __global__ void __launch_bounds__(kKsTileWarps * 32, 1) lwe_ks32_tiled_kernel(co
                                                         (size_t)(cc >> 5) * row_stride + 4 * (cc & 31));
             } else {
                 dig[u] = true;
-                src[u] = reinterpret_cast<const char *>(T.digits + (size_t)r * T.gstride + gb * (kKsTileWarps * 8) +
+                src[u] = reinterpret_cast<const char *>(T.digits + (size_t)r * T.gstride + gb * kDigitBytes +
                                                         16 * (cc - rows_chunks));
             }
         }
@@ -339,9 +381,11 @@ __global__ void __launch_bounds__(kKsTileWarps * 32, 1) lwe_ks32_tiled_kernel(co
         if (fetched < total) issue_stage();
         cp_async_commit();
     }
-    uint32_t acc[GW][4];
+    Acc acc[GW][AE];
 #pragma unroll
-    for (int k = 0; k < GW; k++) acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = 0;
+    for (int k = 0; k < GW; k++)
+#pragma unroll
+        for (int e = 0; e < AE; e++) acc[k][e] = 0;
 
     for (int rg = 0; rg < total; rg += R) {
         cp_async_wait<kKsTileStages - 2>();
@@ -354,16 +398,27 @@ __global__ void __launch_bounds__(kKsTileWarps * 32, 1) lwe_ks32_tiled_kernel(co
         for (int r = 0; r < R; r++) {
             if (rg + r < total) {
                 const uint32_t *grp_w = st + r * group_words;
-                const uint2 dg2 = reinterpret_cast<const uint2 *>(grp_w + Bks * kKsTileCols)[warp];
                 const uint4 *rows4 = reinterpret_cast<const uint4 *>(grp_w);
+                if constexpr (!WIDE) {
+                    const uint2 dg2 = reinterpret_cast<const uint2 *>(grp_w + Bks * kKsTileCols)[warp];
 #pragma unroll
-                for (int k = 0; k < GW; k++) {
-                    const uint32_t d = ((k < 4 ? dg2.x : dg2.y) >> (8 * (k & 3))) & 0xFFu;
-                    const uint4 v = rows4[d * (kKsTileCols / 4) + lane];
-                    acc[k][0] += v.x;
-                    acc[k][1] += v.y;
-                    acc[k][2] += v.z;
-                    acc[k][3] += v.w;
+                    for (int k = 0; k < GW; k++) {
+                        const uint32_t d = ((k < 4 ? dg2.x : dg2.y) >> (8 * (k & 3))) & 0xFFu;
+                        const uint4 v = rows4[d * (kKsTileCols / 4) + lane];
+                        acc[k][0] += v.x;
+                        acc[k][1] += v.y;
+                        acc[k][2] += v.z;
+                        acc[k][3] += v.w;
+                    }
+                } else {
+                    const uint8_t *dgb = reinterpret_cast<const uint8_t *>(grp_w + Bks * kKsTileCols) + warp * GW;
+#pragma unroll
+                    for (int k = 0; k < GW; k++) {
+                        const uint32_t d = dgb[k];
+                        const ulonglong2 v = reinterpret_cast<const ulonglong2 *>(rows4)[d * (kKsTileCols / 4) + lane];
+                        acc[k][0] += v.x;
+                        acc[k][1] += v.y;
+                    }
                 }
             }
         }
@@ -371,29 +426,45 @@ __global__ void __launch_bounds__(kKsTileWarps * 32, 1) lwe_ks32_tiled_kernel(co
 #pragma unroll
             for (int k = 0; k < GW; k++)
 #pragma unroll
-                for (int e = 0; e < 4; e++) acc[k][e] = min(acc[k][e], acc[k][e] - Q16);
+                for (int e = 0; e < AE; e++) acc[k][e] = min(acc[k][e], acc[k][e] - Q16);
         }
     }
     cp_async_wait<0>();
 
-    const uint32_t Q8 = Q / 8 + 1;
+    const Acc Q8 = Q / 8 + 1;
 #pragma unroll
     for (int k = 0; k < GW; k++) {
         const size_t g = g0 + warp * GW + k;
         if (g >= A.count) continue;
-        const uint32_t b0 = A.ext[g * kExtractStride + N];
+        const Acc b0 = WIDE ? (Acc)T.ext64[g * kExtract64 + N] : (Acc)A.ext[g * kExtractStride + N];
         uint64_t *out = A.out + (A.out_idx ? (size_t)A.out_idx[g] : g) * (size_t)(n + 1);
 #pragma unroll
-        for (int e = 0; e < 4; e++) {
-            const int col = c0 + 4 * lane + e;
+        for (int e = 0; e < AE; e++) {
+            const int col = (WIDE ? c0 / 2 + 2 * lane : c0 + 4 * lane) + e;
             if (col > n) continue;
-            const uint32_t s = acc[k][e] % Q;
+            const Acc s = acc[k][e] % Q;
             uint64_t v;
             if (col < n) v = s ? Q - s : 0;
             else v = ((uint64_t)(b0 + Q8) % Q + Q - s) % Q;
             out[col] = A.modswitch ? scale_round_dev(v, A.q, A.Q) : v;
         }
     }
+}
+
+template <int GW>
+__global__ void __launch_bounds__(kKsTileWarps * 32, 1) lwe_ks32_tiled_kernel(const __grid_constant__ KsTiledArgs T)
+{
+    extern __shared__ __align__(16) uint32_t ring[];
+    ks_tiled_body<GW, false>(T, ring);
+}
+
+// The tiled form for 64-bit words (N = 2048, Q < 2^58): same staging, 64-bit
+// sums, gates per warp up to 16.
+template <int GW>
+__global__ void __launch_bounds__(kKsTileWarps * 32, 1) lwe_ks64_tiled_kernel(const __grid_constant__ KsTiledArgs T)
+{
+    extern __shared__ __align__(16) uint32_t ring[];
+    ks_tiled_body<GW, true>(T, ring);
 }
 
 __global__ void modswitch_kernel(const uint64_t *__restrict__ in, uint64_t *__restrict__ out, size_t words,
@@ -405,10 +476,12 @@ __global__ void modswitch_kernel(const uint64_t *__restrict__ in, uint64_t *__re
 
 }  // namespace dev
 
-template <int GW>
+template <int GW, bool WIDE = false>
 static int launch_ks_tiled_gw(Context &c, const dev::KsTiledArgs &T, size_t blocks, size_t smem, cudaStream_t st)
 {
-    auto kern = dev::lwe_ks32_tiled_kernel<GW>;
+    void (*kern)(const dev::KsTiledArgs);
+    if constexpr (WIDE) kern = dev::lwe_ks64_tiled_kernel<GW>;
+    else kern = dev::lwe_ks32_tiled_kernel<GW>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return c.cuda_fail(e, "tiled key switch smem attribute");
     kern<<<(unsigned)blocks, dev::kKsTileWarps * 32, smem, st>>>(T);
@@ -477,6 +550,91 @@ static int launch_ks_tiled(Context &c, const dev::KsArgs &A, void *scratch, int 
     case 6: return launch_ks_tiled_gw<6>(c, T, blocks, smem, st);
     case 7: return launch_ks_tiled_gw<7>(c, T, blocks, smem, st);
     default: return launch_ks_tiled_gw<8>(c, T, blocks, smem, st);
+    }
+}
+
+// ---- tiled form of the 64-bit words (lwe_ks64_tiled_kernel)
+
+// Gates per warp (1..16): the smallest with which the gate blocks times the
+// column slices fit on the SMs (2048 gates at N = 2048, n = 630: 9 gates per
+// warp, 15 blocks x 10 slices = 150 CTAs).
+static int ks64_tiled_gw(size_t count, int sms, int slices)
+{
+    const size_t blocks_target = std::max<size_t>(1, (size_t)sms / slices);
+    const size_t per_warp = ((count + blocks_target - 1) / blocks_target + dev::kKsTileWarps - 1) / dev::kKsTileWarps;
+    return (int)std::min<size_t>(16, std::max<size_t>(1, per_warp));
+}
+
+// ceil(2^64 / Bks), the digits kernel's quotient multiplier; 0 if its
+// quotients are not exact for every word below Q.
+static uint64_t ks64_digit_magic(const Context &c)
+{
+    const uint64_t B = c.p.Bks;
+    if (B < 2) return 0;
+    const uint64_t m = UINT64_MAX / B + 1;
+    const unsigned __int128 err = (unsigned __int128)m * B - ((unsigned __int128)1 << 64);   // in [0, B)
+    return (unsigned __int128)c.p.Q * err < ((unsigned __int128)1 << 64) ? m : 0;
+}
+
+bool ks64_tiled_applies(const Context &c, size_t count, int sms, size_t scratch_bytes)
+{
+    if (c.tune.ks_tiled == 0) return false;
+    const int slices = (int)(2 * c.dp.ks_row / dev::kKsTileCols);
+    if ((2 * c.dp.ks_row) % dev::kKsTileCols != 0 || c.p.N % 32 != 0 || c.p.Bks > 255 || !ks64_digit_magic(c))
+        return false;
+    // a thread copies at most 4 chunks of a stage (16 digit chunks at most)
+    if ((size_t)dev::kKsTileGroups * (c.p.Bks * (dev::kKsTileCols / 4) + 16) > 4 * 32 * (size_t)dev::kKsTileWarps)
+        return false;
+    const size_t G = (size_t)dev::kKsTileWarps * ks64_tiled_gw(count, sms, slices);
+    if ((count + G - 1) / G * G * (size_t)c.p.N * c.p.digitKS > scratch_bytes) return false;
+    if (c.tune.ks_tiled > 0) return true;
+    return count >= 2 * (size_t)sms;
+}
+
+// Runs the tiled 64-bit key switch (ks64_tiled_applies must hold): the digits
+// into `scratch`, then lwe_ks64_tiled_kernel.
+int launch_ks64_tiled(Context &c, const uint64_t *d_extract, size_t count, bool modswitch, uint64_t *d_out,
+                      const uint32_t *d_out_idx, void *scratch, int sms, cudaStream_t st)
+{
+    const int slices = (int)(2 * c.dp.ks_row / dev::kKsTileCols);
+    const int GW = ks64_tiled_gw(count, sms, slices);
+    const size_t G = (size_t)dev::kKsTileWarps * GW, nblocks = (count + G - 1) / G, padded = nblocks * G;
+    dev::KsTiledArgs T{};
+    T.k.ext = nullptr; T.k.count = count; T.k.kskey = reinterpret_cast<const uint32_t *>(c.d_kskey64);
+    T.k.out = d_out; T.k.out_idx = d_out_idx;
+    T.k.n = c.p.n; T.k.N = c.p.N; T.k.digitKS = (int)c.p.digitKS; T.k.Bks = c.p.Bks;
+    T.k.ks_row = 2 * c.dp.ks_row;   // 32-bit words per 64-bit row
+    T.k.q = c.p.q; T.k.modswitch = modswitch ? 1u : 0u; T.k.Q = c.p.Q;
+    T.digits = (const uint8_t *)scratch;
+    T.gstride = padded;
+    T.slices = slices;
+    T.ext64 = d_extract;
+    dim3 dgrid((unsigned)((padded + 31) / 32), (unsigned)(c.p.N / 32));
+    dev::ks_digits64_kernel<<<dgrid, 256, 0, st>>>(d_extract, count, padded, (uint8_t *)scratch, T.gstride,
+                                                   (int)c.p.digitKS, c.p.Bks, ks64_digit_magic(c));
+    c.launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return c.cuda_fail(e, "key-switch digits launch");
+    const size_t blocks = nblocks * slices;
+    const size_t smem = (size_t)dev::kKsTileStages * dev::kKsTileGroups *
+                        ((size_t)c.p.Bks * dev::kKsTileCols + 4 * (size_t)GW) * sizeof(uint32_t);
+    switch (GW) {
+    case 1: return launch_ks_tiled_gw<1, true>(c, T, blocks, smem, st);
+    case 2: return launch_ks_tiled_gw<2, true>(c, T, blocks, smem, st);
+    case 3: return launch_ks_tiled_gw<3, true>(c, T, blocks, smem, st);
+    case 4: return launch_ks_tiled_gw<4, true>(c, T, blocks, smem, st);
+    case 5: return launch_ks_tiled_gw<5, true>(c, T, blocks, smem, st);
+    case 6: return launch_ks_tiled_gw<6, true>(c, T, blocks, smem, st);
+    case 7: return launch_ks_tiled_gw<7, true>(c, T, blocks, smem, st);
+    case 8: return launch_ks_tiled_gw<8, true>(c, T, blocks, smem, st);
+    case 9: return launch_ks_tiled_gw<9, true>(c, T, blocks, smem, st);
+    case 10: return launch_ks_tiled_gw<10, true>(c, T, blocks, smem, st);
+    case 11: return launch_ks_tiled_gw<11, true>(c, T, blocks, smem, st);
+    case 12: return launch_ks_tiled_gw<12, true>(c, T, blocks, smem, st);
+    case 13: return launch_ks_tiled_gw<13, true>(c, T, blocks, smem, st);
+    case 14: return launch_ks_tiled_gw<14, true>(c, T, blocks, smem, st);
+    case 15: return launch_ks_tiled_gw<15, true>(c, T, blocks, smem, st);
+    default: return launch_ks_tiled_gw<16, true>(c, T, blocks, smem, st);
     }
 }
 

@@ -250,11 +250,12 @@ int fheacc_lwe_modswitch_async(fheacc_ctx *ctx, const uint64_t *d_in, size_t cou
  *                             CTAs share the remainder step by step; 0 = off
  *                             (some CTAs take one ciphertext more), -1
  *                             (default) = on
- *  FHEACC_OPT_KS_TILED      : 32-bit LWE key switch of a batched bootstrap:
+ *  FHEACC_OPT_KS_TILED      : LWE key switch of a batched bootstrap:
  *                             1 = the tiled form (gate blocks sharing each
  *                             key row group through shared memory) for any
  *                             batch, 0 = one CTA per gate, -1 (default) =
- *                             tiled from 1024 gates
+ *                             tiled from 1024 gates (32-bit words) or from
+ *                             two gates per SM (64-bit words)
  *  FHEACC_OPT_BR_SOLO       : 32-bit words: the latency form of the blind
  *                             rotation (one CTA per ciphertext, accumulator in
  *                             shared memory, each step's key prefetched into

@@ -159,6 +159,37 @@ def test_wide_fpga_x1_mode(F, ctx1, keys1, pipes):
     assert np.array_equal(out, want)
 
 
+@pytest.mark.parametrize("count", [40, 341, 2048, 4000])
+def test_wide_tiled_keyswitch_equals_per_gate(F, ctx1, keys1, cuda_ok, count):
+    """The tiled 64-bit LWE key switch (gate blocks sharing each key row group
+    through shared memory; from two gates per SM by default) against the
+    one-CTA-per-gate kernel on the same blind-rotation outputs: forced on 40
+    gates (one gate per warp, a partial last block), then 341 (two per warp),
+    2048 (nine per warp, the 2048-gate configuration's shape) and 4000 (16 per
+    warp, more CTAs than SMs); a few gates also against the oracle. Integer
+    words: bit-exact."""
+    torch = cuda_ok
+    x, y, g, c1, c2 = random_gate_batch(keys1, count, seed=181 + count)
+    d1, d2, dg = dev(torch, c1), dev(torch, c2), torch.from_numpy(g).cuda()
+    tiled, per_gate = torch.zeros_like(d1), torch.zeros_like(d1)
+    try:
+        ctx1.set_option(F.OPT_KS_TILED, 1)
+        ctx1.bootstrap_async(d1.data_ptr(), d2.data_ptr(), dg.data_ptr(), count, tiled.data_ptr())
+        ctx1.sync()
+        ctx1.set_option(F.OPT_KS_TILED, 0)
+        ctx1.bootstrap_async(d1.data_ptr(), d2.data_ptr(), dg.data_ptr(), count, per_gate.data_ptr())
+        ctx1.sync()
+    finally:
+        ctx1.set_option(F.OPT_KS_TILED, -1)
+    assert torch.equal(tiled, per_gate)
+    out = host(tiled)
+    truth = np.array([F.gate_truth(int(a), b, c) for a, b, c in zip(g, x, y)], dtype=np.uint8)
+    assert np.array_equal(keys1.decrypt(out), truth)
+    idx = np.array([0, count // 2, count - 1])
+    want, failed = keys1.oracle.eval_bootstrap_batch(c1[idx], c2[idx], g[idx], keys1.btkey, keys1.kskey)
+    assert failed == 0 and np.array_equal(out[idx], want)
+
+
 def test_wide_plain_equals_batched(F, ctx1, keys1, cuda_ok):
     """The plain form at N = 2048 (one launch sequence per gate; each lone
     gate's key switch split over many CTAs, 64-bit partial sums reduced mod
