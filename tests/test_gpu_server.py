@@ -156,3 +156,34 @@ def test_server_wide_parameter_set(F, ctx1, keys1):
             assert np.array_equal(got[rid][1], direct)
     finally:
         srv.close()
+
+
+@pytest.mark.parametrize("wide", [False, True], ids=["n1024", "n2048"])
+def test_server_tiled_keyswitch_rounds(F, cuda_ok, request, wide):
+    """A request of one level of independent NAND gates, large enough that its
+    round takes the tiled LWE key switch (1024 gates and more at N = 1024, two
+    gates per SM at N = 2048), whose outputs go to the server's pool slots
+    through an index array: every output word equals the batched call's on the
+    same inputs (integer words, bit-exact) and decrypts to the NAND."""
+    torch = cuda_ok
+    ctx = request.getfixturevalue("ctx1" if wide else "ctx0")
+    ks = request.getfixturevalue("keys1" if wide else "keys0")
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    count = 2 * sms + 16 if wide else 1100
+    rng = np.random.default_rng(91 + int(wide))
+    bits = rng.integers(0, 2, 2 * count).astype(np.uint8)
+    ct = ks.encrypt(bits, seed=700 + int(wide))
+    gates = [F.NAND] * count
+    in1 = list(range(0, 2 * count, 2))
+    in2 = list(range(1, 2 * count, 2))
+    srv = F.Server(ctx, max_batch=count, pool_ciphertexts=4 * count)
+    try:
+        rid, _ = srv.submit(ct, gates, in1, in2, count)
+        got = wait_all(srv, [rid], timeout_s=300)[rid]
+    finally:
+        srv.close()
+    assert got[0] == F.OK
+    direct = ctx.eval_bootstrap_batch(ct[0::2].copy(), ct[1::2].copy(), np.array(gates, dtype=np.int32))
+    assert np.array_equal(got[1], direct)
+    want = 1 - (bits[0::2] & bits[1::2])
+    assert np.array_equal(ks.decrypt(got[1]), want)
