@@ -138,6 +138,29 @@ __device__ __forceinline__ void store_btile(uint32_t *dst, const uint32_t (&x)[3
                                                                        x[4 * qq + 3]));
 }
 
+// load_btile / store_btile of an accumulator that the next step reads again:
+// the L2 evict-last policy (l2hint.cuh) keeps it in L2 while the key tiles
+// stream through.
+__device__ __forceinline__ void load_btile_keep(uint32_t (&x)[32], const uint32_t *src, int lane)
+{
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+    const uint64_t pol = l2_keep_policy();
+#pragma unroll
+    for (int qq = 0; qq < 8; qq++) {
+        const uint4 v = ld_keep(s4 + qq * 32 + lane, pol);
+        x[4 * qq] = v.x; x[4 * qq + 1] = v.y; x[4 * qq + 2] = v.z; x[4 * qq + 3] = v.w;
+    }
+}
+
+__device__ __forceinline__ void store_btile_keep(uint32_t *dst, const uint32_t (&x)[32], int lane)
+{
+    uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+    const uint64_t pol = l2_keep_policy();
+#pragma unroll
+    for (int qq = 0; qq < 8; qq++)
+        st_keep(d4 + qq * 32 + lane, make_uint4(x[4 * qq], x[4 * qq + 1], x[4 * qq + 2], x[4 * qq + 3]), pol);
+}
+
 // Plans period t + 1 of one pipeline (run by one thread of it while the other
 // threads multiply-accumulate period t's digit item). C is period t's plan, Nx
 // receives the next. The pipelines of a CTA share the group's items: a cursor
@@ -252,10 +275,11 @@ __device__ __noinline__ void pipe_init_item(const PipeArgs &A, const Ntt32Consts
 #pragma unroll
     for (int r = 0; r < 32; r++) x[r] = reduce32(x[r], mu32, c.Q);
     uint32_t *acc = A.accs + gid * 2048;
-    store_btile(acc + 1024, x, lane);
+    store_btile_keep(acc + 1024, x, lane);
     uint4 *a4 = reinterpret_cast<uint4 *>(acc);
+    const uint64_t pol = l2_keep_policy();
 #pragma unroll
-    for (int qq = 0; qq < 8; qq++) __stcg(a4 + qq * 32 + lane, make_uint4(0, 0, 0, 0));
+    for (int qq = 0; qq < 8; qq++) st_keep(a4 + qq * 32 + lane, make_uint4(0, 0, 0, 0), pol);
     __syncwarp();
 }
 
@@ -372,7 +396,7 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
                 if (ctl[6]) {
                     const int hp = pw - GW;
                     uint32_t x[32];
-                    load_btile(x, A.accs + (first + (size_t)ctl[1]) * 2048 + hp * 1024, lane);
+                    load_btile_keep(x, A.accs + (first + (size_t)ctl[1]) * 2048 + hp * 1024, lane);
                     uint32_t *ts = s.tslot[sh][hp];
                     ntt_inv_1024_noscale(x, c, inv_tw, ts, lane);
                     store_row(ts, lane, x);
@@ -399,7 +423,7 @@ __global__ void __launch_bounds__(NP * 32 * (2 * (DG - 1) + 2), MINB)
                 const uint4 *key = reinterpret_cast<const uint4 *>(A.btkey + ((size_t)gs * A.Br + rr) * rgsw_words);
                 uint4 *acc = reinterpret_cast<uint4 *>(A.accs + (first + (size_t)gk) * 2048);
                 for (int u = pw * 32 + lane; u < 256; u += PT)
-                    mac_chunk<DG, true>(u, key, s.dbuf, acc, c.Q, A.qinv_neg, acc);
+                    mac_chunk<DG, true, true>(u, key, s.dbuf, acc, c.Q, A.qinv_neg, acc);
             }
             pipe_barrier(1 + pl, PT);
             // the digit item is finished: other pipelines may issue its

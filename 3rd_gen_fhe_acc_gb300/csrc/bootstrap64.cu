@@ -18,6 +18,7 @@
 // (18 MB with companions) through L2 together; accumulators live in global
 // memory (32 KB per gate).
 #include "ctx.hpp"
+#include "l2hint.cuh"
 #include "ntt64.cuh"
 #include <algorithm>
 
@@ -68,7 +69,8 @@ __device__ __forceinline__ DigitTables64 build_digit_tables64(unsigned char *mem
 // keys were uploaded with K'_h = K_h - BG^(h-DG+1) K_last, K'_last =
 // BG^-(DG-1) K_last (Q < BG^DG, so sum_h BG^h NTT(digit_h) = acc).
 // With dt the digit transforms start from the digit tables (BG <= kMaxTableBG64).
-template <bool P>
+// KEEP: acc_nd is read with the L2 evict-last policy (l2hint.cuh).
+template <bool P, bool KEEP = false>
 __device__ __forceinline__ void step64(Step64SmemT<P> &s, const ulonglong2 *__restrict__ key, int DG, uint32_t bg_bits,
                                        const ulonglong2 *__restrict__ tw, const ulonglong2 *__restrict__ itw,
                                        const Ntt64Consts &c, const uint64_t *acc_nd, int tid, int bar,
@@ -108,7 +110,15 @@ __device__ __forceinline__ void step64(Step64SmemT<P> &s, const ulonglong2 *__re
 #pragma unroll
         for (int i = 0; i < 8; i++) {
             const int k = tid + 256 * i;
-            const uint64_t da = __ldcg(acc_nd + k), db = __ldcg(acc_nd + 2048 + k);
+            uint64_t da, db;
+            if (KEEP) {
+                const uint64_t pol = l2_keep_policy();
+                da = ld_keep64(acc_nd + k, pol);
+                db = ld_keep64(acc_nd + 2048 + k, pol);
+            } else {
+                da = __ldcg(acc_nd + k);
+                db = __ldcg(acc_nd + 2048 + k);
+            }
             const ulonglong2 a0 = __ldg(k0 + k), b0 = __ldg(k0 + 2048 + k);
             const ulonglong2 a1 = __ldg(k1 + k), b1 = __ldg(k1 + 2048 + k);
             sa[i] += shoup64(da, a0.x, a0.y, c.Q) + shoup64(db, a1.x, a1.y, c.Q);
@@ -355,10 +365,11 @@ __device__ __forceinline__ void br64_acc_init(const Br64Args &A, const Ntt64Cons
     if (tid >= 128) ntt64_fwd_2048<128, P>(buf, tw, c, tid - 128, bar + 2);
     group_sync(bar, kT64);
     uint64_t *acc = A.accs + gid * 4096;
+    const uint64_t pol = l2_keep_policy();
     for (int e = tid; e < 2048; e += kT64) {
-        acc[e] = 0;
+        st_keep64(acc + e, 0, pol);
         const uint64_t v = barrett64_2q(buf[pi<P>(e)], c.mu64, c.Q);
-        acc[2048 + e] = v >= c.Q ? v - c.Q : v;
+        st_keep64(acc + 2048 + e, v >= c.Q ? v - c.Q : v, pol);
     }
     group_sync(bar, kT64);
 }
@@ -592,9 +603,10 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
                 if (st < 0) break;
                 const uint32_t r = pool ? A.pool_res[(size_t)k * S + st] : res[k * S + st];
                 const uint64_t *acc = A.accs + ((pool ? A.pool_first : first) + (size_t)k) * 4096;
-                for (int e = tid; e < 4096; e += kT64) s.acc[e >> 11][px(e & 2047)] = __ldcg(acc + e);
+                const uint64_t pol = l2_keep_policy();
+                for (int e = tid; e < 4096; e += kT64) s.acc[e >> 11][px(e & 2047)] = ld_keep64(acc + e, pol);
                 group_sync(bar, kT64);
-                step64(s, A.btkey + ((size_t)st * A.Br + r) * rgsw_pairs, A.DG, A.bg_bits, tw, itw, c,
+                step64<true, true>(s, A.btkey + ((size_t)st * A.Br + r) * rgsw_pairs, A.DG, A.bg_bits, tw, itw, c,
                        A.derive_last ? acc : nullptr, tid, bar, A.digit_tables ? &dt : nullptr);
             }
             // the item again from the plan (not held in registers across the step;
@@ -603,7 +615,10 @@ __global__ void __launch_bounds__(W * kT64, MINB) br64_kernel(const __grid_const
             const int st = pv[0], k = pv[1], pool = pv[2];
             const size_t gid = (pool ? A.pool_first : first) + (size_t)k;
             uint64_t *acc = A.accs + gid * 4096;
-            for (int e = tid; e < 4096; e += kT64) __stcg(acc + e, s.acc[e >> 11][px(e & 2047)]);
+            {
+                const uint64_t pol = l2_keep_policy();
+                for (int e = tid; e < 4096; e += kT64) st_keep64(acc + e, s.acc[e >> 11][px(e & 2047)], pol);
+            }
             if (pool) __threadfence();
             group_sync(bar, kT64);
             if (tid == 0) {

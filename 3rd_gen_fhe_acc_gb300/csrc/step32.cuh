@@ -4,6 +4,7 @@
 // Reference: RLWE_mult_RGSW (FHE_ACC_runtime/src/RLWE.cpp:642-704) and
 // digit_decompose (RLWE.cpp:623-640).
 #pragma once
+#include "l2hint.cuh"
 #include "ntt32.cuh"
 
 namespace fheacc {
@@ -40,19 +41,23 @@ __device__ __forceinline__ uint32_t mont_reduce_2q(uint64_t s, uint32_t Q, uint3
 // key[h][p][P][e], Montgomery-reduced. With acc_nd (the item's NTT-domain
 // accumulator, B-tiled, read before it is overwritten) the last digit's term
 // uses acc_nd[p] in place of its NTT (keys uploaded for that identity).
-template <int DG, bool DERIVE = false>
+// KEEP: the accumulator is read and written with the L2 evict-last policy
+// (l2hint.cuh), for accumulators that the next step reads again.
+template <int DG, bool DERIVE = false, bool KEEP = false>
 __device__ __forceinline__ void mac_chunk(int u, const uint4 *__restrict__ key,
                                           const uint32_t (*dbuf)[kN32], uint4 *acc, uint32_t Q, uint32_t qinv_neg,
                                           const uint4 *acc_nd = nullptr)
 {
     constexpr int DT = DERIVE ? DG - 1 : DG;   // digit NTTs per poly in dbuf: [p * DT + h]
     const int pa = sw_chunk(u & 31, u >> 5);
+    const uint64_t pol = KEEP ? l2_keep_policy() : 0;
     uint64_t sa[4] = {0, 0, 0, 0}, sb[4] = {0, 0, 0, 0};
 #pragma unroll
     for (int qi = 0; qi < 2 * DG; qi++) {
         const int pp = qi / DG, hh = qi % DG;
-        const uint4 dv = (DERIVE && hh == DG - 1) ? __ldcg(acc_nd + pp * 256 + u)
-                                                  : *reinterpret_cast<const uint4 *>(dbuf[pp * DT + hh] + pa);
+        const uint4 dv = (DERIVE && hh == DG - 1)
+                             ? (KEEP ? ld_keep(acc_nd + pp * 256 + u, pol) : __ldcg(acc_nd + pp * 256 + u))
+                             : *reinterpret_cast<const uint4 *>(dbuf[pp * DT + hh] + pa);
         // keys stream through L2 only: an item's 64 KB would otherwise evict
         // the transforms' twiddle tables from the L1 left beside shared memory
         const uint4 a4 = __ldcg(key + ((hh * 2 + pp) * 2 + 0) * 256 + u);
@@ -62,10 +67,17 @@ __device__ __forceinline__ void mac_chunk(int u, const uint4 *__restrict__ key,
         sa[2] += (uint64_t)dv.z * a4.z; sb[2] += (uint64_t)dv.z * b4.z;
         sa[3] += (uint64_t)dv.w * a4.w; sb[3] += (uint64_t)dv.w * b4.w;
     }
-    __stcg(acc + u, make_uint4(mont_reduce_2q(sa[0], Q, qinv_neg), mont_reduce_2q(sa[1], Q, qinv_neg),
-                               mont_reduce_2q(sa[2], Q, qinv_neg), mont_reduce_2q(sa[3], Q, qinv_neg)));
-    __stcg(acc + 256 + u, make_uint4(mont_reduce_2q(sb[0], Q, qinv_neg), mont_reduce_2q(sb[1], Q, qinv_neg),
-                                     mont_reduce_2q(sb[2], Q, qinv_neg), mont_reduce_2q(sb[3], Q, qinv_neg)));
+    const uint4 ra = make_uint4(mont_reduce_2q(sa[0], Q, qinv_neg), mont_reduce_2q(sa[1], Q, qinv_neg),
+                                mont_reduce_2q(sa[2], Q, qinv_neg), mont_reduce_2q(sa[3], Q, qinv_neg));
+    const uint4 rb = make_uint4(mont_reduce_2q(sb[0], Q, qinv_neg), mont_reduce_2q(sb[1], Q, qinv_neg),
+                                mont_reduce_2q(sb[2], Q, qinv_neg), mont_reduce_2q(sb[3], Q, qinv_neg));
+    if (KEEP) {
+        st_keep(acc + u, ra, pol);
+        st_keep(acc + 256 + u, rb, pol);
+    } else {
+        __stcg(acc + u, ra);
+        __stcg(acc + 256 + u, rb);
+    }
 }
 
 // Shared-memory working set of one CTA.

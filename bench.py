@@ -980,6 +980,8 @@ def measure_batch(F, D, cache, preset, B, args, dev_id, n_steps, plain_sample, s
             tj = json.load(f)
         if B == 4096 and preset == 0:
             traffic = tj.get("br32_pipe", {}).get("bytes_per_launch_4096")
+        elif B == 2048 and preset == 1:
+            traffic = tj.get("br64", {}).get("bytes_per_launch_2048")
     hbm_peak = None
     peaks_src = "fallback 6800 GB/s"
     if os.path.exists(PEAKS_FILE):
