@@ -281,7 +281,7 @@ def profile_case(preset=0, gates=912, n=64):
     return 0 if ok == B else 1
 
 
-def run_serving(F, ctx, P, lsk, rate, duration, kmax=256, seed=7, max_batch=4096, pool=1 << 20):
+def run_serving(F, ctx, P, lsk, rate, duration, kmax=256, seed=7, max_batch=2048, pool=1 << 20):
     """Poisson stream of PSI equality queries (a 32-bit client item against
     k ~ U[1, kmax] encrypted server items: 32 XNOR + a 31-gate AND tree per
     item) at `rate` bootstraps/s for `duration` seconds through the
@@ -331,7 +331,7 @@ def run_serving(F, ctx, P, lsk, rate, duration, kmax=256, seed=7, max_batch=4096
     st = srv.stats()
     srv.close()
     return {"offered_bootstraps_per_s": rate, "requests": len(lat), "items_per_request": "U[1,%d]" % kmax,
-            "gates": int(st["gates"]), "rounds": int(st["rounds"]),
+            "max_batch": max_batch, "gates": int(st["gates"]), "rounds": int(st["rounds"]),
             "throughput_bootstraps_per_s": st["gates"] / elapsed, "duration_s": elapsed,
             "latency_ms_p50": float(np.percentile(lat, 50)), "latency_ms_p99": float(np.percentile(lat, 99)),
             "queue_ms_p99": float(np.percentile(queue, 99)), "gpu_busy_frac": st["busy_s"] / elapsed}
