@@ -1,4 +1,6 @@
-// lwe_ks.cu -- RLWE -> LWE key switch and modulus switch, 32-bit words.
+// lwe_ks.cu -- RLWE -> LWE key switch and modulus switch: the 32-bit words'
+// kernels, and the tiled form of both word widths (the 64-bit per-gate and
+// split forms are in bootstrap64.cu).
 //
 // Reference behaviour: LWE::LWE_keyswitch (FHE_ACC_runtime/src/LWE.cpp:233-253)
 // and LWE::LWE_modswitch / scale_round (LWE.cpp:255-269). The reference's FPGA
@@ -9,10 +11,11 @@
 // b[0]). For every coefficient i < N and digit j < digitKS the LWE row
 // kskey[d][j][i], d = base-Bks digit j of a[i], is subtracted.
 //
-// Batches of at least two gates per SM take the tiled form
-// (lwe_ks32_tiled_kernel): ks_digits_kernel first writes every gate's digits
-// gate-minor, [(i * digitKS + j)][gate]; then a CTA takes a block of gates and
-// a 128-word slice of the key rows and walks the N * digitKS row groups (the
+// Batches of 1024 gates and more take the tiled form (lwe_ks32_tiled_kernel;
+// 64-bit words from two gates per SM, lwe_ks64_tiled_kernel):
+// ks_digits_kernel first writes every gate's digits gate-minor,
+// [(i * digitKS + j)][gate]; then a CTA takes a block of gates and a 512-byte
+// slice of the key rows and walks the N * digitKS row groups (the
 // Bks rows of one (i, j)) in order, staging each group's row slices (and the
 // block's digits) in shared memory with cp.async, several groups ahead, while
 // each warp adds the slice its gates select. A row group is then read from L2
@@ -22,8 +25,8 @@
 //
 // Smaller batches: one CTA per ciphertext, the digits computed once into
 // shared memory, then the CTA walks the N * digitKS rows; a row is n+1
-// consecutive words, read by consecutive threads (coalesced). One or two
-// gates per launch split each gate's rows over many CTAs (ks_partial_kernel).
+// consecutive words, read by consecutive threads (coalesced). Below two gates
+// per SM each gate's rows are split over many CTAs (ks_partial_kernel).
 // Sums are kept in 64-bit registers without reduction (N * digitKS * Q <
 // 2^64) and reduced once at the end; the modulus switch is fused into the
 // same epilogue.
