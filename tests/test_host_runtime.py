@@ -196,3 +196,23 @@ def test_container_roundtrip_and_checks(F, keys0, tmp_path):
     with pytest.raises(F.FheaccError) as e:
         F.load(cpath, F.KIND_LWE_CT, P)               # corrupted payload
     assert e.value.code == F.EIO
+
+
+def test_keyswitch_digit_quotients_exact(F):
+    """The 64-bit tiled key switch takes each base-Bks digit's quotient as
+    floor(a m / 2^64) with m = ceil(2^64 / Bks), which equals floor(a / Bks)
+    whenever a (m Bks - 2^64) < 2^64: true for every word below Q of the
+    64-bit preset. Checked on the extreme words and random ones, digit by digit
+    as the kernel walks them (the quotient becomes the next word)."""
+    import random
+    P = F.params_preset(1)
+    Q, B = int(P.Q), int(P.Bks)
+    m = ((1 << 64) - 1) // B + 1
+    assert Q * (m * B - (1 << 64)) < (1 << 64)
+    rng = random.Random(5)
+    words = [0, 1, B - 1, B, Q - 1, Q // 2, Q - B] + [rng.randrange(Q) for _ in range(20000)]
+    for a in words:
+        for _ in range(int(P.digitKS)):
+            q = (a * m) >> 64
+            assert q == a // B and a - q * B == a % B
+            a = q
