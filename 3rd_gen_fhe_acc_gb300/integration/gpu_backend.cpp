@@ -330,6 +330,20 @@ std::unique_ptr<std::vector<RLWE::RLWE_ciphertext>> fpga_expand_RLWE(const RLWE:
     return result;
 }
 
+std::unique_ptr<std::vector<RLWE::RLWE_ciphertext>> fpga_expand_RLWE_cont_rd_wr(const RLWE::RLWE_ciphertext &c1,
+                                                                                const pci_bar_handle_t bar, int *rc,
+                                                                                int read_fd, int write_fd)
+{
+    return fpga_expand_RLWE(c1, bar, rc, read_fd, write_fd);
+}
+
+std::unique_ptr<std::vector<RLWE::RLWE_ciphertext>> fpga_expand_RLWE_batch_rd_wr(const RLWE::RLWE_ciphertext &c1,
+                                                                                 const pci_bar_handle_t bar, int *rc,
+                                                                                 int read_fd, int write_fd)
+{
+    return fpga_expand_RLWE(c1, bar, rc, read_fd, write_fd);
+}
+
 std::shared_ptr<std::vector<RLWE::RGSW_ciphertext>> fpga_homo_expand(
     const std::unique_ptr<std::vector<RLWE::RLWE_ciphertext>> &packed_bits, const pci_bar_handle_t, int *rc, int,
     int)

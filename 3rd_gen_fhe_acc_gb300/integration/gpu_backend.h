@@ -80,6 +80,15 @@ std::vector<LWE::LWE_ciphertext> fpga_eval_bootstrap_x16(const std::vector<LWE::
 std::unique_ptr<std::vector<RLWE::RLWE_ciphertext>> fpga_expand_RLWE(const RLWE::RLWE_ciphertext &c1,
                                                                      const pci_bar_handle_t ocl_bar_handle, int *rc,
                                                                      int read_fd, int write_fd);
+// The reference's two DMA-issue variants of expand_RLWE (continuous and
+// batched reads and writes, myfpga.cpp:1797-1956 and 1959-2275) compute the
+// same N RLWEs; here they are the same device call.
+std::unique_ptr<std::vector<RLWE::RLWE_ciphertext>> fpga_expand_RLWE_cont_rd_wr(const RLWE::RLWE_ciphertext &c1,
+                                                                                const pci_bar_handle_t ocl_bar_handle,
+                                                                                int *rc, int read_fd, int write_fd);
+std::unique_ptr<std::vector<RLWE::RLWE_ciphertext>> fpga_expand_RLWE_batch_rd_wr(const RLWE::RLWE_ciphertext &c1,
+                                                                                 const pci_bar_handle_t ocl_bar_handle,
+                                                                                 int *rc, int read_fd, int write_fd);
 // homo_expand on the device (myfpga.cpp:2278-2452): digitG packed RLWEs to N
 // RGSWs. Needs dma_write_subs_key and dma_write_RGSW_enc_sk.
 std::shared_ptr<std::vector<RLWE::RGSW_ciphertext>> fpga_homo_expand(

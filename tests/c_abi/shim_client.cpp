@@ -213,6 +213,16 @@ int main()
     CHECK(GPU::dma_write_RGSW_enc_sk(0, rgsw_of(rgsw.data())) == 0);
     auto ex = GPU::fpga_expand_RLWE(rlwe_of(packed.data()), bar, &rc, -1, -1);
     CHECK(rc == 0 && ex && ex->size() == (size_t)N);
+    // the reference's DMA-issue variants of expand_RLWE give the same RLWEs
+    auto ex_cont = GPU::fpga_expand_RLWE_cont_rd_wr(rlwe_of(packed.data()), bar, &rc, -1, -1);
+    CHECK(rc == 0 && ex_cont && ex_cont->size() == (size_t)N);
+    auto ex_batch = GPU::fpga_expand_RLWE_batch_rd_wr(rlwe_of(packed.data()), bar, &rc, -1, -1);
+    CHECK(rc == 0 && ex_batch && ex_batch->size() == (size_t)N);
+    for (int i = 0; i < N; i++)
+        for (int k = 0; k < N; k++) {
+            CHECK((*ex_cont)[i].a[k] == (*ex)[i].a[k] && (*ex_cont)[i].b[k] == (*ex)[i].b[k]);
+            CHECK((*ex_batch)[i].a[k] == (*ex)[i].a[k] && (*ex_batch)[i].b[k] == (*ex)[i].b[k]);
+        }
     auto packs = std::make_unique<std::vector<RLWE::RLWE_ciphertext>>();
     for (uint64_t j = 0; j < digitG; j++) packs->push_back(rlwe_of(&packed[j * 2 * (size_t)N]));
     auto he = GPU::fpga_homo_expand(packs, bar, &rc, -1, -1);

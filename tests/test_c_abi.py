@@ -67,8 +67,9 @@ def test_gpu_backend_builds_with_client(F, tmp_path):
 @pytest.mark.gpu
 def test_gpu_backend_runs_fpga_calls(F, tmp_path):
     """Through GPU::fpga_eval_bootstrap_x4/x8/x12/x16/x1 (4, 8, 12 and exactly
-    10 gates; refused sizes and c1 == c2 give rc = -1), fpga_expand_RLWE and
-    fpga_homo_expand: outputs decrypt and equal the C ABI's words."""
+    10 gates; refused sizes and c1 == c2 give rc = -1), fpga_expand_RLWE (and
+    its _cont_rd_wr and _batch_rd_wr variants) and fpga_homo_expand: outputs
+    decrypt and equal the C ABI's words."""
     exe = str(tmp_path / "shim_client")
     _build_shim_client(F, exe)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=900)
