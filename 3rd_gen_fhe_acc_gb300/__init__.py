@@ -43,7 +43,7 @@ KIND_LWE_SK, KIND_RLWE_SK, KIND_BOOTSTRAP_KEY, KIND_LWE_KS_KEY, KIND_SUBS_KEY, K
     KIND_RGSW_CT = range(1, 9)
 
 OK = 0
-EINVAL, ENOMEM, ENODEV, EIO, ETIMEDOUT, ENOKEY, EBUSY = -22, -12, -19, -5, -110, -126, -16
+EINVAL, ENOMEM, ENODEV, EIO, ETIMEDOUT, ENOKEY, EBUSY, EMISMATCH = -22, -12, -19, -5, -110, -126, -16, -74
 
 _u64p = ctypes.POINTER(ctypes.c_uint64)
 _u8p = ctypes.POINTER(ctypes.c_uint8)
@@ -136,6 +136,8 @@ def lib():
             "fheacc_upload_bootstrap_key": (ctypes.c_int, [vp, _u64p, sz]),
             "fheacc_upload_lwe_ks_key": (ctypes.c_int, [vp, _u64p, sz]),
             "fheacc_upload_subs_key": (ctypes.c_int, [vp, _u64p, sz]),
+            "fheacc_verify_bootstrap_key": (ctypes.c_int, [vp, _u64p, sz]),
+            "fheacc_verify_subs_key": (ctypes.c_int, [vp, _u64p, sz]),
             "fheacc_bootstrap": (ctypes.c_int, [vp, _u64p, _u64p, _i32p, sz, _u64p, ctypes.c_uint32]),
             "fheacc_bootstrap_async": (ctypes.c_int, [vp, vp, vp, vp, sz, vp, ctypes.c_uint32, vp]),
             "fheacc_bootstrap_plain_async": (ctypes.c_int, [vp, vp, vp, vp, sz, vp, ctypes.c_uint32, vp]),
@@ -381,6 +383,25 @@ class Context:
         """dma_write_subs_key (myfpga.cpp:658-712)."""
         subs = np.ascontiguousarray(subs, dtype=np.uint64)
         self.check(lib().fheacc_upload_subs_key(self._h, _p64(subs), subs.size))
+
+    def verify_bootstrap_key(self, btkey):
+        """dma_read_compare_bootstrap_key (myfpga.cpp:772-851): True if the
+        device copy is what uploading btkey makes, False if it differs."""
+        btkey = np.ascontiguousarray(btkey, dtype=np.uint64)
+        rc = lib().fheacc_verify_bootstrap_key(self._h, _p64(btkey), btkey.size)
+        if rc == EMISMATCH:
+            return False
+        self.check(rc)
+        return True
+
+    def verify_subs_key(self, subs):
+        """dma_read_compare_subs_key (myfpga.cpp:853-925), as verify_bootstrap_key."""
+        subs = np.ascontiguousarray(subs, dtype=np.uint64)
+        rc = lib().fheacc_verify_subs_key(self._h, _p64(subs), subs.size)
+        if rc == EMISMATCH:
+            return False
+        self.check(rc)
+        return True
 
     def eval_bootstrap_batch(self, c1, c2, gates, flags=0):
         """eval_bootstrap (RLWE.cpp:726-786) of every (c1[i], c2[i], gates[i]),

@@ -405,18 +405,20 @@ size_t fheacc_device_bytes(const fheacc_ctx *ctx)
     return ctx ? reinterpret_cast<const Context *>(ctx)->device_bytes() : 0;
 }
 
-int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t words)
+// One pass over the bootstrap key in device order, one step (all residues) per
+// chunk: upload (verify = false), or compare each chunk as the upload would
+// make it with the resident copy (verify = true; FHEACC_EMISMATCH at the first
+// chunk that differs).
+static int bootstrap_key_pass(Context &c, const uint64_t *btkey, size_t words, bool verify)
 {
-    if (!ctx) return FHEACC_EINVAL;
-    Context &c = *reinterpret_cast<Context *>(ctx);
-    if (!btkey || words != fheacc_bootstrap_key_words(&c.p)) return c.fail(FHEACC_EINVAL, "bootstrap key size mismatch");
-    DeviceGuard g(c.device);
     const size_t n = c.p.n, dR = c.p.digitR, Br = c.p.Br;
     const size_t rw = (size_t)c.p.digitG * 4 * c.p.N;
     const uint64_t Q = c.p.Q;
+    if (verify && !(c.wide ? (void *)c.d_btkey64 : (void *)c.d_btkey))
+        return c.fail(FHEACC_ENOKEY, "bootstrap key not uploaded");
     if (c.wide) {
         // device order, one step (all residues) per chunk, Shoup pairs made on the GPU
-        if (!c.d_btkey64) {
+        if (!verify && !c.d_btkey64) {
             cudaError_t e = cudaMalloc(&c.d_btkey64, words * sizeof(ulonglong2));
             if (e != cudaSuccess) {
                 cudaGetLastError();
@@ -427,8 +429,18 @@ int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t w
         }
         std::vector<uint64_t> stage(Br * rw);
         uint64_t *d_stage = nullptr;
+        ulonglong2 *d_check = nullptr;   // verify: the chunk as the upload makes it
+        std::vector<ulonglong2> made, held;
         cudaError_t e = cudaMalloc(&d_stage, Br * rw * sizeof(uint64_t));
-        if (e != cudaSuccess) return c.cuda_fail(e, "key staging");
+        if (e == cudaSuccess && verify) {
+            e = cudaMalloc(&d_check, Br * rw * sizeof(ulonglong2));
+            made.resize(Br * rw);
+            held.resize(Br * rw);
+        }
+        if (e != cudaSuccess) {
+            cudaFree(d_stage);
+            return c.cuda_fail(e, "key staging");
+        }
         int rc = FHEACC_OK;
         const bool derive = c.dp.last_digit_from_acc != 0;
         for (size_t i = 0; i < n && !rc; i++) {
@@ -438,14 +450,23 @@ int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t w
                 e = cudaMemcpy(d_stage, stage.data(), Br * rw * sizeof(uint64_t), cudaMemcpyHostToDevice);
                 if (e != cudaSuccess) rc = c.cuda_fail(e, "key upload");
                 else if (derive) rc = launch_derive_keys64(c, d_stage, Br, c.d_cf64, c.stream);
-                if (!rc) rc = launch_shoup_pairs64(c, d_stage, c.d_btkey64 + (i * dR + j) * Br * rw, Br * rw, c.stream);
+                ulonglong2 *chunk = c.d_btkey64 + (i * dR + j) * Br * rw;
+                if (!rc) rc = launch_shoup_pairs64(c, d_stage, verify ? d_check : chunk, Br * rw, c.stream);
                 if (!rc && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = c.cuda_fail(cudaGetLastError(), "key pairs");
+                if (!rc && verify) {
+                    e = cudaMemcpy(made.data(), d_check, Br * rw * sizeof(ulonglong2), cudaMemcpyDeviceToHost);
+                    if (e == cudaSuccess) e = cudaMemcpy(held.data(), chunk, Br * rw * sizeof(ulonglong2), cudaMemcpyDeviceToHost);
+                    if (e != cudaSuccess) rc = c.cuda_fail(e, "key read-back");
+                    else if (std::memcmp(made.data(), held.data(), Br * rw * sizeof(ulonglong2)) != 0)
+                        rc = c.fail(FHEACC_EMISMATCH, "device bootstrap key differs from the given key");
+                }
             }
         }
         cudaFree(d_stage);
+        cudaFree(d_check);
         return rc;
     }
-    if (!c.d_btkey) {
+    if (!verify && !c.d_btkey) {
         cudaError_t e = cudaMalloc(&c.d_btkey, words * sizeof(uint32_t));
         if (e != cudaSuccess) {
             cudaGetLastError();
@@ -473,7 +494,7 @@ int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t w
         return v >= Q ? v - Q : v;
     };
     const bool derive = c.dp.last_digit_from_acc != 0;
-    std::vector<uint32_t> stage(Br * rw);
+    std::vector<uint32_t> stage(Br * rw), held(verify ? Br * rw : 0);
     std::vector<uint64_t> row(rw);
     for (size_t i = 0; i < n; i++) {
         for (size_t j = 0; j < dR; j++) {
@@ -495,11 +516,37 @@ int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t w
                     dst[(x & ~(size_t)1023) + btile_index(x & 1023)] = (uint32_t)(v >= Q ? v - Q : v);
                 }
             }
-            int rc = upload_u32(c, c.d_btkey + (i * dR + j) * Br * rw, stage.data(), Br * rw);
+            uint32_t *chunk = c.d_btkey + (i * dR + j) * Br * rw;
+            if (verify) {
+                cudaError_t e = cudaMemcpy(held.data(), chunk, Br * rw * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+                if (e != cudaSuccess) return c.cuda_fail(e, "key read-back");
+                if (std::memcmp(held.data(), stage.data(), Br * rw * sizeof(uint32_t)) != 0)
+                    return c.fail(FHEACC_EMISMATCH, "device bootstrap key differs from the given key");
+                continue;
+            }
+            int rc = upload_u32(c, chunk, stage.data(), Br * rw);
             if (rc) return rc;
         }
     }
     return FHEACC_OK;
+}
+
+int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t words)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    if (!btkey || words != fheacc_bootstrap_key_words(&c.p)) return c.fail(FHEACC_EINVAL, "bootstrap key size mismatch");
+    DeviceGuard g(c.device);
+    return bootstrap_key_pass(c, btkey, words, false);
+}
+
+int fheacc_verify_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t words)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    if (!btkey || words != fheacc_bootstrap_key_words(&c.p)) return c.fail(FHEACC_EINVAL, "bootstrap key size mismatch");
+    DeviceGuard g(c.device);
+    return bootstrap_key_pass(c, btkey, words, true);
 }
 
 int fheacc_upload_lwe_ks_key(fheacc_ctx *ctx, const uint64_t *kskey, size_t words)
@@ -552,14 +599,15 @@ int fheacc_upload_lwe_ks_key(fheacc_ctx *ctx, const uint64_t *kskey, size_t word
     return FHEACC_OK;
 }
 
-int fheacc_upload_subs_key(fheacc_ctx *ctx, const uint64_t *subs_key, size_t words)
+// Upload of the substitute key (verify = false), or comparison of the words the
+// upload would make with the resident copy (verify = true; FHEACC_EMISMATCH if
+// they differ).
+static int subs_key_pass(Context &c, const uint64_t *subs_key, size_t words, bool verify)
 {
-    if (!ctx) return FHEACC_EINVAL;
-    Context &c = *reinterpret_cast<Context *>(ctx);
-    if (!subs_key || words != fheacc_subs_key_words(&c.p)) return c.fail(FHEACC_EINVAL, "substitute key size mismatch");
-    DeviceGuard g(c.device);
+    if (verify && !(c.wide ? (void *)c.d_subs64 : (void *)c.d_subs))
+        return c.fail(FHEACC_ENOKEY, "substitute key not uploaded");
     if (c.wide) {
-        if (!c.d_subs64) {
+        if (!verify && !c.d_subs64) {
             cudaError_t e = cudaMalloc(&c.d_subs64, words * sizeof(ulonglong2));
             if (e != cudaSuccess) {
                 cudaGetLastError();
@@ -569,18 +617,30 @@ int fheacc_upload_subs_key(fheacc_ctx *ctx, const uint64_t *subs_key, size_t wor
             c.subs_bytes = words * sizeof(ulonglong2);
         }
         uint64_t *d_stage = nullptr;
+        ulonglong2 *d_check = nullptr;   // verify: the pairs as the upload makes them
         cudaError_t e = cudaMalloc(&d_stage, words * sizeof(uint64_t));
+        if (e == cudaSuccess && verify) e = cudaMalloc(&d_check, words * sizeof(ulonglong2));
         if (e == cudaSuccess) e = cudaMemcpy(d_stage, subs_key, words * sizeof(uint64_t), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) {
             cudaFree(d_stage);
+            cudaFree(d_check);
             return c.cuda_fail(e, "substitute key upload");
         }
-        int rc = launch_shoup_pairs64(c, d_stage, c.d_subs64, words, c.stream);
+        int rc = launch_shoup_pairs64(c, d_stage, verify ? d_check : c.d_subs64, words, c.stream);
         if (!rc && cudaStreamSynchronize(c.stream) != cudaSuccess) rc = c.cuda_fail(cudaGetLastError(), "key pairs");
+        if (!rc && verify) {
+            std::vector<ulonglong2> made(words), held(words);
+            e = cudaMemcpy(made.data(), d_check, words * sizeof(ulonglong2), cudaMemcpyDeviceToHost);
+            if (e == cudaSuccess) e = cudaMemcpy(held.data(), c.d_subs64, words * sizeof(ulonglong2), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess) rc = c.cuda_fail(e, "key read-back");
+            else if (std::memcmp(made.data(), held.data(), words * sizeof(ulonglong2)) != 0)
+                rc = c.fail(FHEACC_EMISMATCH, "device substitute key differs from the given key");
+        }
         cudaFree(d_stage);
+        cudaFree(d_check);
         return rc;
     }
-    if (!c.d_subs) {
+    if (!verify && !c.d_subs) {
         cudaError_t e = cudaMalloc(&c.d_subs, words * sizeof(uint32_t));
         if (e != cudaSuccess) {
             cudaGetLastError();
@@ -591,7 +651,31 @@ int fheacc_upload_subs_key(fheacc_ctx *ctx, const uint64_t *subs_key, size_t wor
     }
     std::vector<uint32_t> stage(words);
     for (size_t x = 0; x < words; x++) stage[x] = (uint32_t)(subs_key[x] % c.p.Q);
-    return upload_u32(c, c.d_subs, stage.data(), words);
+    if (!verify) return upload_u32(c, c.d_subs, stage.data(), words);
+    std::vector<uint32_t> held(words);
+    cudaError_t e = cudaMemcpy(held.data(), c.d_subs, words * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return c.cuda_fail(e, "key read-back");
+    return std::memcmp(held.data(), stage.data(), words * sizeof(uint32_t)) == 0
+               ? FHEACC_OK
+               : c.fail(FHEACC_EMISMATCH, "device substitute key differs from the given key");
+}
+
+int fheacc_upload_subs_key(fheacc_ctx *ctx, const uint64_t *subs_key, size_t words)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    if (!subs_key || words != fheacc_subs_key_words(&c.p)) return c.fail(FHEACC_EINVAL, "substitute key size mismatch");
+    DeviceGuard g(c.device);
+    return subs_key_pass(c, subs_key, words, false);
+}
+
+int fheacc_verify_subs_key(fheacc_ctx *ctx, const uint64_t *subs_key, size_t words)
+{
+    if (!ctx) return FHEACC_EINVAL;
+    Context &c = *reinterpret_cast<Context *>(ctx);
+    if (!subs_key || words != fheacc_subs_key_words(&c.p)) return c.fail(FHEACC_EINVAL, "substitute key size mismatch");
+    DeviceGuard g(c.device);
+    return subs_key_pass(c, subs_key, words, true);
 }
 
 int fheacc_bootstrap_async(fheacc_ctx *ctx, const uint64_t *d_c1, const uint64_t *d_c2, const int32_t *d_gates,

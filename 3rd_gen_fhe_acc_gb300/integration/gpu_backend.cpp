@@ -178,10 +178,12 @@ int OCL_config_wr_rd(const int slot_id)
 int BAR1_ROU_table_2k_wr(const int slot_id) { return slot_of(slot_id) ? 0 : -1; }
 int BAR1_ROU_table_1k_wr(const int slot_id) { return slot_of(slot_id) ? 0 : -1; }
 
-int dma_write_bootstrap_key(const int slot_id, const RLWE::bootstrap_key &bt_key)
+namespace {
+
+// The runtime's key objects as the C ABI's words (btkey[r][j][i].c_text[h][g],
+// subs_key[l].RLWE_kskey[k]).
+std::vector<uint64_t> flat_bootstrap_key(const RLWE::bootstrap_key &bt_key)
 {
-    Slot *s = slot_of(slot_id);
-    if (!s) return -1;
     std::vector<uint64_t> w;
     w.reserve((size_t)Br * digitR * n * digitG * 4 * N);
     for (uint64_t r = 0; r < Br; r++)
@@ -191,13 +193,11 @@ int dma_write_bootstrap_key(const int slot_id, const RLWE::bootstrap_key &bt_key
                 w.resize(at + (size_t)digitG * 4 * N);
                 flat_rgsw(bt_key.btkey[r][j][i], &w[at]);
             }
-    return fpga_rc(fheacc_upload_bootstrap_key(s->ctx, w.data(), w.size()));
+    return w;
 }
 
-int dma_write_subs_key(const int slot_id, const application::substitute_key &subs_key)
+std::vector<uint64_t> flat_subs_key(const application::substitute_key &subs_key)
 {
-    Slot *s = slot_of(slot_id);
-    if (!s) return -1;
     std::vector<uint64_t> w;
     w.reserve((size_t)digitN * digitKS_R * 2 * N);
     for (const auto &level : subs_key.subs_key)
@@ -206,9 +206,63 @@ int dma_write_subs_key(const int slot_id, const application::substitute_key &sub
             w.resize(at + 2 * (size_t)N);
             flat_rlwe(c, &w[at]);
         }
+    return w;
+}
+
+// a read-back comparison's rc: 0 equal, -ENOMEM, -1 otherwise (a difference included)
+int compare_rc(int code) { return code == FHEACC_OK ? 0 : code == FHEACC_ENOMEM ? -ENOMEM : -1; }
+
+}  // namespace
+
+int check_slot_config(int slot_id)
+{
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return slot_id >= 0 && slot_id < count && slot_id < kSlots ? 0 : 1;
+}
+
+uint64_t buffer_compare(uint8_t *bufa, uint8_t *bufb, size_t buffer_size)
+{
+    uint64_t differ = 0;
+    for (size_t i = 0; i < buffer_size; i++) differ += bufa[i] != bufb[i];
+    return differ;
+}
+
+int dma_write_bootstrap_key(const int slot_id, const RLWE::bootstrap_key &bt_key)
+{
+    Slot *s = slot_of(slot_id);
+    if (!s) return -1;
+    const std::vector<uint64_t> w = flat_bootstrap_key(bt_key);
+    return fpga_rc(fheacc_upload_bootstrap_key(s->ctx, w.data(), w.size()));
+}
+
+int dma_write_subs_key(const int slot_id, const application::substitute_key &subs_key)
+{
+    Slot *s = slot_of(slot_id);
+    if (!s) return -1;
+    const std::vector<uint64_t> w = flat_subs_key(subs_key);
     const int r = fheacc_upload_subs_key(s->ctx, w.data(), w.size());
     s->subs = r == FHEACC_OK;
     return fpga_rc(r);
+}
+
+int dma_read_compare_bootstrap_key(const int slot_id, const RLWE::bootstrap_key &bt_key)
+{
+    Slot *s = slot_of(slot_id);
+    if (!s) return -1;
+    const std::vector<uint64_t> w = flat_bootstrap_key(bt_key);
+    return compare_rc(fheacc_verify_bootstrap_key(s->ctx, w.data(), w.size()));
+}
+
+int dma_read_compare_subs_key(const int slot_id, const application::substitute_key &subs_key)
+{
+    Slot *s = slot_of(slot_id);
+    if (!s) return -1;
+    const std::vector<uint64_t> w = flat_subs_key(subs_key);
+    return compare_rc(fheacc_verify_subs_key(s->ctx, w.data(), w.size()));
 }
 
 int dma_write_RGSW_enc_sk(const int slot_id, const RLWE::RGSW_ciphertext &enc_sec)
@@ -230,6 +284,28 @@ int dma_write_RGSW_enc_sk(const int slot_id, const RLWE::RGSW_ciphertext &enc_se
         return e == cudaErrorMemoryAllocation ? -ENOMEM : -1;
     }
     return 0;
+}
+
+int dma_read_compare_RGSW_enc_sk(const int slot_id, const RLWE::RGSW_ciphertext &enc_sec)
+{
+    Slot *s = slot_of(slot_id);
+    if (!s || !s->d_enc_sec) return -1;
+    const size_t words = (size_t)digitG * 4 * N;
+    std::vector<uint64_t> want(words), held(words);
+    flat_rgsw(enc_sec, want.data());
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaSetDevice(slot_id);
+    const cudaError_t e = cudaMemcpy(held.data(), s->d_enc_sec, words * sizeof(uint64_t), cudaMemcpyDeviceToHost);
+    cudaSetDevice(dev);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return buffer_compare(reinterpret_cast<uint8_t *>(want.data()), reinterpret_cast<uint8_t *>(held.data()),
+                          words * sizeof(uint64_t)) == 0
+               ? 0
+               : -1;
 }
 
 LWE::LWE_ciphertext fpga_eval_bootstrap_x1(const LWE::LWE_ciphertext &c1, const LWE::LWE_ciphertext &c2,

@@ -30,6 +30,12 @@ typedef int pci_bar_handle_t;
 
 namespace GPU {
 
+// 0 if `slot_id` names a CUDA device this backend can use, 1 otherwise
+// (check_slot_config, myfpga.cpp:8-62, checks the FPGA image of the slot).
+int check_slot_config(int slot_id);
+// Number of differing bytes of two buffers (buffer_compare, myfpga.cpp:68-80).
+uint64_t buffer_compare(uint8_t *bufa, uint8_t *bufb, size_t buffer_size);
+
 // Creates the device context of `slot_id` (a CUDA device index) from the
 // runtime's global parameters (params.h). Replaces OCL_config_wr_rd
 // (myfpga.cpp:82-326). 0 on success, -1 on failure.
@@ -43,6 +49,13 @@ int BAR1_ROU_table_1k_wr(const int slot_id);
 int dma_write_bootstrap_key(const int slot_id, const RLWE::bootstrap_key &bt_key);
 int dma_write_subs_key(const int slot_id, const application::substitute_key &subs_key);
 int dma_write_RGSW_enc_sk(const int slot_id, const RLWE::RGSW_ciphertext &enc_sec);
+// Read-back verifiers (dma_read_compare_bootstrap_key, _subs_key,
+// _RGSW_enc_sk; myfpga.cpp:772-1000): 0 if the slot's device copy is what
+// uploading the given key makes (fheacc_verify_bootstrap_key,
+// fheacc_verify_subs_key), -1 if it differs or was never uploaded.
+int dma_read_compare_bootstrap_key(const int slot_id, const RLWE::bootstrap_key &bt_key);
+int dma_read_compare_subs_key(const int slot_id, const application::substitute_key &subs_key);
+int dma_read_compare_RGSW_enc_sk(const int slot_id, const RLWE::RGSW_ciphertext &enc_sec);
 
 // Gate bootstrapping (myfpga.cpp:1003-1660). The FPGA runtime key-switches
 // on the host and passes the key each call; here the key switch runs on the

@@ -36,6 +36,7 @@ extern "C" {
 #define FHEACC_ETIMEDOUT (-110)  /* fheacc_sync / bounded device wait expired */
 #define FHEACC_ENOKEY    (-126)  /* required key not uploaded               */
 #define FHEACC_EBUSY     (-16)   /* serving queue full                       */
+#define FHEACC_EMISMATCH (-74)   /* device key differs from the given key    */
 
 /* flags for the bootstrap calls */
 #define FHEACC_FLAG_FPGA_COMPAT 1u  /* also apply residue-0 keys, as
@@ -159,6 +160,16 @@ size_t fheacc_device_bytes(const fheacc_ctx *ctx);
 int fheacc_upload_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t words);
 int fheacc_upload_lwe_ks_key(fheacc_ctx *ctx, const uint64_t *kskey, size_t words);
 int fheacc_upload_subs_key(fheacc_ctx *ctx, const uint64_t *subs_key, size_t words);
+
+/* Read-back verification of a resident key: FHEACC_OK if the device copy is
+ * word for word what uploading `btkey` / `subs_key` (same formats and sizes as
+ * the uploads) would make, FHEACC_EMISMATCH at the first step tile (bootstrap
+ * key) or key (substitute key) that differs, FHEACC_ENOKEY if none was
+ * uploaded. Blocking; temporary device memory of one step tile (64-bit words:
+ * the whole substitute key). Replace dma_read_compare_bootstrap_key
+ * (myfpga.cpp:772-851) and dma_read_compare_subs_key (myfpga.cpp:853-925). */
+int fheacc_verify_bootstrap_key(fheacc_ctx *ctx, const uint64_t *btkey, size_t words);
+int fheacc_verify_subs_key(fheacc_ctx *ctx, const uint64_t *subs_key, size_t words);
 
 /* Gate bootstrapping of `count` independent gates, HOST buffers, blocking:
  * out[i] = eval_bootstrap(c1[i], c2[i], gates[i]) (RLWE.cpp:726-786).

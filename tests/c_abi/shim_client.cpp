@@ -1,7 +1,7 @@
 // Drives the GPU:: backend (3rd_gen_fhe_acc_gb300/integration/gpu_backend.cpp)
 // the way the runtime's FPGA tests drive FPGA:: (test.cpp:2013-3538):
-// configure slot 0 from the runtime's globals, upload the keys, bootstrap
-// through the fixed-width calls, expand. Keys and ciphertexts come from
+// configure slot 0 from the runtime's globals, upload and read back the keys,
+// bootstrap through the fixed-width calls, expand. Keys and ciphertexts come from
 // libfheacc's seeded host generator; every bootstrap output is decrypted and
 // compared word for word with libfheacc's own host-buffer call, and the expand
 // outputs with the C ABI's device calls. Built against the runtime's headers
@@ -151,6 +151,25 @@ int main()
     CHECK(GPU::dma_write_bootstrap_key(0, bk) == 0);
     CHECK(GPU::dma_write_subs_key(0, sk) == 0);
 
+    // slot check, byte compare and the read-back verifiers: the keys just
+    // uploaded compare equal, a copy with one word changed does not
+    CHECK(GPU::check_slot_config(0) == 0 && GPU::check_slot_config(-1) == 1 && GPU::check_slot_config(4096) == 1);
+    {
+        uint8_t u[8] = {1, 2, 3, 4, 5, 6, 7, 8}, v[8] = {1, 0, 3, 4, 0, 6, 7, 0};
+        CHECK(GPU::buffer_compare(u, v, 8) == 3 && GPU::buffer_compare(u, u, 8) == 0);
+    }
+    CHECK(GPU::dma_read_compare_bootstrap_key(0, bk) == 0);
+    CHECK(GPU::dma_read_compare_subs_key(0, sk) == 0);
+    {
+        RLWE::bootstrap_key bad = bk;
+        bad.btkey[3][1][7].c_text[2][1].a[5] ^= 1;
+        CHECK(GPU::dma_read_compare_bootstrap_key(0, bad) == -1);
+        application::substitute_key bad_sk = sk;
+        bad_sk.subs_key[4].RLWE_kskey[1].b[9] ^= 1;
+        CHECK(GPU::dma_read_compare_subs_key(0, bad_sk) == -1);
+        CHECK(GPU::dma_read_compare_bootstrap_key(1000, bk) == -1);
+    }
+
     // twelve gates of random bits
     const int K = 12;
     std::vector<uint8_t> bits(2 * K), x(K), y(K);
@@ -210,7 +229,14 @@ int main()
     for (uint64_t j = 0; j < digitG; j++)
         CHECK(fheacc_rlwe_encrypt(&P, 100 + j, rsk.data(), msg.data(), &packed[j * 2 * (size_t)N]) == FHEACC_OK);
     CHECK(fheacc_rgsw_encrypt(&P, 41, rsk.data(), msg.data(), rgsw.data()) == FHEACC_OK);
+    CHECK(GPU::dma_read_compare_RGSW_enc_sk(0, rgsw_of(rgsw.data())) == -1);   // not uploaded yet
     CHECK(GPU::dma_write_RGSW_enc_sk(0, rgsw_of(rgsw.data())) == 0);
+    CHECK(GPU::dma_read_compare_RGSW_enc_sk(0, rgsw_of(rgsw.data())) == 0);
+    {
+        std::vector<uint64_t> bad(rgsw);
+        bad[gw / 2 + 3] ^= 1;
+        CHECK(GPU::dma_read_compare_RGSW_enc_sk(0, rgsw_of(bad.data())) == -1);
+    }
     auto ex = GPU::fpga_expand_RLWE(rlwe_of(packed.data()), bar, &rc, -1, -1);
     CHECK(rc == 0 && ex && ex->size() == (size_t)N);
     // the reference's DMA-issue variants of expand_RLWE give the same RLWEs

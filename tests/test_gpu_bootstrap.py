@@ -207,3 +207,22 @@ def test_large_and_ragged_batches(F, ctx0, keys0, count, group):
     want, failed = keys0.oracle.eval_bootstrap_batch(c1[idx], c2[idx], g[idx], keys0.btkey, keys0.kskey)
     assert failed == 0
     assert np.array_equal(out[idx], want)
+
+
+def test_verify_keys(F, ctx0, keys0):
+    """Read-back verification (dma_read_compare_bootstrap_key,
+    myfpga.cpp:772-851): the resident bootstrap key compares equal to the key
+    it was uploaded from; a copy with one word changed, early or late in the
+    device order, does not; a context without a key reports it."""
+    assert ctx0.verify_bootstrap_key(keys0.btkey)
+    for at in (5, keys0.btkey.size - 17):
+        keys0.btkey[at] ^= 1   # in place, restored below
+        try:
+            assert not ctx0.verify_bootstrap_key(keys0.btkey)
+        finally:
+            keys0.btkey[at] ^= 1
+    assert ctx0.verify_bootstrap_key(keys0.btkey)
+    with F.Context(keys0.P, 0) as fresh:
+        with pytest.raises(F.FheaccError) as e:
+            fresh.verify_bootstrap_key(keys0.btkey)
+        assert e.value.code == F.ENOKEY

@@ -328,3 +328,21 @@ def test_reference_fixture_wide(F, ctx1, keys1, cuda_ok):
     assert digest(f1, f2) == fx["full_inputs_sha256"].item().decode()
     fout = ctx1.eval_bootstrap_batch(f1, f2, fg)
     assert np.array_equal(fout, fx["full_out"].astype(np.uint64))
+
+
+def test_wide_verify_keys(F, ctx1, keys1, cuda_ok):
+    """Read-back verification at N = 2048 (keys held as Shoup pairs made on
+    the GPU): the resident bootstrap and substitute keys compare equal to the
+    keys they were uploaded from, and a copy with one word changed does not."""
+    assert ctx1.verify_bootstrap_key(keys1.btkey)
+    keys1.btkey[11] ^= 1   # in place (the key is 11.4 GB), restored below
+    try:
+        assert not ctx1.verify_bootstrap_key(keys1.btkey)
+    finally:
+        keys1.btkey[11] ^= 1
+    assert ctx1.verify_bootstrap_key(keys1.btkey)
+    ctx1.upload_subs_key(keys1.subs)
+    assert ctx1.verify_subs_key(keys1.subs)
+    bad_subs = keys1.subs.copy()
+    bad_subs[-3] ^= 1
+    assert not ctx1.verify_subs_key(bad_subs)
