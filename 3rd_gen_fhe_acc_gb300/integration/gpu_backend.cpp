@@ -18,6 +18,7 @@ constexpr int kSlots = 16;
 
 struct Slot {
     fheacc_ctx *ctx = nullptr;
+    const RLWE::bootstrap_key *bt = nullptr;  // eval_bootstrap's key object on the device (nullptr: uploaded by dma_write)
     const LWE::keyswitch_key *ks = nullptr;   // the key switch key on the device
     uint64_t *d_enc_sec = nullptr;            // RGSW(-s) of dma_write_RGSW_enc_sk
     bool subs = false;
@@ -236,7 +237,24 @@ int dma_write_bootstrap_key(const int slot_id, const RLWE::bootstrap_key &bt_key
     Slot *s = slot_of(slot_id);
     if (!s) return -1;
     const std::vector<uint64_t> w = flat_bootstrap_key(bt_key);
+    s->bt = nullptr;
     return fpga_rc(fheacc_upload_bootstrap_key(s->ctx, w.data(), w.size()));
+}
+
+LWE::LWE_ciphertext eval_bootstrap(const LWE::LWE_ciphertext &c1, const LWE::LWE_ciphertext &c2,
+                                   const RLWE::bootstrap_key &btkey, const LWE::keyswitch_key &kskey, const GATES gate)
+{
+    int sid = 0;
+    while (sid < kSlots && !slot_of(sid)) sid++;
+    if (sid == kSlots) return LWE::LWE_ciphertext();
+    Slot *s = slot_of(sid);
+    if (s->bt != &btkey) {
+        if (dma_write_bootstrap_key(sid, btkey) != 0) return LWE::LWE_ciphertext();
+        s->bt = &btkey;
+    }
+    int rc = 0;
+    std::vector<LWE::LWE_ciphertext> out = bootstrap({c1}, {c2}, kskey, {gate}, 1, &rc);
+    return rc == 0 ? out[0] : LWE::LWE_ciphertext();
 }
 
 int dma_write_subs_key(const int slot_id, const application::substitute_key &subs_key)

@@ -87,6 +87,15 @@ std::vector<LWE::LWE_ciphertext> fpga_eval_bootstrap_x16(const std::vector<LWE::
                                                          const std::vector<GATES> gate,
                                                          const pci_bar_handle_t ocl_bar_handle, int *rc, int read_fd);
 
+// RLWE::eval_bootstrap (RLWE.cpp:726-786) with its own signature, for code
+// that called the CPU path: on the lowest configured slot, uploading btkey
+// the first time this key object is passed (and again when another one is)
+// and the key switch key as the calls above do. c1 == c2, which the CPU path
+// answers with exit(1), and device errors return a default-constructed
+// (all-zero) ciphertext, as the FPGA calls do.
+LWE::LWE_ciphertext eval_bootstrap(const LWE::LWE_ciphertext &c1, const LWE::LWE_ciphertext &c2,
+                                   const RLWE::bootstrap_key &btkey, const LWE::keyswitch_key &kskey, const GATES gate);
+
 // expand_RLWE on the device (myfpga.cpp:1662-1790): N RLWEs, result[i] =
 // RLWE(N b_i X^i) for the input RLWE(sum b_i X^i) in the NTT domain. Needs
 // dma_write_subs_key. NULL and *rc != 0 on failure.

@@ -217,6 +217,16 @@ int main()
     CHECK(rc == 0);
     check_decrypts(lsk, {o1}, {g[5]}, {x[5]}, {y[5]});
     check_same({c1[5]}, {c2[5]}, {g[5]}, {o1}, 0);
+    // the RLWE::eval_bootstrap-compatible call: the same words as the CPU-order x1
+    LWE::LWE_ciphertext oe = GPU::eval_bootstrap(c1[5], c2[5], bk, kk, g[5]);
+    check_same({c1[5]}, {c2[5]}, {g[5]}, {oe}, 0);
+    {
+        // c1 == c2: a default-constructed (all-zero) ciphertext, as the FPGA calls return on error
+        const LWE::LWE_ciphertext z = GPU::eval_bootstrap(c1[5], c1[5], bk, kk, g[5]);
+        bool zero = z.b == 0;
+        for (int i = 0; i < n; i++) zero = zero && z.a[i] == 0;
+        CHECK(zero);
+    }
     GPU::set_issue_flags(FHEACC_FLAG_FPGA_X1);
     LWE::LWE_ciphertext o1x = GPU::fpga_eval_bootstrap_x1(c1[5], c2[5], kk, g[5], bar, &rc, -1);
     CHECK(rc == 0);
