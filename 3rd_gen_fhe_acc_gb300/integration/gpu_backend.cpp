@@ -478,6 +478,75 @@ std::shared_ptr<std::vector<RLWE::RGSW_ciphertext>> fpga_homo_expand(
     return result;
 }
 
+namespace {
+
+// The lowest configured slot and its index (nullptr if none), with that
+// device made current for the duration of a call.
+struct SlotCall {
+    Slot *s = nullptr;
+    int prev = 0;
+    SlotCall()
+    {
+        int sid = 0;
+        while (sid < kSlots && !slot_of(sid)) sid++;
+        if (sid == kSlots) return;
+        s = slot_of(sid);
+        cudaGetDevice(&prev);
+        cudaSetDevice(sid);
+    }
+    ~SlotCall()
+    {
+        if (s) cudaSetDevice(prev);
+        cudaGetLastError();
+    }
+};
+
+}  // namespace
+
+RLWE::RLWE_ciphertext CMUX(const RLWE::RLWE_ciphertext &c0, const RLWE::RLWE_ciphertext &c1,
+                           const RLWE::RGSW_ciphertext &SEL)
+{
+    SlotCall sc;
+    if (!sc.s || !c0.NTT_form || !c1.NTT_form) return RLWE::RLWE_ciphertext();
+    const size_t rw = 2 * (size_t)N, gw = (size_t)digitG * 4 * N;
+    std::vector<uint64_t> in(2 * rw), sel(gw), out(rw);
+    flat_rlwe(c0, in.data());
+    flat_rlwe(c1, in.data() + rw);
+    flat_rgsw(SEL, sel.data());
+    DevBuf din(2 * rw), dsel(gw), dout(rw);
+    cudaError_t e = din.e != cudaSuccess ? din.e : dsel.e != cudaSuccess ? dsel.e : dout.e;
+    if (e == cudaSuccess) e = cudaMemcpy(din.p, in.data(), in.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dsel.p, sel.data(), gw * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    int r = e == cudaSuccess ? fheacc_cmux_async(sc.s->ctx, din.p, din.p + rw, rw, dsel.p, 1, dout.p, 1, nullptr) : FHEACC_EIO;
+    if (r == FHEACC_OK) r = fheacc_sync(sc.s->ctx, 0);
+    if (r == FHEACC_OK && cudaMemcpy(out.data(), dout.p, rw * sizeof(uint64_t), cudaMemcpyDeviceToHost) != cudaSuccess)
+        r = FHEACC_EIO;
+    return r == FHEACC_OK ? rlwe_of(out.data()) : RLWE::RLWE_ciphertext();
+}
+
+RLWE::RLWE_ciphertext blind_rotate(const RLWE::RLWE_ciphertext &c_in, const bool forward,
+                                   const std::vector<RLWE::RGSW_ciphertext> &C)
+{
+    SlotCall sc;
+    if (!sc.s || C.size() != (size_t)digitN) return RLWE::RLWE_ciphertext();
+    const size_t rw = 2 * (size_t)N, gw = (size_t)digitG * 4 * N;
+    std::vector<uint64_t> in(rw), rg(gw * C.size()), out(rw);
+    flat_rlwe(c_in, in.data());
+    for (size_t i = 0; i < C.size(); i++) flat_rgsw(C[i], &rg[i * gw]);
+    DevBuf din(rw), drg(rg.size()), dout(rw);
+    cudaError_t e = din.e != cudaSuccess ? din.e : drg.e != cudaSuccess ? drg.e : dout.e;
+    if (e == cudaSuccess) e = cudaMemcpy(din.p, in.data(), rw * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(drg.p, rg.data(), rg.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    int r = e == cudaSuccess ? FHEACC_OK : FHEACC_EIO;
+    // the CPU path moves the input to the NTT domain first (RLWE.cpp:830)
+    if (r == FHEACC_OK && !c_in.NTT_form) r = fheacc_ntt_forward(sc.s->ctx, din.p, 2, nullptr);
+    if (r == FHEACC_OK) r = fheacc_rlwe_blind_rotate_async(sc.s->ctx, din.p, drg.p, forward ? 1 : 0, dout.p, 1, nullptr);
+    if (r == FHEACC_OK) r = fheacc_sync(sc.s->ctx, 0);
+    if (r == FHEACC_OK && cudaMemcpy(out.data(), dout.p, rw * sizeof(uint64_t), cudaMemcpyDeviceToHost) != cudaSuccess)
+        r = FHEACC_EIO;
+    return r == FHEACC_OK ? rlwe_of(out.data()) : RLWE::RLWE_ciphertext();
+}
+
 void set_issue_flags(uint32_t flags) { g_flags = flags & (FHEACC_FLAG_FPGA_COMPAT | FHEACC_FLAG_FPGA_X1); }
 
 fheacc_ctx *context(const int slot_id)

@@ -117,6 +117,17 @@ std::shared_ptr<std::vector<RLWE::RGSW_ciphertext>> fpga_homo_expand(
     const std::unique_ptr<std::vector<RLWE::RLWE_ciphertext>> &packed_bits, const pci_bar_handle_t ocl_bar_handle,
     int *rc, int read_fd, int write_fd);
 
+// The PSI operations the reference runs on the CPU (RLWE::CMUX and
+// RLWE::blind_rotate, RLWE.cpp:788-793 and 824-838), with their signatures,
+// on the lowest configured slot: CMUX of NTT-domain RLWEs; blind_rotate with
+// log2 N RGSWs (num_rotate_poly, params.h), its input moved to the NTT domain
+// first as the CPU path does. An error returns a default-constructed
+// ciphertext where the CPU path would exit(1).
+RLWE::RLWE_ciphertext CMUX(const RLWE::RLWE_ciphertext &c0, const RLWE::RLWE_ciphertext &c1,
+                           const RLWE::RGSW_ciphertext &SEL);
+RLWE::RLWE_ciphertext blind_rotate(const RLWE::RLWE_ciphertext &c_in, const bool forward,
+                                   const std::vector<RLWE::RGSW_ciphertext> &C);
+
 // Not in the FPGA API: the issue order of the bootstrap calls (0, the
 // default: the CPU path's; FHEACC_FLAG_FPGA_X1 or FHEACC_FLAG_FPGA_COMPAT),
 // the context of a slot for direct use of the C ABI, and its release.

@@ -1,7 +1,7 @@
 // Drives the GPU:: backend (3rd_gen_fhe_acc_gb300/integration/gpu_backend.cpp)
 // the way the runtime's FPGA tests drive FPGA:: (test.cpp:2013-3538):
 // configure slot 0 from the runtime's globals, upload and read back the keys,
-// bootstrap through the fixed-width calls, expand. Keys and ciphertexts come from
+// bootstrap through the fixed-width calls, expand, CMUX and blind-rotate. Keys and ciphertexts come from
 // libfheacc's seeded host generator; every bootstrap output is decrypted and
 // compared word for word with libfheacc's own host-buffer call, and the expand
 // outputs with the C ABI's device calls. Built against the runtime's headers
@@ -288,6 +288,36 @@ int main()
                     const RLWE::RLWE_ciphertext &c = (*he)[i].c_text[h][r];
                     for (int k = 0; k < N; k++) CHECK(c.a[k] == w[k] && c.b[k] == w[N + k]);
                 }
+        // CMUX and blind_rotate with the RLWE:: signatures, against the C ABI's
+        // device calls on the same words; a time-domain input of blind_rotate
+        // gives what its NTT-domain form gives
+        const RLWE::RLWE_ciphertext c0 = rlwe_of(&packed[0]), c1 = rlwe_of(&packed[rw]);
+        const RLWE::RGSW_ciphertext sel = rgsw_of(rgsw.data());
+        const RLWE::RLWE_ciphertext mux = GPU::CMUX(c0, c1, sel);
+        CHECK(fheacc_cmux_async(GPU::context(0), d_in, d_in + rw, rw, d_sec, 1, d_out, 1, nullptr) == FHEACC_OK);
+        CHECK(fheacc_sync(GPU::context(0), 0) == FHEACC_OK);
+        CHECK(cudaMemcpy(want.data(), d_out, rw * 8, cudaMemcpyDeviceToHost) == cudaSuccess);
+        for (int k = 0; k < N; k++) CHECK(mux.a[k] == want[k] && mux.b[k] == want[N + k]);
+        std::vector<RLWE::RGSW_ciphertext> ctl(digitN, sel);
+        uint64_t *d_ctl = nullptr;
+        CHECK(cudaMalloc(&d_ctl, gw * digitN * 8) == cudaSuccess);
+        for (int i = 0; i < digitN; i++)
+            CHECK(cudaMemcpy(d_ctl + i * gw, rgsw.data(), gw * 8, cudaMemcpyHostToDevice) == cudaSuccess);
+        const RLWE::RLWE_ciphertext rot = GPU::blind_rotate(c0, true, ctl);
+        CHECK(fheacc_rlwe_blind_rotate_async(GPU::context(0), d_in, d_ctl, 1, d_out, 1, nullptr) == FHEACC_OK);
+        CHECK(fheacc_sync(GPU::context(0), 0) == FHEACC_OK);
+        CHECK(cudaMemcpy(want.data(), d_out, rw * 8, cudaMemcpyDeviceToHost) == cudaSuccess);
+        for (int k = 0; k < N; k++) CHECK(rot.a[k] == want[k] && rot.b[k] == want[N + k]);
+        CHECK(fheacc_ntt_inverse(GPU::context(0), d_in, 2, nullptr) == FHEACC_OK);   // c0 to the time domain
+        CHECK(fheacc_sync(GPU::context(0), 0) == FHEACC_OK);
+        std::vector<uint64_t> t0(rw);
+        CHECK(cudaMemcpy(t0.data(), d_in, rw * 8, cudaMemcpyDeviceToHost) == cudaSuccess);
+        RLWE::RLWE_ciphertext c0t = rlwe_of(t0.data());
+        c0t.NTT_form = false;
+        const RLWE::RLWE_ciphertext rot_t = GPU::blind_rotate(c0t, true, ctl);
+        for (int k = 0; k < N; k++) CHECK(rot_t.a[k] == rot.a[k] && rot_t.b[k] == rot.b[k]);
+        CHECK(GPU::blind_rotate(c0, true, std::vector<RLWE::RGSW_ciphertext>(digitN - 1, sel)).a[0] == 0);
+        cudaFree(d_ctl);
         cudaFree(d_in);
         cudaFree(d_out);
         cudaFree(d_sec);
